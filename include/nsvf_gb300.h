@@ -1,0 +1,153 @@
+/*
+ * nsvf_gb300 -- C ABI of the GB300-native (sm_103a) sparse-voxel rendering
+ * hot path of NSVF (facebookresearch/NSVF, package `fairnr`).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as `void *`, a cudaStream_t), launches asynchronously on that
+ * stream, allocates nothing unless stated, and returns an int status
+ * (NSVF_OK or a negative NSVF_ERR_*). None of them exits the process: the
+ * reference's CUDA_CHECK_ERRORS calls exit(-1) on a launch error
+ * (fairnr/clib/include/cuda_utils.h:35-44).
+ *
+ * Layouts are row-major and contiguous; "[b, m, 3]" means b*m*3 elements.
+ *
+ * Floating point: geometry ops compute in FP32 with the reference's
+ * operation order and its fused multiply-adds (nvcc contracts `a + b * c` by
+ * default); the one deliberate difference is the ray reciprocal 1/dir, which
+ * the reference takes with the approximate __fdividef and this library with
+ * the correctly rounded __frcp_rn, so results are reproducible bit for bit on
+ * a CPU.
+ */
+#ifndef NSVF_GB300_H
+#define NSVF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSVF_OK 0
+#define NSVF_ERR_INVALID (-1)   /* bad sizes or null pointers */
+#define NSVF_ERR_CUDA (-2)      /* a CUDA launch or API call failed */
+#define NSVF_ERR_OCTREE (-3)    /* malformed octree (host validation) */
+#define NSVF_ERR_CAPACITY (-4)  /* an output buffer is too small */
+
+/* Human-readable text for a status code. */
+const char *nsvf_status_string(int status);
+
+/* ------------------------------------------------------------------------ */
+/* Ray-voxel intersection (fairnr/clib/include/intersect.h:10-17)            */
+
+/* aabb_intersect: replaces `aabb_intersect(ray_start, ray_dir, points,
+ * voxelsize, n_max)` (fairnr/clib/src/intersect.cpp:49-75,
+ * fairnr/clib/src/intersect_gpu.cu:125-167).
+ * ray_start, ray_dir [b, m, 3]; points [b_pts, n, 3] with b_pts == b or 1
+ * (1 = one voxel set shared by all b ray batches; the reference copies it b
+ * times). Each ray tests voxels 0..n-1 in index order and keeps its first
+ * n_max hits. Outputs [b, m, n_max]: idx (int32, -1 = none), min_depth and
+ * max_depth (FP32, 0 = none). */
+int nsvf_aabb_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_max,
+                        const float *ray_start, const float *ray_dir, const float *points,
+                        int32_t *idx, float *min_depth, float *max_depth, void *stream);
+
+/* svo_intersect: replaces `svo_intersect(ray_start, ray_dir, points,
+ * children, voxelsize, n_max)` (fairnr/clib/src/intersect.cpp:84-112,
+ * fairnr/clib/src/intersect_gpu.cu:170-237).
+ * points [b_pts, n, 3] node centres, children [b_pts, n, 9] int32 (8 child
+ * ids or -1, then the node size in leaf units: 1 for a leaf); the root is row
+ * n-1. Rays traverse the octree depth first, visiting children 7..0, and keep
+ * the first n_max leaves hit, in that order. Outputs as aabb_intersect.
+ * `workspace` is device memory of nsvf_svo_workspace_bytes(b_pts, n) bytes,
+ * 16-byte aligned, used for a packed copy of the octree (it may be reused for
+ * the next call only after this call's kernels have finished). `err` (device
+ * int, may be NULL) gets bit 0 set if the octree is malformed (a child id
+ * outside [0, n), a cycle, or deeper than 36 levels); such rays stop early
+ * instead of reading out of bounds (the reference asserts or faults). */
+int64_t nsvf_svo_workspace_bytes(int b_pts, int n);
+int nsvf_svo_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_max,
+                       const float *ray_start, const float *ray_dir, const float *points,
+                       const int32_t *children, int32_t *idx, float *min_depth,
+                       float *max_depth, int32_t *err, void *workspace, void *stream);
+
+/* svo_intersect_sorted: svo_intersect followed by the encoder's
+ * post-processing (fairnr/modules/encoder.py:518-524) in the same kernel:
+ * missing slots get depth 10000 (MAX_DEPTH), each ray's n_max slots are
+ * sorted by min_depth (stable: ties keep traversal order), and hits[b*m]
+ * (uint8) is 1 where a ray hit any voxel. n_max <= 128. */
+int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, int n_max,
+                              const float *ray_start, const float *ray_dir, const float *points,
+                              const int32_t *children, int32_t *idx, float *min_depth,
+                              float *max_depth, uint8_t *hits, int32_t *err, void *workspace,
+                              void *stream);
+
+/* ball_intersect: replaces `ball_intersect(ray_start, ray_dir, points,
+ * radius, n_max)` (fairnr/clib/src/intersect.cpp:15-41). Rays vs spheres of
+ * `radius` around each point; first n_max hits in point order. */
+int nsvf_ball_intersect(int b, int b_pts, int n, int m, float radius, int n_max,
+                        const float *ray_start, const float *ray_dir, const float *points,
+                        int32_t *idx, float *min_depth, float *max_depth, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Sample placement (fairnr/clib/include/sample.h:11-16)                     */
+
+/* uniform_ray_sampling: replaces `uniform_ray_sampling(pts_idx, min_depth,
+ * max_depth, uniform_noise, step_size, max_steps)`
+ * (fairnr/clib/src/sample.cpp:23-55, fairnr/clib/src/sample_gpu.cu:15-106).
+ * pts_idx/min_depth/max_depth [b, m, max_hits], noise [b, m, max_steps];
+ * outputs sampled_idx (int32, -1 pad), sampled_depth, sampled_dists
+ * [b, m, max_steps], fully written. `err` (device int, may be NULL) gets
+ * bit 1 set if a ray needed more than max_steps slots (the reference writes
+ * past its row there). */
+int nsvf_uniform_ray_sampling(int b, int m, int max_hits, int max_steps, float step_size,
+                              const int32_t *pts_idx, const float *min_depth,
+                              const float *max_depth, const float *noise, int32_t *sampled_idx,
+                              float *sampled_depth, float *sampled_dists, int32_t *err,
+                              void *stream);
+
+/* inverse_cdf_sampling: replaces `inverse_cdf_sampling(pts_idx, min_depth,
+ * max_depth, uniform_noise, probs, steps, fixed_step_size)`
+ * (fairnr/clib/src/sample.cpp:58-96, fairnr/clib/src/sample_gpu.cu:108-202).
+ * pts_idx/min_depth/max_depth/probs [rows, max_hits], steps [rows], noise
+ * [rows, noise_stride] (noise_stride >= max_steps), outputs [rows, max_steps].
+ * `noise` may be NULL: every jitter is then 0.5 (the reference's
+ * deterministic mode fills a tensor with 0.5).
+ *
+ * Two reads of the reference leave the ray's row and depend on how the rays
+ * were blocked into kernel launches (fairnr/clib/src/sample_gpu.cu:189, 194);
+ * `layout` reproduces them:
+ *   layout[0] = K (rays per block), layout[1] = chunk (rays of a block per
+ *   launch), layout[2] = N (real rays; rows >= N are padding copies of row
+ *   0), layout[3] = G (blocks).
+ * For the raw op on [b, m, H] tensors pass {m, m, b*m, b}; for the
+ * reference's InverseCDFRaySampling wrapper over N rays pass
+ * {ceil(N/200), 800, N, 200} (fairnr/clib/__init__.py:234-270).
+ * `max_len` (device int, may be NULL) receives atomically the largest number
+ * of non -1 ids over the rows (the wrapper's truncation width); `err` bit 1
+ * is set if a ray needed more than max_steps slots or noise columns. */
+int nsvf_inverse_cdf_sampling(int64_t rows, int max_hits, int max_steps, int noise_stride,
+                              float fixed_step_size, const int32_t *pts_idx,
+                              const float *min_depth, const float *max_depth, const float *noise,
+                              const float *probs, const float *steps, const int64_t layout[4],
+                              int32_t *sampled_idx, float *sampled_depth, float *sampled_dists,
+                              int32_t *max_len, int32_t *err, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Octree build (fairnr/clib/include/octree.h:10)                            */
+
+/* build_octree: replaces `build_octree(center, points, depth)`
+ * (fairnr/clib/src/octree.cpp:125-136). HOST function on host memory.
+ * center[3] (float), points [n_points, 3] int64 (integer half-voxel
+ * coordinates), depth. Writes up to `capacity` rows of centers [., 3] and
+ * children [., 9] (int32) and returns the node count, or a negative status
+ * (NSVF_ERR_CAPACITY if capacity is too small: call again with more room).
+ * Numbering as the reference: leaves keep their point index 0..n_points-1,
+ * internal nodes count down from n_nodes-1 (the root) in breadth-first order;
+ * children[., 8] = 1 << (node depth + 1); centres truncated to int. */
+int64_t nsvf_build_octree(const float center[3], const int64_t *points, int64_t n_points,
+                          int depth, int32_t *centers, int32_t *children, int64_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSVF_GB300_H */

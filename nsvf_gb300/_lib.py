@@ -1,0 +1,62 @@
+"""Loader of the C-ABI library (nsvf_gb300/_build/libnsvf_gb300.so).
+
+The library is the product: there is no CPU or PyTorch fallback. If it is
+missing, importing this module raises, naming the build command.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libnsvf_gb300.so")
+
+NSVF_OK = 0
+
+
+class NsvfError(RuntimeError):
+    pass
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            "nsvf_gb300: %s is missing; build it with `python -m nsvf_gb300.build` "
+            "(or __graft_entry__.build())" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    P, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+    sig = {
+        "nsvf_status_string": ([i32], ctypes.c_char_p),
+        "nsvf_aabb_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P], i32),
+        "nsvf_svo_workspace_bytes": ([i32, i32], i64),
+        "nsvf_svo_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P, P, P, P], i32),
+        "nsvf_svo_intersect_sorted": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P, P, P,
+                                       P, P], i32),
+        "nsvf_ball_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P], i32),
+        "nsvf_uniform_ray_sampling": ([i32, i32, i32, i32, f32, P, P, P, P, P, P, P, P, P], i32),
+        "nsvf_inverse_cdf_sampling": ([i64, i32, i32, i32, f32, P, P, P, P, P, P, P, P, P, P,
+                                       P, P, P], i32),
+        "nsvf_build_octree": ([P, P, i64, i32, P, P, i64], i64),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+LIB = _load()
+
+
+def check(status, what):
+    if status != NSVF_OK:
+        msg = LIB.nsvf_status_string(int(status)).decode()
+        raise NsvfError("nsvf_gb300: %s failed: %s (%d)" % (what, msg, status))
+    return status
+
+
+def exported_symbols():
+    """Names declared in include/nsvf_gb300.h that the library must export."""
+    return [
+        "nsvf_status_string", "nsvf_aabb_intersect", "nsvf_svo_workspace_bytes",
+        "nsvf_svo_intersect", "nsvf_svo_intersect_sorted", "nsvf_ball_intersect",
+        "nsvf_uniform_ray_sampling", "nsvf_inverse_cdf_sampling", "nsvf_build_octree",
+    ]

@@ -1,0 +1,58 @@
+// Shared device helpers for the nsvf_gb300 kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nsvf_gb300.h"
+
+#define NSVF_MAX_DEPTH_F 10000.0f
+
+// Launch-status helper: every entry point returns an int status, never exits.
+static inline int nsvf_launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NSVF_OK : NSVF_ERR_CUDA;
+}
+
+static inline int nsvf_grid(int64_t work, int block) {
+  int64_t g = (work + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > 0x7fffffff) g = 0x7fffffff;
+  return (int)g;
+}
+
+// Slab test of a ray (origin o, reciprocal direction inv) against the cube of
+// centre c and half size h. Same operations, in the same order, as the
+// reference's RayAABBIntersection (fairnr/clib/src/intersect_gpu.cu:73-122):
+// per axis two subtractions and one product per bound, a swap, then the
+// running max/min with t starting in [0, 1e5]. The reference exits early when
+// an axis already separates; the running interval only shrinks, so testing
+// lo > hi once at the end gives the same verdict and the same (lo, hi).
+// Comparisons with NaN are false, so a NaN axis leaves the interval unchanged.
+__device__ __forceinline__ bool nsvf_slab(float ox, float oy, float oz, float ix, float iy,
+                                          float iz, float cx, float cy, float cz, float h,
+                                          float &t_lo, float &t_hi) {
+  float lo = 0.0f, hi = 100000.0f;
+  float l, u;
+  l = __fmul_rn(__fsub_rn(__fsub_rn(cx, h), ox), ix);
+  u = __fmul_rn(__fsub_rn(__fadd_rn(cx, h), ox), ix);
+  if (u < l) { float t = l; l = u; u = t; }
+  lo = (l > lo) ? l : lo;
+  hi = (u < hi) ? u : hi;
+  l = __fmul_rn(__fsub_rn(__fsub_rn(cy, h), oy), iy);
+  u = __fmul_rn(__fsub_rn(__fadd_rn(cy, h), oy), iy);
+  if (u < l) { float t = l; l = u; u = t; }
+  lo = (l > lo) ? l : lo;
+  hi = (u < hi) ? u : hi;
+  l = __fmul_rn(__fsub_rn(__fsub_rn(cz, h), oz), iz);
+  u = __fmul_rn(__fsub_rn(__fadd_rn(cz, h), oz), iz);
+  if (u < l) { float t = l; l = u; u = t; }
+  lo = (l > lo) ? l : lo;
+  hi = (u < hi) ? u : hi;
+  t_lo = lo;
+  t_hi = hi;
+  return !(lo > hi);
+}
+
+// Correctly rounded reciprocal (the reference uses the approximate
+// __fdividef(1, d); see the note in include/nsvf_gb300.h).
+__device__ __forceinline__ float nsvf_rcp(float d) { return __frcp_rn(d); }

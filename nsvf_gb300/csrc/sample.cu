@@ -1,0 +1,209 @@
+// Sample placement inside the hit intervals: inverse-CDF (the sampler NSVF
+// uses) and the three-way-merge uniform sampler.
+//
+// Reference behaviour: fairnr/clib/src/sample_gpu.cu:15-202 and
+// fairnr/clib/src/sample.cpp:23-96. FP32 with the reference's operation order;
+// `a + b * c` is written as __fmaf_rn where nvcc contracts it in the
+// reference build (this file is compiled with -fmad=false so that no other
+// contraction happens).
+#include "common.cuh"
+
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ void warp_max_atomic(int32_t *dst, int v, bool live) {
+  unsigned mask = __activemask();
+  int x = live ? v : 0;
+  for (int o = 16; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(mask, x, o));
+  if ((threadIdx.x & 31) == (__ffs(mask) - 1) && dst) atomicMax(dst, x);
+}
+
+// One thread walks one ray's piecewise-uniform CDF over its hit intervals
+// (fairnr/clib/src/sample_gpu.cu:108-202).
+__global__ void __launch_bounds__(kBlock) inverse_cdf_kernel(
+    int64_t rows, int H, int M, int noise_stride, float fixed_step_size,
+    const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
+    const float *__restrict__ max_depth, const float *__restrict__ noise,
+    const float *__restrict__ probs, const float *__restrict__ steps, int64_t K, int64_t C,
+    int64_t N, int64_t G, int32_t *__restrict__ s_idx, float *__restrict__ s_depth,
+    float *__restrict__ s_dist, int32_t *__restrict__ max_len, int32_t *__restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  bool live = r < rows;
+  int valid = 0;
+  if (live) {
+    // Rows the reference reads outside this ray (see include/nsvf_gb300.h).
+    int64_t g = r / K, i = r % K;
+    int64_t c0 = (i / C) * C, W = min(C, K - c0), ii = i - c0;
+    int64_t tail = g * K + c0;
+    if (tail >= N) tail = 0;
+    int64_t nxt;
+    if (ii + 1 < W) nxt = r + 1;
+    else nxt = (g + 1 < G) ? (g + 1) * K + c0 : -1;
+    if (nxt >= N) nxt = 0;
+
+    const int32_t *I = pts_idx + r * H;
+    const int32_t *I0 = pts_idx + tail * H;
+    const float *lo = min_depth + r * H, *hi = max_depth + r * H, *pr = probs + r * H;
+    const float *U = noise ? noise + r * noise_stride : nullptr;
+    int32_t *SI = s_idx + r * M;
+    float *SD = s_depth + r * M, *SS = s_dist + r * M;
+
+    int bin = 0, s = 0;
+    float cmin = lo[0], cmax = hi[0];
+    float cdf_lo = 0.0f, cdf_hi = pr[0];
+    float step_size = __double2float_rn(__ddiv_rn(1.0, (double)steps[r]));
+    float z_low = cmin;
+    int total_steps = (int)ceilf(steps[r]);
+    bool done = false, overflow = false;
+    if (fixed_step_size > 0.0f) step_size = fixed_step_size;
+
+    for (int st = 0; st < total_steps; ++st) {
+      if (st >= noise_stride && U) { overflow = true; break; }
+      float u0 = U ? U[st] : 0.5f;
+      float cdf = __fmul_rn(__fadd_rn((float)st, u0), step_size);
+      while (cdf > cdf_hi) {
+        if (s >= M) { overflow = true; break; }
+        int32_t id = I[bin];
+        SI[s] = id; SS[s] = __fsub_rn(cmax, z_low);
+        SD[s] = __fmul_rn(__fadd_rn(cmax, z_low), 0.5f);
+        valid += (id != -1);
+        bin++; s++;
+        if (bin >= H || I[bin] == -1) { done = true; break; }
+        cmin = lo[bin]; cmax = hi[bin];
+        cdf_lo = cdf_hi;
+        cdf_hi = __fadd_rn(cdf_hi, pr[bin]);
+        z_low = cmin;
+      }
+      if (done || overflow) break;
+      if (s >= M) { overflow = true; break; }
+      float u = __fdiv_rn(__fsub_rn(cdf, cdf_lo), __fsub_rn(cdf_hi, cdf_lo));
+      float z = __fmaf_rn(u, __fsub_rn(cmax, cmin), cmin);
+      int32_t id = I[bin];
+      SI[s] = id; SS[s] = __fsub_rn(z, z_low); SD[s] = __fmul_rn(__fadd_rn(z, z_low), 0.5f);
+      valid += (id != -1);
+      z_low = z; s++;
+    }
+    // Tail: the reference runs it even after `done` (`~done` is always true),
+    // re-emitting the last partial segment; with bin == H it reads the first
+    // id of the next row in memory, and it tests emptiness on the block's
+    // first row (fairnr/clib/src/sample_gpu.cu:188-201).
+    while (!overflow && z_low < cmax) {
+      if (s >= M) { overflow = true; break; }
+      int32_t id;
+      if (bin < H) id = I[bin];
+      else id = (nxt >= 0) ? pts_idx[nxt * H] : -1;
+      SI[s] = id; SS[s] = __fsub_rn(cmax, z_low);
+      SD[s] = __fmul_rn(__fadd_rn(cmax, z_low), 0.5f);
+      valid += (id != -1);
+      bin++; s++;
+      if (bin >= H || I0[bin] == -1) break;
+      cmin = lo[bin]; cmax = hi[bin];
+      z_low = cmin;
+    }
+    for (int q = s; q < M; ++q) { SI[q] = -1; SD[q] = 0.0f; SS[q] = 0.0f; }
+    if (overflow && err) atomicOr(err, 2);
+  }
+  warp_max_atomic(max_len, valid, live);
+}
+
+// Uniform sampler (fairnr/clib/src/sample_gpu.cu:15-106): merge interval
+// starts, interval ends and jittered steps into one sorted depth list in the
+// output row, then turn it into midpoints/lengths and keep those inside a
+// voxel, compacting in place.
+__global__ void __launch_bounds__(kBlock) uniform_kernel(
+    int64_t rows, int H, int M, float step_size, const int32_t *__restrict__ pts_idx,
+    const float *__restrict__ min_depth, const float *__restrict__ max_depth,
+    const float *__restrict__ noise, int32_t *__restrict__ s_idx, float *__restrict__ s_depth,
+    float *__restrict__ s_dist, int32_t *__restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (r >= rows) return;
+  const int32_t *I = pts_idx + r * H;
+  const float *lo = min_depth + r * H, *hi = max_depth + r * H;
+  const float *U = noise + r * M;
+  int32_t *SI = s_idx + r * M;
+  float *SD = s_depth + r * M, *SS = s_dist + r * M;
+  for (int q = 0; q < M; ++q) { SI[q] = -1; SD[q] = 0.0f; SS[q] = 0.0f; }
+
+  int s = 0, ucur = 0, umin = 0, umax = 0;
+  float lmin, lmax, cur = 0.0f;
+  bool overflow = false;
+  while (true) {
+    if (umax == H || ucur == M || I[umax] == -1) break;
+    if (s >= M) { overflow = true; break; }
+    lmin = (umin < H) ? lo[umin] : 10000.0f;
+    lmax = (umax < H) ? hi[umax] : 10000.0f;
+    cur = __fmaf_rn(__fadd_rn((float)ucur, U[ucur]), step_size, lo[0]);
+    if (lmax <= cur && lmax <= lmin) {
+      SD[s] = lmax; SI[s] = I[umax]; umax++; s++; continue;
+    }
+    if (cur <= lmin && cur <= lmax) {
+      // umin == 0 only for a jitter of exactly 0: the reference then reads the
+      // element before the row (the previous ray's last id).
+      int64_t off = r * H + umin - 1;
+      SD[s] = cur; SI[s] = (off >= 0) ? pts_idx[off] : -1; ucur++; s++; continue;
+    }
+    if (lmin <= cur && lmin <= lmax) {
+      SD[s] = lmin; SI[s] = I[umin]; umin++; s++; continue;
+    }
+    break;  // NaN input: the reference would spin here forever
+  }
+
+  int step = 0;
+  umin = 0; umax = 0;
+  for (ucur = 0; ucur < M - 1; ucur++) {
+    if (SI[ucur + 1] == -1) break;
+    float l = SD[ucur], rr = SD[ucur + 1];
+    SD[ucur] = __fmul_rn(__fadd_rn(l, rr), 0.5f);
+    SS[ucur] = __fsub_rn(rr, l);
+    if (umin < H && SD[ucur] >= lo[umin] && I[umin] > -1) umin++;
+    if (umax < H && SD[ucur] >= hi[umax] && I[umax] > -1) umax++;
+    if (umax == H || I[umax] == -1) break;
+    if (umin - 1 == umax && SS[ucur] > 0) {
+      SD[step] = SD[ucur]; SS[step] = SS[ucur]; SI[step] = SI[ucur]; step++;
+    }
+  }
+  for (int q = step; q < M; ++q) SI[q] = -1;
+  if (overflow && err) atomicOr(err, 2);
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsvf_inverse_cdf_sampling(int64_t rows, int max_hits, int max_steps, int noise_stride,
+                              float fixed_step_size, const int32_t *pts_idx,
+                              const float *min_depth, const float *max_depth, const float *noise,
+                              const float *probs, const float *steps, const int64_t layout[4],
+                              int32_t *sampled_idx, float *sampled_depth, float *sampled_dists,
+                              int32_t *max_len, int32_t *err, void *stream) {
+  if (rows < 0 || max_hits < 1 || max_steps < 1 || !layout || !pts_idx || !min_depth ||
+      !max_depth || !probs || !steps || !sampled_idx || !sampled_depth || !sampled_dists)
+    return NSVF_ERR_INVALID;
+  if (noise && noise_stride < 1) return NSVF_ERR_INVALID;
+  int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
+  if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
+  if (rows == 0) return NSVF_OK;
+  inverse_cdf_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      rows, max_hits, max_steps, noise_stride, fixed_step_size, pts_idx, min_depth, max_depth,
+      noise, probs, steps, K, C, N, G, sampled_idx, sampled_depth, sampled_dists, max_len, err);
+  return nsvf_launch_status();
+}
+
+int nsvf_uniform_ray_sampling(int b, int m, int max_hits, int max_steps, float step_size,
+                              const int32_t *pts_idx, const float *min_depth,
+                              const float *max_depth, const float *noise, int32_t *sampled_idx,
+                              float *sampled_depth, float *sampled_dists, int32_t *err,
+                              void *stream) {
+  if (b < 0 || m < 0 || max_hits < 1 || max_steps < 1 || !pts_idx || !min_depth || !max_depth ||
+      !noise || !sampled_idx || !sampled_depth || !sampled_dists)
+    return NSVF_ERR_INVALID;
+  int64_t rows = (int64_t)b * m;
+  if (rows == 0) return NSVF_OK;
+  uniform_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      rows, max_hits, max_steps, step_size, pts_idx, min_depth, max_depth, noise, sampled_idx,
+      sampled_depth, sampled_dists, err);
+  return nsvf_launch_status();
+}
+
+}  // extern "C"

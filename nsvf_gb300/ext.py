@@ -1,0 +1,249 @@
+"""Drop-in for the reference's native module ``fairnr.clib._ext``.
+
+Same function names, argument order, dtypes and output shapes as the
+pybind11 module of fairnr/clib/src/binding.cpp:11-20; each call launches the
+sm_103a kernels of libnsvf_gb300.so on the current CUDA stream. Precondition
+failures raise RuntimeError like the reference's TORCH_CHECKs
+(fairnr/clib/include/utils.h:10-30); a failed launch raises NsvfError instead
+of exiting the process.
+
+Kernel-detected input problems (a malformed octree, a noise tensor too short
+for the requested steps) are OR-ed into a per-device error word rather than
+trapping; ``check_errors()`` synchronises and raises if any was recorded.
+The sampling wrappers of nsvf_gb300.clib, which synchronise anyway for their
+output width, check it on every call.
+"""
+import torch
+
+from ._lib import LIB, check
+
+_err_words = {}
+
+
+def _stream(t):
+    return ctypes_stream(t.device)
+
+
+def ctypes_stream(device):
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def error_word(device):
+    """Per-device int32 error word the kernels OR their findings into."""
+    key = torch.device(device).index if torch.device(device).index is not None \
+        else torch.cuda.current_device()
+    w = _err_words.get(key)
+    if w is None:
+        w = torch.zeros(1, dtype=torch.int32, device=torch.device("cuda", key))
+        _err_words[key] = w
+    return w
+
+
+def check_errors(device=None):
+    """Raise if any kernel on `device` recorded an input error since the last check."""
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    w = error_word(dev)
+    v = int(w.item())
+    if v:
+        w.zero_()
+        what = []
+        if v & 1:
+            what.append("malformed octree (child id out of range, cycle or too deep)")
+        if v & 2:
+            what.append("a ray needed more sample slots than max_steps / noise columns")
+        raise RuntimeError("nsvf_gb300: " + "; ".join(what))
+
+
+def _ptr(t):
+    return t.data_ptr() if t is not None else None
+
+
+def _need(cond, msg):
+    if not cond:
+        raise RuntimeError(msg)
+
+
+def _check_cuda_contig(name, t):
+    _need(t.is_cuda, "%s must be a CUDA tensor" % name)
+    _need(t.is_contiguous(), "%s must be a contiguous tensor" % name)
+
+
+def _check_float(name, t):
+    _check_cuda_contig(name, t)
+    _need(t.dtype == torch.float32, "%s must be a float tensor" % name)
+
+
+def _check_int(name, t):
+    _check_cuda_contig(name, t)
+    _need(t.dtype == torch.int32, "%s must be an int tensor" % name)
+
+
+def _batch_pts(points, b):
+    bp = points.size(0)
+    _need(bp == b or bp == 1, "points batch (%d) must be 1 or match the ray batch (%d)" % (bp, b))
+    return bp
+
+
+def aabb_intersect(ray_start, ray_dir, points, voxelsize, n_max):
+    """fairnr/clib/src/intersect.cpp:49-75: -> (idx int32, min_depth, max_depth) [B, M, n_max]."""
+    for n, t in (("ray_start", ray_start), ("ray_dir", ray_dir), ("points", points)):
+        _check_float(n, t)
+    B, M = ray_start.shape[:2]
+    bp = _batch_pts(points, B)
+    N = points.size(1)
+    dev = ray_start.device
+    idx = torch.empty(B, M, n_max, dtype=torch.int32, device=dev)
+    lo = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    hi = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    check(LIB.nsvf_aabb_intersect(B, bp, N, M, float(voxelsize), int(n_max), _ptr(ray_start),
+                                  _ptr(ray_dir), _ptr(points), _ptr(idx), _ptr(lo), _ptr(hi),
+                                  _stream(ray_start)), "aabb_intersect")
+    return idx, lo, hi
+
+
+def _svo_workspace(bp, n, dev):
+    nbytes = int(LIB.nsvf_svo_workspace_bytes(bp, n))
+    return torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev)
+
+
+def svo_intersect(ray_start, ray_dir, points, children, voxelsize, n_max):
+    """fairnr/clib/src/intersect.cpp:84-112: -> (idx, min_depth, max_depth) [B, M, n_max]."""
+    for n, t in (("ray_start", ray_start), ("ray_dir", ray_dir), ("points", points)):
+        _check_float(n, t)
+    _check_int("children", children)
+    B, M = ray_start.shape[:2]
+    bp = _batch_pts(points, B)
+    N = points.size(1)
+    _need(children.shape[:2] == points.shape[:2] and children.size(2) == 9,
+          "children must be [B, N, 9] matching points")
+    dev = ray_start.device
+    idx = torch.empty(B, M, n_max, dtype=torch.int32, device=dev)
+    lo = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    hi = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    ws = _svo_workspace(bp, N, dev)
+    check(LIB.nsvf_svo_intersect(B, bp, N, M, float(voxelsize), int(n_max), _ptr(ray_start),
+                                 _ptr(ray_dir), _ptr(points), _ptr(children), _ptr(idx), _ptr(lo),
+                                 _ptr(hi), _ptr(error_word(dev)), _ptr(ws), _stream(ray_start)),
+          "svo_intersect")
+    return idx, lo, hi
+
+
+def svo_intersect_sorted(ray_start, ray_dir, points, children, voxelsize, n_max):
+    """svo_intersect plus the encoder's post-processing (fairnr/modules/encoder.py:518-524):
+    -> (idx, min_depth, max_depth) sorted by min_depth with misses at 10000, hits [B, M] bool."""
+    for n, t in (("ray_start", ray_start), ("ray_dir", ray_dir), ("points", points)):
+        _check_float(n, t)
+    _check_int("children", children)
+    _need(n_max <= 128, "sorted SVO intersection supports n_max <= 128")
+    B, M = ray_start.shape[:2]
+    bp = _batch_pts(points, B)
+    N = points.size(1)
+    dev = ray_start.device
+    idx = torch.empty(B, M, n_max, dtype=torch.int32, device=dev)
+    lo = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    hi = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    hits = torch.empty(B, M, dtype=torch.uint8, device=dev)
+    ws = _svo_workspace(bp, N, dev)
+    check(LIB.nsvf_svo_intersect_sorted(B, bp, N, M, float(voxelsize), int(n_max), _ptr(ray_start),
+                                        _ptr(ray_dir), _ptr(points), _ptr(children), _ptr(idx),
+                                        _ptr(lo), _ptr(hi), _ptr(hits), _ptr(error_word(dev)),
+                                        _ptr(ws), _stream(ray_start)), "svo_intersect_sorted")
+    return idx, lo, hi, hits.bool()
+
+
+def ball_intersect(ray_start, ray_dir, points, radius, n_max):
+    """fairnr/clib/src/intersect.cpp:15-41: -> (idx, min_depth, max_depth) [B, M, n_max]."""
+    for n, t in (("ray_start", ray_start), ("ray_dir", ray_dir), ("points", points)):
+        _check_float(n, t)
+    B, M = ray_start.shape[:2]
+    bp = _batch_pts(points, B)
+    N = points.size(1)
+    dev = ray_start.device
+    idx = torch.empty(B, M, n_max, dtype=torch.int32, device=dev)
+    lo = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    hi = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
+    check(LIB.nsvf_ball_intersect(B, bp, N, M, float(radius), int(n_max), _ptr(ray_start),
+                                  _ptr(ray_dir), _ptr(points), _ptr(idx), _ptr(lo), _ptr(hi),
+                                  _stream(ray_start)), "ball_intersect")
+    return idx, lo, hi
+
+
+def uniform_ray_sampling(pts_idx, min_depth, max_depth, uniform_noise, step_size, max_steps):
+    """fairnr/clib/src/sample.cpp:23-55: -> (sampled_idx, sampled_depth, sampled_dists) [B, M, max_steps]."""
+    _check_int("pts_idx", pts_idx)
+    for n, t in (("min_depth", min_depth), ("max_depth", max_depth),
+                 ("uniform_noise", uniform_noise)):
+        _check_float(n, t)
+    B, M, H = pts_idx.shape
+    _need(uniform_noise.shape[:2] == (B, M) and uniform_noise.size(2) >= max_steps,
+          "uniform_noise must be [B, M, >= max_steps]")
+    if uniform_noise.size(2) != max_steps:
+        uniform_noise = uniform_noise[..., :max_steps].contiguous()
+    dev = pts_idx.device
+    si = torch.empty(B, M, max_steps, dtype=torch.int32, device=dev)
+    sd = torch.empty(B, M, max_steps, dtype=torch.float32, device=dev)
+    ss = torch.empty(B, M, max_steps, dtype=torch.float32, device=dev)
+    check(LIB.nsvf_uniform_ray_sampling(B, M, H, int(max_steps), float(step_size), _ptr(pts_idx),
+                                        _ptr(min_depth), _ptr(max_depth), _ptr(uniform_noise),
+                                        _ptr(si), _ptr(sd), _ptr(ss), _ptr(error_word(dev)),
+                                        _stream(pts_idx)), "uniform_ray_sampling")
+    return si, sd, ss
+
+
+def inverse_cdf_sampling_rows(pts_idx, min_depth, max_depth, noise, probs, steps,
+                              fixed_step_size, layout, max_steps, max_len=None):
+    """Inverse-CDF sampling over [rows, H] inputs with an explicit launch layout
+    (see nsvf_inverse_cdf_sampling in include/nsvf_gb300.h). noise is
+    [>= rows, >= max_steps] or None for the deterministic 0.5 jitter."""
+    rows, H = pts_idx.shape
+    dev = pts_idx.device
+    si = torch.empty(rows, max_steps, dtype=torch.int32, device=dev)
+    sd = torch.empty(rows, max_steps, dtype=torch.float32, device=dev)
+    ss = torch.empty(rows, max_steps, dtype=torch.float32, device=dev)
+    lay = (torch.tensor(layout, dtype=torch.int64)).contiguous()
+    check(LIB.nsvf_inverse_cdf_sampling(
+        rows, H, int(max_steps), noise.size(-1) if noise is not None else 0,
+        float(fixed_step_size), _ptr(pts_idx), _ptr(min_depth), _ptr(max_depth), _ptr(noise),
+        _ptr(probs), _ptr(steps), lay.data_ptr(), _ptr(si), _ptr(sd), _ptr(ss), _ptr(max_len),
+        _ptr(error_word(dev)), _stream(pts_idx)), "inverse_cdf_sampling")
+    return si, sd, ss
+
+
+def inverse_cdf_sampling(pts_idx, min_depth, max_depth, uniform_noise, probs, steps,
+                         fixed_step_size):
+    """fairnr/clib/src/sample.cpp:58-96 over [B, M, H] inputs (max_steps = noise.size(-1)):
+    -> (sampled_idx, sampled_depth, sampled_dists) [B, M, max_steps]."""
+    _check_int("pts_idx", pts_idx)
+    for n, t in (("min_depth", min_depth), ("max_depth", max_depth),
+                 ("uniform_noise", uniform_noise), ("probs", probs), ("steps", steps)):
+        _check_float(n, t)
+    B, M, H = pts_idx.shape
+    S = uniform_noise.size(-1)
+    rows = B * M
+    si, sd, ss = inverse_cdf_sampling_rows(
+        pts_idx.view(rows, H), min_depth.view(rows, H), max_depth.view(rows, H),
+        uniform_noise.view(rows, S), probs.view(rows, H), steps.view(rows), fixed_step_size,
+        (max(M, 1), max(M, 1), rows, max(B, 1)), S)
+    return si.view(B, M, S), sd.view(B, M, S), ss.view(B, M, S)
+
+
+def build_octree(center, points, depth):
+    """fairnr/clib/src/octree.cpp:125-136 (host build): center [3], points [V, 3]
+    integer coordinates -> (centers [Nn, 3] int32, children [Nn, 9] int32) on points' device."""
+    import ctypes
+    import numpy as np
+    c = np.ascontiguousarray(center.detach().float().cpu().numpy().reshape(3), dtype=np.float32)
+    p = np.ascontiguousarray(points.detach().cpu().numpy().reshape(-1, 3), dtype=np.int64)
+    cp = ctypes.c_void_p(c.ctypes.data)
+    pp = ctypes.c_void_p(p.ctypes.data)
+    n = LIB.nsvf_build_octree(cp, pp, p.shape[0], int(depth), None, None, 0)
+    if n < 0:
+        check(int(n), "build_octree")
+    cen = np.empty((n, 3), np.int32)
+    chi = np.empty((n, 9), np.int32)
+    n2 = LIB.nsvf_build_octree(cp, pp, p.shape[0], int(depth), ctypes.c_void_p(cen.ctypes.data),
+                               ctypes.c_void_p(chi.ctypes.data), n)
+    if n2 < 0:
+        check(int(n2), "build_octree")
+    dev = points.device
+    return torch.from_numpy(cen).to(dev), torch.from_numpy(chi).to(dev)
