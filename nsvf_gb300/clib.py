@@ -1,0 +1,229 @@
+"""Drop-in for the reference's op API ``fairnr.clib`` (fairnr/clib/__init__.py).
+
+Same function names, arguments and outputs as the reference's
+autograd.Function wrappers (all non-differentiable). What changes is how the
+work reaches the GPU:
+
+* Intersection: the reference splits the rays into up to 2048 groups and
+  copies the voxel set / octree into every group to fill its one-block-per-
+  row kernels (fairnr/clib/__init__.py:62-71, 101-111; ~8 GB of copies for the
+  125k-voxel scene). Here one launch covers all rays against one copy.
+* Sampling: the reference pads the rays to 200 (or 256) blocks and launches
+  in slices of 800 columns (fairnr/clib/__init__.py:181-189, 234-270). Here
+  one launch covers all rays; the two places where the reference's result
+  depends on that blocking (see include/nsvf_gb300.h) are reproduced from the
+  layout parameters, and the noise tensor is drawn with the same shape and
+  torch RNG calls, so results are identical for the same seed.
+"""
+import numpy as np
+import torch
+from torch.autograd import Function
+
+from . import ext
+
+MAX_DEPTH = 10000.0
+
+
+class BallRayIntersect(Function):
+    @staticmethod
+    def forward(ctx, radius, n_max, points, ray_start, ray_dir):
+        inds, min_depth, max_depth = ext.ball_intersect(
+            ray_start.float().contiguous(), ray_dir.float().contiguous(),
+            points.float().contiguous(), radius, n_max)
+        min_depth = min_depth.type_as(ray_start)
+        max_depth = max_depth.type_as(ray_start)
+        ctx.mark_non_differentiable(inds, min_depth, max_depth)
+        return inds, min_depth, max_depth
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None
+
+
+ball_ray_intersect = BallRayIntersect.apply
+
+
+class AABBRayIntersect(Function):
+    @staticmethod
+    def forward(ctx, voxelsize, n_max, points, ray_start, ray_dir):
+        inds, min_depth, max_depth = ext.aabb_intersect(
+            ray_start.float().contiguous(), ray_dir.float().contiguous(),
+            points.float().contiguous(), float(voxelsize), int(n_max))
+        min_depth = min_depth.type_as(ray_start)
+        max_depth = max_depth.type_as(ray_start)
+        ctx.mark_non_differentiable(inds, min_depth, max_depth)
+        return inds, min_depth, max_depth
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None
+
+
+aabb_ray_intersect = AABBRayIntersect.apply
+
+
+class SparseVoxelOctreeRayIntersect(Function):
+    @staticmethod
+    def forward(ctx, voxelsize, n_max, points, children, ray_start, ray_dir):
+        inds, min_depth, max_depth = ext.svo_intersect(
+            ray_start.float().contiguous(), ray_dir.float().contiguous(),
+            points.float().contiguous(), children.int().contiguous(), float(voxelsize), int(n_max))
+        min_depth = min_depth.type_as(ray_start)
+        max_depth = max_depth.type_as(ray_start)
+        ctx.mark_non_differentiable(inds, min_depth, max_depth)
+        return inds, min_depth, max_depth
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None, None
+
+
+svo_ray_intersect = SparseVoxelOctreeRayIntersect.apply
+
+
+def _truncate(sampled_idx, sampled_depth, sampled_dists, max_len):
+    return sampled_idx[:, :max_len], sampled_depth[:, :max_len], sampled_dists[:, :max_len]
+
+
+class UniformRaySampling(Function):
+    @staticmethod
+    def forward(ctx, pts_idx, min_depth, max_depth, step_size, max_ray_length, deterministic=False):
+        G, N, P = 256, pts_idx.size(0), pts_idx.size(1)
+        H = int(np.ceil(N / G)) * G
+        max_steps = int(max_ray_length / step_size) + P * 2
+        # noise drawn exactly as the reference: [G, H/G, max_steps], U(0, 1)
+        noise = min_depth.new_zeros(H, max_steps)
+        if deterministic:
+            noise += 0.5
+        else:
+            noise = noise.uniform_()
+        # the reference pads rows by repeating the FIRST H-N rows; rows are
+        # independent except that a jitter of exactly 0 reads the previous
+        # row's last id, which is the same element here
+        si, sd, ss = ext.uniform_ray_sampling(
+            pts_idx.int().contiguous().view(1, N, P), min_depth.float().contiguous().view(1, N, P),
+            max_depth.float().contiguous().view(1, N, P),
+            noise.float()[:N].contiguous().view(1, N, max_steps), float(step_size), max_steps)
+        si, sd, ss = si.view(N, -1), sd.view(N, -1).type_as(min_depth), ss.view(N, -1).type_as(min_depth)
+        ext.check_errors(pts_idx.device)
+        max_len = si.ne(-1).sum(-1).max()
+        si, sd, ss = _truncate(si, sd, ss, max_len)
+        ctx.mark_non_differentiable(si, sd, ss)
+        return si, sd, ss
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None, None
+
+
+uniform_ray_sampling = UniformRaySampling.apply
+
+
+def inverse_cdf_layout(N, G=200, chunk=800):
+    """The reference wrapper's launch layout for N rays: K = ceil(N/G) rays per
+    block, launched `chunk` columns at a time (fairnr/clib/__init__.py:234-270)."""
+    K = max(1, int(np.ceil(N / G)))
+    return (K, chunk, N, G)
+
+
+class InverseCDFRaySampling(Function):
+    @staticmethod
+    def forward(ctx, pts_idx, min_depth, max_depth, probs, steps, fixed_step_size=-1,
+                deterministic=False):
+        G, N, P = 200, pts_idx.size(0), pts_idx.size(1)
+        H = int(np.ceil(N / G)) * G
+        # max_steps over the padded rows (padding copies row 0): same as over N
+        max_steps = int(steps.ceil().long().max()) + P
+        if deterministic:
+            noise = None   # the kernel's built-in 0.5 jitter
+        else:
+            # drawn exactly as the reference: [G, H/G, max_steps], clamped
+            noise = min_depth.new_zeros(H, max_steps).uniform_().clamp(min=0.001, max=0.999)
+            noise = noise.float()
+        dev = pts_idx.device
+        max_len = torch.zeros(1, dtype=torch.int32, device=dev)
+        si, sd, ss = ext.inverse_cdf_sampling_rows(
+            pts_idx.int().contiguous(), min_depth.float().contiguous(),
+            max_depth.float().contiguous(), noise, probs.float().contiguous(),
+            steps.float().contiguous(), float(fixed_step_size), inverse_cdf_layout(N),
+            max_steps, max_len)
+        sd, ss = sd.type_as(min_depth), ss.type_as(min_depth)
+        ext.check_errors(dev)
+        L = int(max_len.item())
+        si, sd, ss = _truncate(si, sd, ss, L)
+        ctx.mark_non_differentiable(si, sd, ss)
+        return si, sd, ss
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None, None, None
+
+
+inverse_cdf_sampling = InverseCDFRaySampling.apply
+
+
+@torch.no_grad()
+def _parallel_ray_sampling(MARCH_SIZE, pts_idx, min_depth, max_depth, deterministic=False):
+    """Pure-torch uniform sampler kept by the reference as a back-up
+    (fairnr/clib/__init__.py:303-351): uniform steps from the first entry
+    point plus every interval boundary, sorted; midpoints outside a voxel are
+    dropped."""
+    _min_depth = min_depth.min(1)[0]
+    _max_depth = max_depth.masked_fill(max_depth.eq(MAX_DEPTH), 0).max(1)[0]
+    max_ray_length = (_max_depth - _min_depth).max()
+    delta = torch.arange(int(max_ray_length / MARCH_SIZE), device=min_depth.device,
+                         dtype=min_depth.dtype)
+    delta = delta[None, :].expand(min_depth.size(0), delta.size(-1))
+    if deterministic:
+        delta = delta + 0.5
+    else:
+        delta = delta + delta.clone().uniform_().clamp(min=0.01, max=0.99)
+    delta = delta * MARCH_SIZE
+    sampled_depth = min_depth[:, :1] + delta
+    sampled_idx = (sampled_depth[:, :, None] >= min_depth[:, None, :]).sum(-1) - 1
+    sampled_idx = pts_idx.gather(1, sampled_idx)
+    sampled_depth = torch.cat([min_depth, max_depth, sampled_depth], -1)
+    sampled_idx = torch.cat([pts_idx, pts_idx, sampled_idx], -1)
+    sampled_depth, order = sampled_depth.sort(-1)
+    sampled_idx = sampled_idx.gather(1, order)
+    sampled_dists = sampled_depth[:, 1:] - sampled_depth[:, :-1]
+    sampled_depth = .5 * (sampled_depth[:, 1:] + sampled_depth[:, :-1])
+    min_ids = (sampled_depth[:, :, None] >= min_depth[:, None, :]).sum(-1) - 1
+    max_ids = (sampled_depth[:, :, None] >= max_depth[:, None, :]).sum(-1)
+    sampled_depth.masked_fill_(
+        (max_ids.ne(min_ids)) | (sampled_depth > _max_depth[:, None]) | (sampled_dists == 0.0),
+        MAX_DEPTH)
+    sampled_depth, order = sampled_depth.sort(-1)
+    masks = sampled_depth.eq(MAX_DEPTH)
+    n = (~masks).sum(-1).max()
+    sampled_depth = sampled_depth[:, :n]
+    sampled_dists = sampled_dists.gather(1, order).masked_fill_(masks, 0.0)[:, :n]
+    sampled_idx = sampled_idx.gather(1, order).masked_fill_(masks, -1)[:, :n]
+    return sampled_idx, sampled_depth, sampled_dists
+
+
+@torch.no_grad()
+def parallel_ray_sampling(MARCH_SIZE, pts_idx, min_depth, max_depth, deterministic=False):
+    chunk_size = 4096
+    full_size = min_depth.shape[0]
+    if full_size <= chunk_size:
+        return _parallel_ray_sampling(MARCH_SIZE, pts_idx, min_depth, max_depth,
+                                      deterministic=deterministic)
+    outs = list(zip(*[
+        _parallel_ray_sampling(MARCH_SIZE, pts_idx[i:i + chunk_size],
+                               min_depth[i:i + chunk_size], max_depth[i:i + chunk_size],
+                               deterministic=deterministic)
+        for i in range(0, full_size, chunk_size)]))
+
+    def pad(xs, value):
+        if len(xs) == 1:
+            return xs[0]
+        width = max(x.size(1) for x in xs)
+        out = xs[0].new_full((sum(x.size(0) for x in xs), width), value)
+        st = 0
+        for x in xs:
+            out[st:st + x.size(0), :x.size(1)] = x
+            st += x.size(0)
+        return out
+
+    return pad(outs[0], -1), pad(outs[1], MAX_DEPTH), pad(outs[2], 0.0)

@@ -108,9 +108,10 @@ extern "C" int64_t nsvf_build_octree(const float center[3], const int64_t *point
   // A repeated point leaves a hole in the leaf numbering; the reference then
   // writes outside its tensors. Reject it.
   if (next != terminal) return NSVF_ERR_INVALID;
+  // The surviving leaf ids must be exactly 0..terminal-1.
   for (size_t h = 0; h < bfs.size(); ++h) {
     const Node &x = nodes[bfs[h]];
-    if (x.index < 0 || x.index >= total) return NSVF_ERR_INVALID;
+    if (x.depth == -1 && (x.index < 0 || x.index >= terminal)) return NSVF_ERR_INVALID;
   }
   for (size_t h = 0; h < bfs.size(); ++h) {
     const Node &x = nodes[bfs[h]];

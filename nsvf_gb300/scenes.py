@@ -7,7 +7,7 @@ of the five workloads:
 * c1 "small":  bbox [-1, 1]^3, voxel 0.25, centres within 0.8 of the origin
                (147 voxels on the reference's voxel grid), 64x64 view, f=80.
 * c2 "shell":  voxel 1/64 on [-1, 1]^3, the shell |SDF| < 2 voxels of
-               sphere(r=0.6) U torus(R=0.7, r=0.2 about z): 125,452 voxels,
+               sphere(r=0.6) U torus(R=0.7, r=0.2 about z): 125,476 voxels,
                800x800 views from 100 seeded cameras on a radius-4 sphere.
 * c4:          the same shell at voxel 1/128 (500,832 voxels).
 * c5:          8 scenes of sphere/torus/box unions with 10k-400k voxels.
@@ -148,10 +148,13 @@ def voxel_embeddings(num_keys, dim=32, std=0.01, seed=1, device="cpu"):
     return (torch.randn(num_keys, dim, generator=g) * std).to(device)
 
 
-def stand_in_mlp_weights(in_dim=32, hidden=128, layers=4, out_dim=4, seed=2):
+def stand_in_mlp_weights(in_dim=32, hidden=128, layers=4, out_dim=4, seed=2,
+                         sigma_scale=1.0, sigma_bias=0.0):
     """Xavier-uniform weights and zero biases of the 4x128 ReLU field MLP
     (the reference's Linear init, fairnr/modules/module_utils.py:15-20):
-    [(W [out, in], b [out]), ...], last layer -> (sigma, r, g, b)."""
+    [(W [out, in], b [out]), ...], last layer -> (sigma, r, g, b).
+    sigma_scale / sigma_bias rescale the density row of the last layer (test
+    scenes use them to get an opaque, partly prunable field)."""
     g = torch.Generator().manual_seed(seed)
     dims = [in_dim] + [hidden] * layers + [out_dim]
     out = []
@@ -159,4 +162,7 @@ def stand_in_mlp_weights(in_dim=32, hidden=128, layers=4, out_dim=4, seed=2):
         bound = math.sqrt(6.0 / (a + b))
         W = (torch.rand(b, a, generator=g) * 2 - 1) * bound
         out.append((W, torch.zeros(b)))
+    W, b = out[-1]
+    W[0] *= sigma_scale
+    b[0] = sigma_bias
     return out
