@@ -1,0 +1,396 @@
+"""Benchmark: full-frame rendering of the 125k-voxel shell scene on GB300.
+
+Workload (the c2 configuration): voxel 1/64 shell of sphere(0.6) U
+torus(0.7, 0.2) -> 125,476 voxels, 277,630-node octree; 32-d corner
+embeddings N(0, 0.01^2); 4 x 128 ReLU field MLP (Xavier); 800 x 800 pinhole
+frames (640,000 rays) from 100 seeded cameras on the radius-4 sphere; SVO
+traversal with max_hits 64; inverse-CDF sampling at step voxel/8 = 1/512,
+deterministic (eval) jitter; front-to-back compositing; background fill.
+A "step" renders one full frame. Synthetic data (seeded), see
+nsvf_gb300/scenes.py.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--path plain|served]
+    python bench.py --impl reference ...   # the CPU reference arm
+
+Prints one JSON line (rank 0). Timing: CUDA events per frame on the
+rendering stream, L2 flushed (256 MB write) between frames outside the timed
+events; clocks sampled with nvidia-smi during the timed region.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RAYS_PER_FRAME = 800 * 800
+MAX_HITS = 64
+METRIC = "rays/s (full 800x800 frames)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="plain", choices=["plain", "served"])
+    ap.add_argument("--cpu-rays", type=int, default=16384,
+                    help="rays of the frame in the CPU baseline sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- workload --
+
+def make_scene(dev):
+    import torch
+    from nsvf_gb300 import scenes
+    from nsvf_gb300.encoder import SparseVoxelEncoder
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.renderer import VolumeRenderer
+    p, vs = scenes.scene_shell(1.0 / 64)
+    args = argparse.Namespace(voxel_size=vs, max_hits=MAX_HITS, raymarching_stepsize_ratio=0.125,
+                              voxel_embed_dim=32, use_octree=True, deterministic_step=True,
+                              chunk_size=256)
+    enc = SparseVoxelEncoder(args, points=p)
+    with torch.no_grad():
+        enc.values.weight.copy_(scenes.voxel_embeddings(enc.values.weight.shape[0], 32, 0.01, seed=1))
+    weights = scenes.stand_in_mlp_weights(seed=2)
+    field = StandInField(weights=weights)
+    ren = VolumeRenderer(args)
+    enc, field, ren = enc.to(dev).eval(), field.to(dev).eval(), ren.eval()
+    states = enc.precompute(id=None)
+    return dict(points=p, voxel_size=vs, enc=enc, field=field, ren=ren, states=states,
+                weights=weights)
+
+
+def frame_rays(index):
+    from nsvf_gb300 import scenes
+    rs, rd = scenes.frame_view(index % 100)
+    return rs, rd
+
+
+# ------------------------------------------------------------- clocks ------
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------- GPU arm ---------
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+    from nsvf_gb300 import ext
+    from nsvf_gb300._lib import LIB
+    from nsvf_gb300.renderer import render_rays
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    torch.backends.cudnn.allow_tf32 = False
+    sc = make_scene(dev)
+    enc, field, ren, states = sc["enc"], sc["field"], sc["ren"], sc["states"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # host-resident inputs of every frame (pinned), one camera per step
+    n_frames = a.warmup + a.steps
+    host = []
+    for i in range(n_frames):
+        rs, rd = frame_rays(i + 7 * rank)
+        rdt = torch.from_numpy(rd).pin_memory()
+        rst = torch.from_numpy(rs).pin_memory()
+        host.append((rst, rdt))
+    dev_in = [(h[0].to(dev), h[1].to(dev)) for h in host]
+
+    def step(rs, rd):
+        with torch.no_grad():
+            return render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3),
+                               encoder_states=states)
+
+    # --- device-resident timing (value) ---
+    ext.KERNEL_TIMING = True
+    for i in range(a.warmup):
+        step(*dev_in[i])
+    torch.cuda.synchronize()
+    ext.kernel_events.clear()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    l0 = LIB.nsvf_launch_count()
+    for i in range(a.steps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        out = step(*dev_in[a.warmup + i])
+        e.record()
+        torch.cuda.synchronize()
+        times.append(s.elapsed_time(e) / 1e3)
+    launches = LIB.nsvf_launch_count() - l0
+    clk = clocks.stop()
+    ext.KERNEL_TIMING = False
+    kernel_ms = ext.kernel_times_ms()
+    t_dev = sum(times)
+    if world > 1:
+        t = torch.tensor([t_dev], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev = float(t.item())
+
+    # --- end to end through the public API with host buffers ---
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e2e_times = []
+    h2d = d2h = 0
+    for i in range(a.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rst, rdt = host[a.warmup + i]
+        rs_d = rst.to(dev, non_blocking=True)
+        rd_d = rdt.to(dev, non_blocking=True)
+        out = step(rs_d, rd_d)
+        col = out["colors"].reshape(-1, 3).to("cpu")
+        dep = out["depths"].reshape(-1).to("cpu")
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        h2d = rst.numel() * 4 + rdt.numel() * 4
+        d2h = col.numel() * 4 + dep.numel() * 4
+    t_e2e = sum(e2e_times)
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    rays_total = RAYS_PER_FRAME * a.steps * world
+    value = rays_total / t_dev
+    ms = [x * 1e3 for x in times]
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    hbm_peak = peaks["hbm_gbs"] if peaks else 6800.0
+    # roofline of the dominant kernel of this library on this path: the SVO
+    # traversal with the fused sort. Algorithmic bytes per launch:
+    # R*24 (ray origin + direction) + Nn*48 (packed octree) + R*H*12 (sorted
+    # ids/min/max) + R (hit flags).
+    Nn = int(states["voxel_octree_children_idx"].shape[0])
+    alg = RAYS_PER_FRAME * 24 + Nn * 48 + RAYS_PER_FRAME * MAX_HITS * 12 + RAYS_PER_FRAME
+    k = kernel_ms.get("svo_intersect_sorted")
+    roof = None
+    if k:
+        ach = alg / (k["avg_ms"] / 1e3) / 1e9
+        roof = {"kernel": "svo_intersect_sorted", "bound": "hbm", "achieved": round(ach, 1),
+                "peak": hbm_peak, "unit": "GB/s", "frac": round(ach / hbm_peak, 4),
+                "peak_source": "measured" if peaks else "fallback",
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": round(k["avg_ms"], 4),
+                "traffic": None}
+    cpu = cpu_baseline(a.cpu_rays, threads=1)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(statistics.mean(ms), 3),
+        "p50_ms": round(float(np.percentile(ms, 50)), 3), "p99_ms": round(float(np.percentile(ms, 99)), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene, embeddings, MLP and cameras)",
+        "config": {"workload": "c2: 125,476-voxel sphere+torus shell, 800x800 frame, SVO, "
+                               "max_hits 64, step 1/512, 4x128 MLP", "path": a.path,
+                   "voxels": int(sc["points"].shape[0]), "octree_nodes": Nn,
+                   "l2": "flushed (256 MB write) between timed frames", "parallelism": "replicas"},
+        "e2e": {"value": round(RAYS_PER_FRAME * a.steps * world / t_e2e, 1), "unit": "rays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "kernels_ms": kernel_ms,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------ CPU arm --------
+
+def cpu_render(rays_o, rays_d, sc, threads=1):
+    """The hot path on the CPU with the oracle: C restatement of the SVO
+    traversal and inverse-CDF sampling (ctypes, GIL released, `threads` ray
+    chunks in parallel), float64 numpy interpolation, MLP and compositing."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import cpu
+    vs = sc["voxel_size"]
+    cen, chi = sc["octree"]
+    step = vs / 8
+    R = rays_d.shape[0]
+    chunks = np.array_split(np.arange(R), max(1, threads * 4))
+
+    def one(ix):
+        o = np.broadcast_to(rays_o, (len(ix), 3))[None]
+        idx, lo, hi = cpu.sort_hits(*cpu.svo_intersect(o, rays_d[ix][None], cen[None], chi[None],
+                                                       vs, MAX_HITS))
+        idx, lo, hi = idx[0], lo[0], hi[0]
+        hit = (idx != -1).any(-1)
+        col = np.zeros((len(ix), 3))
+        mis = np.ones(len(ix))
+        if hit.sum() == 0:
+            return col, mis
+        I, L, Hh = idx[hit], lo[hit], hi[hit]
+        pr, st = cpu.probs_steps(I, L, Hh, step)
+        N = I.shape[0]
+        M = int(np.ceil(st).max()) + MAX_HITS
+        si, sd, ss = cpu.inverse_cdf_op(I, L, Hh, pr, st, np.full((N, M), 0.5, np.float32))
+        ss = np.maximum(ss, 0)
+        mask = si != -1
+        xyz = rays_o[None, None].astype(np.float64) + rays_d[ix][hit][:, None, :] * sd[..., None]
+        emb = cpu.trilinear_embed(xyz[mask], si[mask], sc["centers_shifted"], sc["feats"],
+                                  sc["values"], vs)
+        sig, rgb = cpu.mlp_forward(emb, sc["weights_np"])
+        S = np.zeros(mask.shape)
+        C = np.zeros(mask.shape + (3,))
+        S[mask], C[mask] = sig, rgb
+        out = cpu.composite(S, C, sd.astype(np.float64), ss.astype(np.float64), mask)
+        col[hit] = out["colors"]
+        mis[hit] = out["missed"]
+        return col, mis
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, chunks))
+    col = np.concatenate([r[0] for r in res])
+    mis = np.concatenate([r[1] for r in res])
+    return col + mis[:, None] * 1.0, mis
+
+
+def cpu_scene():
+    import torch
+    from nsvf_gb300 import geometry, scenes
+    p, vs = scenes.scene_shell(1.0 / 64)
+    pts = torch.from_numpy(p)
+    cen, chi = geometry.build_easy_octree(pts, vs / 2)
+    keys, feats = geometry.voxel_corner_table(pts, vs)
+    values = scenes.voxel_embeddings(keys.shape[0], 32, 0.01, seed=1).numpy()
+    shifted = p.copy()
+    shifted[:, 0] += np.float32(vs / 10)
+    weights = scenes.stand_in_mlp_weights(seed=2)
+    return dict(voxel_size=vs, octree=(cen.numpy(), chi.numpy()), feats=feats.numpy(),
+                values=values, centers_shifted=shifted,
+                weights_np=[(W.numpy(), b.numpy()) for W, b in weights])
+
+
+def cpu_baseline(n_rays, threads=1):
+    """Oracle CPU render of a fixed seeded sample of n_rays rays of frame 0."""
+    sc = cpu_scene()
+    rs, rd = frame_rays(0)
+    sel = np.random.RandomState(0).choice(rd.shape[0], n_rays, replace=False)
+    t0 = time.perf_counter()
+    cpu_render(rs, rd[sel], sc, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(n_rays / dt, 1), "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": "%d seeded rays of the 800x800 frame 0 (oracle C traversal/sampling, "
+                      "float64 numpy interpolation/MLP/compositing)" % n_rays,
+            "seconds": round(dt, 2), "nproc": os.cpu_count()}
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    import torch
+    torch.set_num_threads(threads)
+    sc = cpu_scene()
+    n = a.cpu_rays
+    times = []
+    for i in range(a.warmup + a.steps):
+        rs, rd = frame_rays(i)
+        sel = np.random.RandomState(i).choice(rd.shape[0], n, replace=False)
+        t0 = time.perf_counter()
+        cpu_render(rs, rd[sel], sc, threads=threads)
+        if i >= a.warmup:
+            times.append(time.perf_counter() - t0)
+    value = n * len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "rays/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": round(1e3 * sum(times) / len(times), 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "c2: 125,476-voxel shell, 800x800 frames, SVO, max_hits 64, "
+                                   "step 1/512, 4x128 MLP", "sample_rays_per_step": n},
+            "cpu_baseline": {"value": round(value, 1), "unit": "rays/s", "cores": threads,
+                             "kind": "port",
+                             "sample": "%d seeded rays per frame, oracle port (C traversal and "
+                                       "sampling, numpy float64 rest), %d threads" % (n, threads)},
+            "e2e": {"value": round(value, 1), "unit": "rays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

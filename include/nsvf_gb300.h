@@ -36,6 +36,10 @@ extern "C" {
 /* Human-readable text for a status code. */
 const char *nsvf_status_string(int status);
 
+/* Number of kernels this library has launched in this process (all
+ * devices, all streams); for profiling and launch accounting. */
+long long nsvf_launch_count(void);
+
 /* ------------------------------------------------------------------------ */
 /* Ray-voxel intersection (fairnr/clib/include/intersect.h:10-17)            */
 
@@ -146,6 +150,58 @@ int nsvf_inverse_cdf_sampling(int64_t rows, int max_hits, int max_steps, int noi
  * children[., 8] = 1 << (node depth + 1); centres truncated to int. */
 int64_t nsvf_build_octree(const float center[3], const int64_t *points, int64_t n_points,
                           int depth, int32_t *centers, int32_t *children, int64_t capacity);
+
+/* ------------------------------------------------------------------------ */
+/* Trilinear interpolation of corner embeddings                              */
+
+/* trilinear_embed: replaces the embedding part of SparseVoxelEncoder.forward
+ * (fairnr/modules/encoder.py:578-590 with fairnr/data/geometry.py:195-200).
+ * For sample s in voxel v = sampled_idx[s] (int32 or int64: idx_bytes 4|8):
+ * p = (xyz[s] - centers[v]) / voxel_size + 0.5; corner k = 4*ix + 2*iy + iz
+ * weighs prod_d (bit_d(k) ? p_d : 1 - p_d); emb[s] = sum_k w_k *
+ * values[feats[v, k]]. xyz [n, 3], centers [n_voxels, 3], feats
+ * [n_voxels, 8] (int32/int64: feat_bytes), values [n_keys, embed_dim], emb
+ * [n, embed_dim], FP32; embed_dim in {4, 8, 16, 32, 64, 128}; values and emb
+ * 16-byte aligned. Ids out of range are not read (emb 0, err bit 2). */
+int nsvf_trilinear_embed(int64_t n_samples, int embed_dim, float voxel_size, int64_t n_voxels,
+                         int64_t n_keys, const void *sampled_idx, int idx_bytes, const float *xyz,
+                         const float *centers, const void *feats, int feat_bytes,
+                         const float *values, float *emb, int32_t *err, void *stream);
+
+/* Backward of trilinear_embed: grad_values [n_keys, embed_dim] (accumulated
+ * with atomics; zero it first) and/or grad_xyz [n, 3] (written), either may
+ * be NULL (not both). The reference gets these from autograd through its two
+ * F.embedding gathers (an index_add into the embedding table). */
+int nsvf_trilinear_embed_backward(int64_t n_samples, int embed_dim, float voxel_size,
+                                  int64_t n_voxels, int64_t n_keys, const void *sampled_idx,
+                                  int idx_bytes, const float *xyz, const float *centers,
+                                  const void *feats, int feat_bytes, const float *values,
+                                  const float *grad_emb, float *grad_values, float *grad_xyz,
+                                  void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Compositing                                                               */
+
+/* composite: replaces the compositing of VolumeRenderer.forward_chunk
+ * (fairnr/modules/renderer.py:193-218) over [rays, max_steps] samples:
+ * a_i = 1 - exp(-fe_i), T_i = exp(-sum_{j<i} fe_j), p_i = a_i T_i;
+ * probs [rays, max_steps], depth [rays] = sum p_i t_i, missed = 1 - sum p_i,
+ * colors [rays, 3] = sum p_i tex_i. texture [rays, max_steps, 3] and
+ * sampled_depth may be NULL (their outputs are then skipped); any output may
+ * be NULL. kahan != 0 carries the transmittance prefix as a compensated sum. */
+int nsvf_composite(int64_t rays, int max_steps, const float *free_energy, const float *texture,
+                   const float *sampled_depth, float *probs, float *depth, float *missed,
+                   float *colors, int kahan, void *stream);
+
+/* Backward of composite: gradients w.r.t. free_energy (written) and texture
+ * (written, may be NULL) from the gradients of probs/depth/missed/colors
+ * (each may be NULL = zero). */
+int nsvf_composite_backward(int64_t rays, int max_steps, const float *free_energy,
+                            const float *texture, const float *sampled_depth,
+                            const float *grad_probs, const float *grad_depth,
+                            const float *grad_missed, const float *grad_colors,
+                            float *grad_free_energy, float *grad_texture, int kahan,
+                            void *stream);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,7 @@ def _load():
     P, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
     sig = {
         "nsvf_status_string": ([i32], ctypes.c_char_p),
+        "nsvf_launch_count": ([], ctypes.c_longlong),
         "nsvf_aabb_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P], i32),
         "nsvf_svo_workspace_bytes": ([i32, i32], i64),
         "nsvf_svo_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P, P, P, P], i32),
@@ -35,6 +36,11 @@ def _load():
         "nsvf_inverse_cdf_sampling": ([i64, i32, i32, i32, f32, P, P, P, P, P, P, P, P, P, P,
                                        P, P, P], i32),
         "nsvf_build_octree": ([P, P, i64, i32, P, P, i64], i64),
+        "nsvf_trilinear_embed": ([i64, i32, f32, i64, i64, P, i32, P, P, P, i32, P, P, P, P], i32),
+        "nsvf_trilinear_embed_backward": ([i64, i32, f32, i64, i64, P, i32, P, P, P, i32, P, P, P,
+                                           P, P], i32),
+        "nsvf_composite": ([i64, i32, P, P, P, P, P, P, P, i32, P], i32),
+        "nsvf_composite_backward": ([i64, i32, P, P, P, P, P, P, P, P, P, i32, P], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -56,7 +62,9 @@ def check(status, what):
 def exported_symbols():
     """Names declared in include/nsvf_gb300.h that the library must export."""
     return [
-        "nsvf_status_string", "nsvf_aabb_intersect", "nsvf_svo_workspace_bytes",
+        "nsvf_status_string", "nsvf_launch_count", "nsvf_aabb_intersect", "nsvf_svo_workspace_bytes",
         "nsvf_svo_intersect", "nsvf_svo_intersect_sorted", "nsvf_ball_intersect",
         "nsvf_uniform_ray_sampling", "nsvf_inverse_cdf_sampling", "nsvf_build_octree",
+        "nsvf_trilinear_embed", "nsvf_trilinear_embed_backward", "nsvf_composite",
+        "nsvf_composite_backward",
     ]

@@ -7,8 +7,13 @@
 
 #define NSVF_MAX_DEPTH_F 10000.0f
 
-// Launch-status helper: every entry point returns an int status, never exits.
+// Process-wide count of kernels launched by this library (nsvf_launch_count).
+void nsvf_count_launch();
+
+// Launch-status helper, called right after each kernel launch: counts it and
+// turns the launch error into a status (never exits).
 static inline int nsvf_launch_status() {
+  nsvf_count_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? NSVF_OK : NSVF_ERR_CUDA;
 }

@@ -8,6 +8,8 @@
 // or octree into every row: fairnr/clib/__init__.py:62-71, 101-111). Here
 // every ray batch reads ONE copy of the voxels/octree, which stays resident in
 // L2 (c2 scene: 277,580 nodes x 48 B = 13 MB of a 129 MB L2).
+#include <atomic>
+
 #include "common.cuh"
 
 namespace {
@@ -212,14 +214,22 @@ __global__ void __launch_bounds__(kRayBlock) ball_kernel(
   for (int l = cnt; l < n_max; ++l) { I[l] = -1; LO[l] = 0.0f; HI[l] = 0.0f; }
 }
 
+// Ray pointers may be NULL when there are no rays (empty tensors).
 bool bad_common(int b, int b_pts, int n, int m, int n_max, const void *a, const void *c,
                 const void *d) {
-  return b < 0 || m < 0 || n < 1 || n_max < 1 || (b_pts != 1 && b_pts != b) || !a || !c || !d;
+  bool no_rays = (int64_t)b * m == 0;
+  return b < 0 || m < 0 || n < 1 || n_max < 1 || (b_pts != 1 && b_pts != b) ||
+         (!no_rays && (!a || !c)) || !d;
 }
 
 }  // namespace
 
+static std::atomic<long long> g_launches{0};
+void nsvf_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 extern "C" {
+
+long long nsvf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 const char *nsvf_status_string(int status) {
   switch (status) {
@@ -235,10 +245,9 @@ const char *nsvf_status_string(int status) {
 int nsvf_aabb_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_max,
                         const float *ray_start, const float *ray_dir, const float *points,
                         int32_t *idx, float *min_depth, float *max_depth, void *stream) {
-  if (bad_common(b, b_pts, n, m, n_max, ray_start, ray_dir, points) || !idx || !min_depth ||
-      !max_depth)
-    return NSVF_ERR_INVALID;
+  if (bad_common(b, b_pts, n, m, n_max, ray_start, ray_dir, points)) return NSVF_ERR_INVALID;
   if ((int64_t)b * m == 0) return NSVF_OK;
+  if (!idx || !min_depth || !max_depth) return NSVF_ERR_INVALID;
   int blocks_per_row = (m + kRayBlock - 1) / kRayBlock;
   int64_t grid = (int64_t)b * blocks_per_row;
   if (grid > 0x7fffffff) return NSVF_ERR_INVALID;
@@ -256,8 +265,10 @@ static int svo_launch(bool sorted, int b, int b_pts, int n, int m, float voxelsi
                       const float *ray_start, const float *ray_dir, const float *points,
                       const int32_t *children, int32_t *idx, float *min_depth, float *max_depth,
                       uint8_t *hits, int32_t *err, void *workspace, void *stream) {
-  if (bad_common(b, b_pts, n, m, n_max, ray_start, ray_dir, points) || !children || !idx ||
-      !min_depth || !max_depth || !workspace || (sorted && (!hits || n_max > 128)))
+  if (bad_common(b, b_pts, n, m, n_max, ray_start, ray_dir, points) || !children || !workspace ||
+      (sorted && n_max > 128))
+    return NSVF_ERR_INVALID;
+  if ((int64_t)b * m > 0 && (!idx || !min_depth || !max_depth || (sorted && !hits)))
     return NSVF_ERR_INVALID;
   if (((uintptr_t)workspace) & 15) return NSVF_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
@@ -266,6 +277,7 @@ static int svo_launch(bool sorted, int b, int b_pts, int n, int m, float voxelsi
   int4 *kids = (int4 *)(box + total);
   float hv = voxelsize * 0.5f;
   pack_octree_kernel<<<nsvf_grid(total, 256), 256, 0, s>>>(total, hv, points, children, box, kids);
+  nsvf_count_launch();
   int64_t rays = (int64_t)b * m;
   if (rays == 0) return nsvf_launch_status();
   if (sorted)
@@ -299,11 +311,10 @@ int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, i
 int nsvf_ball_intersect(int b, int b_pts, int n, int m, float radius, int n_max,
                         const float *ray_start, const float *ray_dir, const float *points,
                         int32_t *idx, float *min_depth, float *max_depth, void *stream) {
-  if (bad_common(b, b_pts, n, m, n_max, ray_start, ray_dir, points) || !idx || !min_depth ||
-      !max_depth)
-    return NSVF_ERR_INVALID;
+  if (bad_common(b, b_pts, n, m, n_max, ray_start, ray_dir, points)) return NSVF_ERR_INVALID;
   int64_t rays = (int64_t)b * m;
   if (rays == 0) return NSVF_OK;
+  if (!idx || !min_depth || !max_depth) return NSVF_ERR_INVALID;
   ball_kernel<<<nsvf_grid(rays, kRayBlock), kRayBlock, 0, (cudaStream_t)stream>>>(
       rays, m, b_pts, n, radius, n_max, ray_start, ray_dir, points, idx, min_depth, max_depth);
   return nsvf_launch_status();

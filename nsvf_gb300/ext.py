@@ -13,11 +13,46 @@ trapping; ``check_errors()`` synchronises and raises if any was recorded.
 The sampling wrappers of nsvf_gb300.clib, which synchronise anyway for their
 output width, check it on every call.
 """
+import contextlib
+
 import torch
 
 from ._lib import LIB, check
 
 _err_words = {}
+
+# Optional per-op CUDA-event timing on the launching stream (used by bench.py
+# to report per-kernel durations inside its timed region).
+KERNEL_TIMING = False
+kernel_events = []
+
+
+@contextlib.contextmanager
+def _timed(name, device):
+    if not KERNEL_TIMING:
+        yield
+        return
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record(torch.cuda.current_stream(device))
+    yield
+    e.record(torch.cuda.current_stream(device))
+    kernel_events.append((name, s, e))
+
+
+def kernel_times_ms():
+    """{op: {"launches", "total_ms", "avg_ms"}} of the recorded events (synchronises)."""
+    torch.cuda.synchronize()
+    out = {}
+    for name, s, e in kernel_events:
+        d = out.setdefault(name, {"launches": 0, "total_ms": 0.0})
+        d["launches"] += 1
+        d["total_ms"] += s.elapsed_time(e)
+    for d in out.values():
+        d["avg_ms"] = d["total_ms"] / d["launches"]
+        d["total_ms"] = round(d["total_ms"], 4)
+        d["avg_ms"] = round(d["avg_ms"], 4)
+    return out
 
 
 def _stream(t):
@@ -51,6 +86,8 @@ def check_errors(device=None):
             what.append("malformed octree (child id out of range, cycle or too deep)")
         if v & 2:
             what.append("a ray needed more sample slots than max_steps / noise columns")
+        if v & 4:
+            what.append("a voxel or corner id out of range in trilinear interpolation")
         raise RuntimeError("nsvf_gb300: " + "; ".join(what))
 
 
@@ -144,10 +181,12 @@ def svo_intersect_sorted(ray_start, ray_dir, points, children, voxelsize, n_max)
     hi = torch.empty(B, M, n_max, dtype=torch.float32, device=dev)
     hits = torch.empty(B, M, dtype=torch.uint8, device=dev)
     ws = _svo_workspace(bp, N, dev)
-    check(LIB.nsvf_svo_intersect_sorted(B, bp, N, M, float(voxelsize), int(n_max), _ptr(ray_start),
-                                        _ptr(ray_dir), _ptr(points), _ptr(children), _ptr(idx),
-                                        _ptr(lo), _ptr(hi), _ptr(hits), _ptr(error_word(dev)),
-                                        _ptr(ws), _stream(ray_start)), "svo_intersect_sorted")
+    with _timed("svo_intersect_sorted", dev):
+        check(LIB.nsvf_svo_intersect_sorted(B, bp, N, M, float(voxelsize), int(n_max),
+                                            _ptr(ray_start), _ptr(ray_dir), _ptr(points),
+                                            _ptr(children), _ptr(idx), _ptr(lo), _ptr(hi),
+                                            _ptr(hits), _ptr(error_word(dev)), _ptr(ws),
+                                            _stream(ray_start)), "svo_intersect_sorted")
     return idx, lo, hi, hits.bool()
 
 
@@ -201,11 +240,12 @@ def inverse_cdf_sampling_rows(pts_idx, min_depth, max_depth, noise, probs, steps
     sd = torch.empty(rows, max_steps, dtype=torch.float32, device=dev)
     ss = torch.empty(rows, max_steps, dtype=torch.float32, device=dev)
     lay = (torch.tensor(layout, dtype=torch.int64)).contiguous()
-    check(LIB.nsvf_inverse_cdf_sampling(
-        rows, H, int(max_steps), noise.size(-1) if noise is not None else 0,
-        float(fixed_step_size), _ptr(pts_idx), _ptr(min_depth), _ptr(max_depth), _ptr(noise),
-        _ptr(probs), _ptr(steps), lay.data_ptr(), _ptr(si), _ptr(sd), _ptr(ss), _ptr(max_len),
-        _ptr(error_word(dev)), _stream(pts_idx)), "inverse_cdf_sampling")
+    with _timed("inverse_cdf_sampling", dev):
+        check(LIB.nsvf_inverse_cdf_sampling(
+            rows, H, int(max_steps), noise.size(-1) if noise is not None else 0,
+            float(fixed_step_size), _ptr(pts_idx), _ptr(min_depth), _ptr(max_depth), _ptr(noise),
+            _ptr(probs), _ptr(steps), lay.data_ptr(), _ptr(si), _ptr(sd), _ptr(ss), _ptr(max_len),
+            _ptr(error_word(dev)), _stream(pts_idx)), "inverse_cdf_sampling")
     return si, sd, ss
 
 
