@@ -136,6 +136,26 @@ int nsvf_inverse_cdf_sampling(int64_t rows, int max_hits, int max_steps, int noi
                               int32_t *sampled_idx, float *sampled_depth, float *sampled_dists,
                               int32_t *max_len, int32_t *err, void *stream);
 
+/* sample_count / sample_compact: the served renderer's form of the same
+ * inverse-CDF walk (deterministic 0.5 jitter, the wrapper's launch layout):
+ * sample_count writes count[r] = number of samples with a voxel id (not -1)
+ * of each ray; with offset = exclusive prefix sum of count (rows + 1
+ * entries), sample_compact writes those samples contiguously per ray, in
+ * order: voxel[j] (int32), xyz_dist[j] = (o + d * t, max(dist, 0)) as float4,
+ * depth[j] = t. This is exactly the list of valid samples the reference's
+ * renderer evaluates (fairnr/modules/encoder.py:538-556,
+ * fairnr/modules/renderer.py:86-100), without the padded [rows, M] tensors.
+ * ray_start is [rows, 3] (stride 3) or one shared origin (stride 0). */
+int nsvf_sample_count(int64_t rows, int max_hits, const int32_t *pts_idx, const float *min_depth,
+                      const float *max_depth, const float *probs, const float *steps,
+                      const int64_t layout[4], int32_t *count, void *stream);
+int nsvf_sample_compact(int64_t rows, int max_hits, const int32_t *pts_idx,
+                        const float *min_depth, const float *max_depth, const float *probs,
+                        const float *steps, const int64_t layout[4], const float *ray_start,
+                        int64_t ray_start_stride, const float *ray_dir, const int64_t *offset,
+                        int32_t *voxel, float *xyz_dist, float *depth, int32_t *err,
+                        void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Octree build (fairnr/clib/include/octree.h:10)                            */
 
@@ -202,6 +222,33 @@ int nsvf_composite_backward(int64_t rays, int max_steps, const float *free_energ
                             const float *grad_missed, const float *grad_colors,
                             float *grad_free_energy, float *grad_texture, int kahan,
                             void *stream);
+
+/* composite_segments: compositing of the compacted samples of the served
+ * renderer plus the background fill of NSVFModel.postprocessing
+ * (fairnr/models/nsvf.py:89-110). Ray r owns samples [offset[r],
+ * offset[r+1]); field [n, 4] = (sigma, r, g, b) (16-byte aligned);
+ * fe = relu(sigma) * dist * sigma_scale. Writes pixel[r] of out_color
+ * [., 3] = sum p c + missed * bg, out_depth = sum p t + missed * bg_depth
+ * and out_missed. */
+int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *field,
+                            const float *xyz_dist, const float *depth, const int64_t *pixel,
+                            float sigma_scale, const float bg[3], float bg_depth,
+                            float *out_color, float *out_depth, float *out_missed, int kahan,
+                            void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Field MLP on the tensor cores                                             */
+
+/* mlp_forward_bf16: the workloads' field MLP 32 -> 128 -> 128 -> 128 -> 128
+ * -> 4 (ReLU between layers) with tcgen05 BF16 MMAs and FP32 accumulation;
+ * replaces the nn.Linear stack the reference's field runs in FP32
+ * (fairnr/modules/implicit.py:42-75). emb [n, 32] FP32 (rounded to bf16 on
+ * load), weights[l] row-major [out, in] bf16 (128x32, 128x128 x3, 4x128),
+ * biases[l] FP32, out [n, 4] = (sigma, r, g, b) FP32. Hidden activations are
+ * rounded to bf16 between layers. Pointers 16-byte aligned. err bit 3: a
+ * pipeline wait timed out (kernel stopped early). */
+int nsvf_mlp_forward_bf16(int64_t n_samples, const float *emb, const void *const weights[5],
+                          const float *const biases[5], float *out, int32_t *err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -41,6 +41,10 @@ def _load():
                                            P, P], i32),
         "nsvf_composite": ([i64, i32, P, P, P, P, P, P, P, i32, P], i32),
         "nsvf_composite_backward": ([i64, i32, P, P, P, P, P, P, P, P, P, i32, P], i32),
+        "nsvf_mlp_forward_bf16": ([i64, P, P, P, P, P, P], i32),
+        "nsvf_sample_count": ([i64, i32, P, P, P, P, P, P, P, P], i32),
+        "nsvf_sample_compact": ([i64, i32, P, P, P, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
+        "nsvf_composite_segments": ([i64, P, P, P, P, P, f32, P, f32, P, P, P, i32, P], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -66,5 +70,6 @@ def exported_symbols():
         "nsvf_svo_intersect", "nsvf_svo_intersect_sorted", "nsvf_ball_intersect",
         "nsvf_uniform_ray_sampling", "nsvf_inverse_cdf_sampling", "nsvf_build_octree",
         "nsvf_trilinear_embed", "nsvf_trilinear_embed_backward", "nsvf_composite",
-        "nsvf_composite_backward",
+        "nsvf_composite_backward", "nsvf_mlp_forward_bf16", "nsvf_sample_count",
+        "nsvf_sample_compact", "nsvf_composite_segments",
     ]

@@ -161,9 +161,72 @@ __global__ void __launch_bounds__(kWarps * 32) composite_bwd_kernel(
   }
 }
 
+// Served path: compositing of compacted samples. Ray r owns samples
+// [offset[r], offset[r+1]) (its valid samples in depth order); field[s] =
+// (sigma, r, g, b), xyzd[s].w = distance, depth[s]. Writes pixel pix[r] of
+// the frame: color = sum p c + missed * bg, depth = sum p t + missed *
+// bg_depth, missed. fe = relu(sigma) * dist * sigma_scale as the reference
+// renderer (fairnr/modules/renderer.py:117-121).
+__global__ void __launch_bounds__(kWarps * 32) composite_segments_kernel(
+    int64_t rays, const int64_t *__restrict__ offset, const float4 *__restrict__ field,
+    const float4 *__restrict__ xyzd, const float *__restrict__ depth,
+    const int64_t *__restrict__ pix, float sigma_scale, float bg_r, float bg_g, float bg_b,
+    float bg_depth, float *__restrict__ out_color, float *__restrict__ out_depth,
+    float *__restrict__ out_missed, int kahan) {
+  int lane = threadIdx.x & 31;
+  int64_t r = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
+  if (r >= rays) return;
+  int64_t a = offset[r], n = offset[r + 1] - a;
+  Prefix carry{0.f, 0.f};
+  float sp = 0.f, sd = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+  for (int64_t base = 0; base < n; base += 32) {
+    int64_t i = base + lane;
+    bool in = i < n;
+    float4 f = in ? field[a + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float dist = in ? xyzd[a + i].w : 0.f;
+    float fe = (fmaxf(f.x, 0.0f) * dist) * sigma_scale;
+    float pre = chunk_prefix(fe, lane, carry, kahan != 0);
+    if (in) {
+      float p = (1.0f - expf(-fe)) * expf(-pre);
+      sp += p;
+      sd += p * depth[a + i];
+      c0 += p * f.y; c1 += p * f.z; c2 += p * f.w;
+    }
+  }
+  sp = warp_sum(sp);
+  sd = warp_sum(sd);
+  c0 = warp_sum(c0); c1 = warp_sum(c1); c2 = warp_sum(c2);
+  if (lane == 0) {
+    int64_t q = pix[r];
+    float missed = 1.0f - sp;
+    out_color[q * 3 + 0] = c0 + missed * bg_r;
+    out_color[q * 3 + 1] = c1 + missed * bg_g;
+    out_color[q * 3 + 2] = c2 + missed * bg_b;
+    out_depth[q] = sd + missed * bg_depth;
+    out_missed[q] = missed;
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *field,
+                            const float *xyz_dist, const float *depth, const int64_t *pixel,
+                            float sigma_scale, const float bg[3], float bg_depth,
+                            float *out_color, float *out_depth, float *out_missed, int kahan,
+                            void *stream) {
+  if (rays < 0 || !bg) return NSVF_ERR_INVALID;
+  if (rays == 0) return NSVF_OK;
+  if (!offset || !field || !xyz_dist || !depth || !pixel || !out_color || !out_depth ||
+      !out_missed || ((((uintptr_t)field) | ((uintptr_t)xyz_dist)) & 15))
+    return NSVF_ERR_INVALID;
+  composite_segments_kernel<<<nsvf_grid(rays, kWarps), kWarps * 32, 0, (cudaStream_t)stream>>>(
+      rays, offset, (const float4 *)field, (const float4 *)xyz_dist, depth, pixel, sigma_scale,
+      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan);
+  return nsvf_launch_status();
+}
+
 
 int nsvf_composite(int64_t rays, int max_steps, const float *free_energy, const float *texture,
                    const float *sampled_depth, float *probs, float *depth, float *missed,

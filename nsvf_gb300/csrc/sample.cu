@@ -19,8 +19,95 @@ __device__ __forceinline__ void warp_max_atomic(int32_t *dst, int v, bool live) 
   if ((threadIdx.x & 31) == (__ffs(mask) - 1) && dst) atomicMax(dst, x);
 }
 
-// One thread walks one ray's piecewise-uniform CDF over its hit intervals
-// (fairnr/clib/src/sample_gpu.cu:108-202).
+// Walk of one ray's piecewise-uniform CDF over its hit intervals
+// (fairnr/clib/src/sample_gpu.cu:108-202). `emit(id, depth, dist)` receives
+// the samples in order and returns false when it has no room (the walk then
+// stops and reports overflow). Returns true on overflow.
+//   I, lo, hi, pr : this ray's H slots; I0 : the block's first row (tail
+//   test); nxt : row whose first id is read when the tail runs past slot H
+//   (-1 = none); U : jitter row (NULL = 0.5), noise_cols its width.
+template <typename Emit>
+__device__ __forceinline__ bool icdf_walk(int H, const int32_t *__restrict__ I,
+                                          const int32_t *__restrict__ I0,
+                                          const int32_t *__restrict__ pts_all, int64_t nxt,
+                                          const float *__restrict__ lo,
+                                          const float *__restrict__ hi,
+                                          const float *__restrict__ pr, float steps,
+                                          const float *__restrict__ U, int noise_cols,
+                                          float fixed_step_size, Emit &emit) {
+  int bin = 0;
+  float cmin = lo[0], cmax = hi[0];
+  float cdf_lo = 0.0f, cdf_hi = pr[0];
+  float step_size = __double2float_rn(__ddiv_rn(1.0, (double)steps));
+  float z_low = cmin;
+  int total_steps = (int)ceilf(steps);
+  bool done = false;
+  if (fixed_step_size > 0.0f) step_size = fixed_step_size;
+
+  for (int st = 0; st < total_steps; ++st) {
+    if (U && st >= noise_cols) return true;
+    float u0 = U ? U[st] : 0.5f;
+    float cdf = __fmul_rn(__fadd_rn((float)st, u0), step_size);
+    while (cdf > cdf_hi) {
+      if (!emit(I[bin], __fmul_rn(__fadd_rn(cmax, z_low), 0.5f), __fsub_rn(cmax, z_low)))
+        return true;
+      bin++;
+      if (bin >= H || I[bin] == -1) { done = true; break; }
+      cmin = lo[bin]; cmax = hi[bin];
+      cdf_lo = cdf_hi;
+      cdf_hi = __fadd_rn(cdf_hi, pr[bin]);
+      z_low = cmin;
+    }
+    if (done) break;
+    float u = __fdiv_rn(__fsub_rn(cdf, cdf_lo), __fsub_rn(cdf_hi, cdf_lo));
+    float z = __fmaf_rn(u, __fsub_rn(cmax, cmin), cmin);
+    if (!emit(I[bin], __fmul_rn(__fadd_rn(z, z_low), 0.5f), __fsub_rn(z, z_low))) return true;
+    z_low = z;
+  }
+  // Tail: the reference runs it even after `done` (`~done` is always true),
+  // re-emitting the last partial segment; with bin == H it reads the first
+  // id of the next row in memory, and it tests emptiness on the block's
+  // first row (fairnr/clib/src/sample_gpu.cu:188-201).
+  while (z_low < cmax) {
+    int32_t id;
+    if (bin < H) id = I[bin];
+    else id = (nxt >= 0) ? pts_all[nxt * H] : -1;
+    if (!emit(id, __fmul_rn(__fadd_rn(cmax, z_low), 0.5f), __fsub_rn(cmax, z_low))) return true;
+    bin++;
+    if (bin >= H || I0[bin] == -1) break;
+    cmin = lo[bin]; cmax = hi[bin];
+    z_low = cmin;
+  }
+  return false;
+}
+
+// Rows the reference's tail reads outside a ray's own row, from the launch
+// layout (see include/nsvf_gb300.h): tail row and next row of ray r.
+__device__ __forceinline__ void icdf_rows(int64_t r, int64_t K, int64_t C, int64_t N, int64_t G,
+                                          int64_t &tail, int64_t &nxt) {
+  int64_t g = r / K, i = r % K;
+  int64_t c0 = (i / C) * C, W = min(C, K - c0), ii = i - c0;
+  tail = g * K + c0;
+  if (tail >= N) tail = 0;
+  if (ii + 1 < W) nxt = r + 1;
+  else nxt = (g + 1 < G) ? (g + 1) * K + c0 : -1;
+  if (nxt >= N) nxt = 0;
+}
+
+struct RowEmit {
+  int32_t *SI;
+  float *SD, *SS;
+  int M, s, valid;
+  __device__ bool operator()(int32_t id, float depth, float dist) {
+    if (s >= M) return false;
+    SI[s] = id; SD[s] = depth; SS[s] = dist;
+    valid += (id != -1);
+    ++s;
+    return true;
+  }
+};
+
+// One thread per ray: the padded [rows, M] outputs of the reference op.
 __global__ void __launch_bounds__(kBlock) inverse_cdf_kernel(
     int64_t rows, int H, int M, int noise_stride, float fixed_step_size,
     const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
@@ -32,79 +119,84 @@ __global__ void __launch_bounds__(kBlock) inverse_cdf_kernel(
   bool live = r < rows;
   int valid = 0;
   if (live) {
-    // Rows the reference reads outside this ray (see include/nsvf_gb300.h).
-    int64_t g = r / K, i = r % K;
-    int64_t c0 = (i / C) * C, W = min(C, K - c0), ii = i - c0;
-    int64_t tail = g * K + c0;
-    if (tail >= N) tail = 0;
-    int64_t nxt;
-    if (ii + 1 < W) nxt = r + 1;
-    else nxt = (g + 1 < G) ? (g + 1) * K + c0 : -1;
-    if (nxt >= N) nxt = 0;
-
-    const int32_t *I = pts_idx + r * H;
-    const int32_t *I0 = pts_idx + tail * H;
-    const float *lo = min_depth + r * H, *hi = max_depth + r * H, *pr = probs + r * H;
-    const float *U = noise ? noise + r * noise_stride : nullptr;
-    int32_t *SI = s_idx + r * M;
-    float *SD = s_depth + r * M, *SS = s_dist + r * M;
-
-    int bin = 0, s = 0;
-    float cmin = lo[0], cmax = hi[0];
-    float cdf_lo = 0.0f, cdf_hi = pr[0];
-    float step_size = __double2float_rn(__ddiv_rn(1.0, (double)steps[r]));
-    float z_low = cmin;
-    int total_steps = (int)ceilf(steps[r]);
-    bool done = false, overflow = false;
-    if (fixed_step_size > 0.0f) step_size = fixed_step_size;
-
-    for (int st = 0; st < total_steps; ++st) {
-      if (st >= noise_stride && U) { overflow = true; break; }
-      float u0 = U ? U[st] : 0.5f;
-      float cdf = __fmul_rn(__fadd_rn((float)st, u0), step_size);
-      while (cdf > cdf_hi) {
-        if (s >= M) { overflow = true; break; }
-        int32_t id = I[bin];
-        SI[s] = id; SS[s] = __fsub_rn(cmax, z_low);
-        SD[s] = __fmul_rn(__fadd_rn(cmax, z_low), 0.5f);
-        valid += (id != -1);
-        bin++; s++;
-        if (bin >= H || I[bin] == -1) { done = true; break; }
-        cmin = lo[bin]; cmax = hi[bin];
-        cdf_lo = cdf_hi;
-        cdf_hi = __fadd_rn(cdf_hi, pr[bin]);
-        z_low = cmin;
-      }
-      if (done || overflow) break;
-      if (s >= M) { overflow = true; break; }
-      float u = __fdiv_rn(__fsub_rn(cdf, cdf_lo), __fsub_rn(cdf_hi, cdf_lo));
-      float z = __fmaf_rn(u, __fsub_rn(cmax, cmin), cmin);
-      int32_t id = I[bin];
-      SI[s] = id; SS[s] = __fsub_rn(z, z_low); SD[s] = __fmul_rn(__fadd_rn(z, z_low), 0.5f);
-      valid += (id != -1);
-      z_low = z; s++;
-    }
-    // Tail: the reference runs it even after `done` (`~done` is always true),
-    // re-emitting the last partial segment; with bin == H it reads the first
-    // id of the next row in memory, and it tests emptiness on the block's
-    // first row (fairnr/clib/src/sample_gpu.cu:188-201).
-    while (!overflow && z_low < cmax) {
-      if (s >= M) { overflow = true; break; }
-      int32_t id;
-      if (bin < H) id = I[bin];
-      else id = (nxt >= 0) ? pts_idx[nxt * H] : -1;
-      SI[s] = id; SS[s] = __fsub_rn(cmax, z_low);
-      SD[s] = __fmul_rn(__fadd_rn(cmax, z_low), 0.5f);
-      valid += (id != -1);
-      bin++; s++;
-      if (bin >= H || I0[bin] == -1) break;
-      cmin = lo[bin]; cmax = hi[bin];
-      z_low = cmin;
-    }
-    for (int q = s; q < M; ++q) { SI[q] = -1; SD[q] = 0.0f; SS[q] = 0.0f; }
+    int64_t tail, nxt;
+    icdf_rows(r, K, C, N, G, tail, nxt);
+    RowEmit em{s_idx + r * M, s_depth + r * M, s_dist + r * M, M, 0, 0};
+    bool overflow = icdf_walk(H, pts_idx + r * H, pts_idx + tail * H, pts_idx, nxt,
+                              min_depth + r * H, max_depth + r * H, probs + r * H, steps[r],
+                              noise ? noise + r * noise_stride : nullptr, noise_stride,
+                              fixed_step_size, em);
+    for (int q = em.s; q < M; ++q) { em.SI[q] = -1; em.SD[q] = 0.0f; em.SS[q] = 0.0f; }
+    valid = em.valid;
     if (overflow && err) atomicOr(err, 2);
   }
   warp_max_atomic(max_len, valid, live);
+}
+
+// Served path, pass 1: number of valid (id != -1) samples of each ray.
+struct CountEmit {
+  int n;
+  __device__ bool operator()(int32_t id, float, float) {
+    n += (id != -1);
+    return true;
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) icdf_count_kernel(
+    int64_t rows, int H, const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
+    const float *__restrict__ max_depth, const float *__restrict__ probs,
+    const float *__restrict__ steps, int64_t K, int64_t C, int64_t N, int64_t G,
+    int32_t *__restrict__ count) {
+  int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (r >= rows) return;
+  int64_t tail, nxt;
+  icdf_rows(r, K, C, N, G, tail, nxt);
+  CountEmit em{0};
+  icdf_walk(H, pts_idx + r * H, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H,
+            max_depth + r * H, probs + r * H, steps[r], nullptr, 0, -1.0f, em);
+  count[r] = em.n;
+}
+
+// Served path, pass 2: the valid samples of every ray, compacted in ray
+// order at offset[r]: voxel id, (x, y, z, clamped distance) and depth,
+// with x = o + d * t as the renderer computes it.
+struct CompactEmit {
+  int32_t *vox;
+  float4 *xyzd;
+  float *depth;
+  float ox, oy, oz, dx, dy, dz;
+  int64_t pos, end;
+  __device__ bool operator()(int32_t id, float t, float dist) {
+    if (id == -1) return true;
+    if (pos >= end) return false;
+    vox[pos] = id;
+    xyzd[pos] = make_float4(__fadd_rn(ox, __fmul_rn(dx, t)), __fadd_rn(oy, __fmul_rn(dy, t)),
+                            __fadd_rn(oz, __fmul_rn(dz, t)), fmaxf(dist, 0.0f));
+    depth[pos] = t;
+    ++pos;
+    return true;
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) icdf_compact_kernel(
+    int64_t rows, int H, const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
+    const float *__restrict__ max_depth, const float *__restrict__ probs,
+    const float *__restrict__ steps, int64_t K, int64_t C, int64_t N, int64_t G,
+    const float *__restrict__ ray_start, int64_t ray_start_stride,
+    const float *__restrict__ ray_dir, const int64_t *__restrict__ offset,
+    int32_t *__restrict__ vox, float4 *__restrict__ xyzd, float *__restrict__ depth,
+    int32_t *__restrict__ err) {
+  int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (r >= rows) return;
+  int64_t tail, nxt;
+  icdf_rows(r, K, C, N, G, tail, nxt);
+  const float *o = ray_start + r * ray_start_stride;
+  CompactEmit em{vox, xyzd, depth, o[0], o[1], o[2], ray_dir[r * 3], ray_dir[r * 3 + 1],
+                 ray_dir[r * 3 + 2], offset[r], offset[r + 1]};
+  bool overflow = icdf_walk(H, pts_idx + r * H, pts_idx + tail * H, pts_idx, nxt,
+                            min_depth + r * H, max_depth + r * H, probs + r * H, steps[r],
+                            nullptr, 0, -1.0f, em);
+  if ((overflow || em.pos != em.end) && err) atomicOr(err, 2);
 }
 
 // Uniform sampler (fairnr/clib/src/sample_gpu.cu:15-106): merge interval
@@ -187,6 +279,39 @@ int nsvf_inverse_cdf_sampling(int64_t rows, int max_hits, int max_steps, int noi
   inverse_cdf_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
       rows, max_hits, max_steps, noise_stride, fixed_step_size, pts_idx, min_depth, max_depth,
       noise, probs, steps, K, C, N, G, sampled_idx, sampled_depth, sampled_dists, max_len, err);
+  return nsvf_launch_status();
+}
+
+int nsvf_sample_count(int64_t rows, int max_hits, const int32_t *pts_idx, const float *min_depth,
+                      const float *max_depth, const float *probs, const float *steps,
+                      const int64_t layout[4], int32_t *count, void *stream) {
+  if (rows < 0 || max_hits < 1 || !layout) return NSVF_ERR_INVALID;
+  if (rows == 0) return NSVF_OK;
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !count) return NSVF_ERR_INVALID;
+  int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
+  if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
+  icdf_count_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, count);
+  return nsvf_launch_status();
+}
+
+int nsvf_sample_compact(int64_t rows, int max_hits, const int32_t *pts_idx,
+                        const float *min_depth, const float *max_depth, const float *probs,
+                        const float *steps, const int64_t layout[4], const float *ray_start,
+                        int64_t ray_start_stride, const float *ray_dir, const int64_t *offset,
+                        int32_t *voxel, float *xyz_dist, float *depth, int32_t *err,
+                        void *stream) {
+  if (rows < 0 || max_hits < 1 || !layout || (ray_start_stride != 0 && ray_start_stride != 3))
+    return NSVF_ERR_INVALID;
+  if (rows == 0) return NSVF_OK;
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !ray_start || !ray_dir ||
+      !offset || !voxel || !xyz_dist || !depth || (((uintptr_t)xyz_dist) & 15))
+    return NSVF_ERR_INVALID;
+  int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
+  if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
+  icdf_compact_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, ray_start,
+      ray_start_stride, ray_dir, offset, voxel, (float4 *)xyz_dist, depth, err);
   return nsvf_launch_status();
 }
 

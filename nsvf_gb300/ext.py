@@ -88,6 +88,8 @@ def check_errors(device=None):
             what.append("a ray needed more sample slots than max_steps / noise columns")
         if v & 4:
             what.append("a voxel or corner id out of range in trilinear interpolation")
+        if v & 8:
+            what.append("a tensor-core pipeline wait timed out")
         raise RuntimeError("nsvf_gb300: " + "; ".join(what))
 
 

@@ -238,8 +238,10 @@ def test_edge_cases(cuda):
     # wrong dtype / layout raise like the reference's TORCH_CHECK
     with pytest.raises(RuntimeError):
         ext.svo_intersect(o.double(), d, cen, chi, vs, 8)
+    strided = torch.zeros(1, 2, 6, device=cuda)[..., ::2]
+    assert not strided.is_contiguous()
     with pytest.raises(RuntimeError):
-        ext.aabb_intersect(o.transpose(0, 1), d, cen, vs, 8)
+        ext.aabb_intersect(strided, d, cen, vs, 8)
     # a malformed octree (child id out of range) is reported, not faulted
     bad = chi.clone()
     bad[0, -1, 0] = 10 ** 6

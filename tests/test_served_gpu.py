@@ -1,0 +1,116 @@
+"""The served renderer (compacted samples, tcgen05 BF16 MLP, compensated
+compositing) against the drop-in FP32 path and the float64 oracle.
+
+The geometry is shared: the served path must evaluate exactly the samples
+the drop-in path evaluates (same count, same voxel ids). Colours: BF16 field
+vs the FP32 render within 2e-3 max abs RGB error, the workload's bar."""
+import argparse
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(dev, voxel, embed_std, sigma_scale, sigma_bias, max_hits):
+    from nsvf_gb300 import scenes
+    from nsvf_gb300.encoder import SparseVoxelEncoder
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.renderer import VolumeRenderer
+    if voxel == 0.25:
+        p, vs = scenes.scene_small()
+    else:
+        p, vs = scenes.scene_shell(voxel)
+    args = argparse.Namespace(voxel_size=vs, max_hits=max_hits, raymarching_stepsize_ratio=0.125,
+                              voxel_embed_dim=32, use_octree=True, deterministic_step=True,
+                              chunk_size=64)
+    enc = SparseVoxelEncoder(args, points=p)
+    with torch.no_grad():
+        enc.values.weight.copy_(scenes.voxel_embeddings(enc.values.weight.shape[0], 32,
+                                                        embed_std, seed=1))
+    field = StandInField(weights=scenes.stand_in_mlp_weights(seed=2, sigma_scale=sigma_scale,
+                                                             sigma_bias=sigma_bias))
+    return enc.to(dev).eval(), field.to(dev).eval(), VolumeRenderer(args).eval(), vs
+
+
+@pytest.mark.parametrize("voxel,size,std,ss,sb,H", [
+    (0.25, 64, 1.0, 60.0, 0.5, 20),          # small scene, opaque field
+    (1.0 / 32, 160, 1.0, 30.0, 0.5, 64),     # shell scene
+    (1.0 / 32, 160, 0.01, 1.0, 0.0, 64),     # the workloads' near-transparent init
+])
+def test_served_matches_dropin(cuda, voxel, size, std, ss, sb, H):
+    from nsvf_gb300 import ext, scenes
+    from nsvf_gb300.renderer import render_rays
+    from nsvf_gb300.served import SceneState, render_frame
+    enc, field, ren, vs = _scene(cuda, voxel, std, ss, sb, H)
+    rs, rd = scenes.pinhole_rays(scenes.sphere_cameras(3, 4.0, seed=9)[1], size, size,
+                                 80.0 * size / 64.0)
+    rs_t = torch.from_numpy(rs).to(cuda)
+    rd_t = torch.from_numpy(rd).to(cuda)
+    with torch.no_grad():
+        ref = render_rays(enc, field, ren, rs_t.reshape(1, 1, 1, 3), rd_t.reshape(1, 1, -1, 3))
+    scene = SceneState(enc, field)
+    out = render_frame(scene, rs_t, rd_t)
+    ext.check_errors(cuda)
+    col = out["colors"].cpu().numpy()
+    rcol = ref["colors"].reshape(-1, 3).cpu().numpy()
+    err = np.abs(col - rcol).max()
+    assert err <= 2e-3, err
+    np.testing.assert_allclose(out["missed"].cpu().numpy(), ref["missed"].reshape(-1).cpu().numpy(),
+                               atol=2e-3)
+    # same set of evaluated samples as the drop-in path
+    with torch.no_grad():
+        st = enc.precompute(id=None)
+        _, _, inter, hits = enc.ray_intersect(rs_t.reshape(1, 1, 1, 3), rd_t.reshape(1, 1, -1, 3),
+                                              {k: (v.unsqueeze(0) if v is not None else None)
+                                               for k, v in st.items()})
+        d = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
+        inter['probs'] = d / d.sum(-1, keepdim=True)
+        inter['steps'] = d.sum(-1) / enc.step_size
+        sub = {k: v[hits] for k, v in inter.items()}
+        smp = enc.ray_sample(sub)
+    assert out["n_samples"] == int(smp['sampled_point_voxel_idx'].ne(-1).sum())
+    assert out["n_hit_rays"] == int(hits.sum())
+
+
+def test_served_vs_float64_oracle(cuda):
+    """Max and RMS RGB error of the served BF16 frame against a float64 render
+    of the same samples (oracle), small opaque scene."""
+    from nsvf_gb300 import scenes
+    from nsvf_gb300.served import SceneState, render_frame
+    from oracle import cpu
+    enc, field, ren, vs = _scene(cuda, 0.25, 1.0, 60.0, 0.5, 20)
+    rs, rd = scenes.small_view(0)
+    scene = SceneState(enc, field)
+    out = render_frame(scene, torch.from_numpy(rs).to(cuda), torch.from_numpy(rd).to(cuda))
+    col = out["colors"].cpu().numpy()
+    # float64 oracle on the same rays
+    st = enc.precompute(id=None)
+    cen, chi = st['voxel_octree_center_xyz'].cpu().numpy(), st['voxel_octree_children_idx'].cpu().numpy()
+    R = rd.shape[0]
+    idx, lo, hi = cpu.sort_hits(*cpu.svo_intersect(np.broadcast_to(rs, (R, 3))[None], rd[None],
+                                                   cen[None], chi[None], vs, 20))
+    idx, lo, hi = idx[0], lo[0], hi[0]
+    hit = (idx != -1).any(-1)
+    pr, stp = cpu.probs_steps(idx[hit], lo[hit], hi[hit], vs / 8)
+    N = int(hit.sum())
+    M = int(np.ceil(stp).max()) + 20
+    si, sd, ss = cpu.inverse_cdf_op(idx[hit], lo[hit], hi[hit], pr, stp, np.full((N, M), 0.5, np.float32))
+    ss = np.maximum(ss, 0)
+    mask = si != -1
+    xyz = rs[None, None].astype(np.float64) + rd[hit][:, None].astype(np.float64) * sd[..., None]
+    emb = cpu.trilinear_embed(xyz[mask], si[mask], st['voxel_center_xyz'].cpu().numpy(),
+                              st['voxel_vertex_idx'].cpu().numpy(),
+                              st['voxel_vertex_emb'].detach().cpu().numpy(), vs)
+    W = [(l.weight.detach().cpu().numpy(), l.bias.detach().cpu().numpy()) for l in field.layers]
+    sig, rgb = cpu.mlp_forward(emb, W)
+    S = np.zeros(mask.shape)
+    C = np.zeros(mask.shape + (3,))
+    S[mask], C[mask] = sig, rgb
+    o = cpu.composite(S, C, sd.astype(np.float64), ss.astype(np.float64), mask)
+    ref = np.ones((R, 3))
+    ref[hit] = o["colors"] + o["missed"][:, None]
+    err = np.abs(col - ref)
+    assert err.max() <= 2e-3, err.max()
+    assert np.sqrt((err ** 2).mean()) <= 5e-4
