@@ -162,10 +162,18 @@ def run_ours(a):
         host.append((rst, rdt))
     dev_in = [(h[0].to(dev), h[1].to(dev)) for h in host]
 
-    def step(rs, rd):
-        with torch.no_grad():
-            return render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3),
-                               encoder_states=states)
+    if a.path == "served":
+        from nsvf_gb300.served import SceneState, render_frame
+        scene = SceneState(enc, field)
+
+        def step(rs, rd):
+            with torch.no_grad():
+                return render_frame(scene, rs, rd)
+    else:
+        def step(rs, rd):
+            with torch.no_grad():
+                return render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3),
+                                   rd.reshape(1, 1, -1, 3), encoder_states=states)
 
     # --- device-resident timing (value) ---
     ext.KERNEL_TIMING = True
@@ -179,6 +187,7 @@ def run_ours(a):
     clocks = ClockSampler(local)
     clocks.start()
     times = []
+    out_samples = [0]
     l0 = LIB.nsvf_launch_count()
     for i in range(a.steps):
         flush.zero_()
@@ -188,6 +197,7 @@ def run_ours(a):
         e.record()
         torch.cuda.synchronize()
         times.append(s.elapsed_time(e) / 1e3)
+        out_samples[0] += int(out.get("n_samples", 0) or 0)
     launches = LIB.nsvf_launch_count() - l0
     clk = clocks.stop()
     ext.KERNEL_TIMING = False
@@ -241,7 +251,19 @@ def run_ours(a):
     alg = RAYS_PER_FRAME * 24 + Nn * 48 + RAYS_PER_FRAME * MAX_HITS * 12 + RAYS_PER_FRAME
     k = kernel_ms.get("svo_intersect_sorted")
     roof = None
-    if k:
+    if a.path == "served" and kernel_ms.get("mlp_forward_bf16"):
+        # the tensor-core MLP dominates the served path: 107,520 FLOP per
+        # sample (2 * (32*128 + 3*128*128 + 128*4)) x samples per launch
+        km = kernel_ms["mlp_forward_bf16"]
+        flops = 107520.0 * out_samples[0] / max(1, km["launches"]) if out_samples[0] else 0
+        ach = flops / (km["avg_ms"] / 1e3) / 1e12
+        tpk = peaks["bf16_tflops"] if peaks else 1900.0
+        roof = {"kernel": "mlp_forward_bf16", "bound": "tensor", "achieved": round(ach, 1),
+                "peak": tpk, "unit": "TFLOP/s", "frac": round(ach / tpk, 4),
+                "peak_source": "measured (bf16 burst)" if peaks else "fallback",
+                "algorithmic_flops_per_launch": flops, "avg_launch_ms": km["avg_ms"],
+                "traffic": None}
+    elif k:
         ach = alg / (k["avg_ms"] / 1e3) / 1e9
         roof = {"kernel": "svo_intersect_sorted", "bound": "hbm", "achieved": round(ach, 1),
                 "peak": hbm_peak, "unit": "GB/s", "frac": round(ach / hbm_peak, 4),
@@ -253,7 +275,7 @@ def run_ours(a):
         "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(statistics.mean(ms), 3),
         "p50_ms": round(float(np.percentile(ms, 50)), 3), "p99_ms": round(float(np.percentile(ms, 99)), 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 MLP / f32 geometry" if a.path == "served" else "f32",
         "data": "synthetic (seeded scene, embeddings, MLP and cameras)",
         "config": {"workload": "c2: 125,476-voxel sphere+torus shell, 800x800 frame, SVO, "
                                "max_hits 64, step 1/512, 4x128 MLP", "path": a.path,

@@ -58,9 +58,11 @@ class SceneState:
         return sum(t.numel() * t.element_size() for t in ts)
 
 
-def render_frame(scene, ray_start, ray_dir, kahan=True, out=None):
+def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     """ray_start [3] (shared origin) or [R, 3], ray_dir [R, 3] (FP32, on the
-    scene's device) -> dict(colors [R, 3], depths [R], missed [R])."""
+    scene's device) -> dict(colors [R, 3], depths [R], missed [R]).
+    mlp: "tc" (tcgen05 BF16 kernel), "bf16_emulated" (torch emulation of the
+    kernel's rounding) or "fp32" (the field's FP32 torch forward)."""
     dev = scene.device
     R = ray_dir.shape[0]
     rd = ray_dir.float().contiguous()
@@ -109,7 +111,12 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None):
                                       stream), "sample_compact")
     emb = trilinear_embed(vox, xyzd[:, :3], scene.centers, scene.feats, scene.values,
                           scene.voxel_size)
-    field = scene.mlp(emb)
+    if mlp == "tc":
+        field = scene.mlp(emb)
+    elif mlp == "bf16_emulated":
+        field = scene.mlp.reference_bf16(emb).contiguous()
+    else:
+        field = scene.field.mlp(emb).float().contiguous()
     with ext._timed("composite_segments", dev):
         check(LIB.nsvf_composite_segments(
             n, _p(offset), _p(field), _p(xyzd), _p(depth), _p(pix), 7.0, scene.bg,
