@@ -250,6 +250,33 @@ int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *fi
 int nsvf_mlp_forward_bf16(int64_t n_samples, const float *emb, const void *const weights[5],
                           const float *const biases[5], float *out, int32_t *err, void *stream);
 
+/* field_samples_bf16: trilinear interpolation (as nsvf_trilinear_embed,
+ * bit-identical FP32 embedding) fused into the input stage of the
+ * tensor-core MLP: voxel [n] int32, xyz_dist [n, 4] FP32 (x, y, z, .),
+ * centers [n_voxels, 3], feats [n_voxels, 8] int32, values [n_keys, 32]
+ * FP32 -> out [n, 4] = (sigma, r, g, b). The embedding never reaches HBM.
+ * feats, values, xyz_dist, out 16-byte aligned. */
+int nsvf_field_samples_bf16(int64_t n_samples, const int32_t *voxel, const float *xyz_dist,
+                            int64_t n_voxels, int64_t n_keys, float voxel_size,
+                            const float *centers, const int32_t *feats, const float *values,
+                            const void *const weights[5], const float *const biases[5],
+                            float *out, int32_t *err, void *stream);
+
+/* prune_scores_bf16: self-pruning scores (SparseVoxelEncoder.get_scores,
+ * fairnr/modules/encoder.py:620-654) in one kernel: for every voxel v,
+ * bits^3 points at the offset_points positions around centers[v]
+ * (fairnr/data/geometry.py:229-238), their embedding, the MLP's sigma, and
+ *   rule 0 (reference pruning, encoder.py:610): score[v] = min exp(-relu s)
+ *   rule 1 (sigma * step rule):                score[v] = max 1 - exp(-relu(s) step)
+ * reduced into score[v] (FP32 bits, as uint32) with atomics: initialise
+ * score to 0x7f800000 (+inf) for rule 0 and 0 for rule 1. keep is then
+ * 1 - score > th (rule 0) or score >= th (rule 1). */
+int nsvf_prune_scores_bf16(int64_t n_voxels, int bits, int rule, float step, int64_t n_keys,
+                           float voxel_size, const float *centers, const int32_t *feats,
+                           const float *values, const void *const weights[5],
+                           const float *const biases[5], uint32_t *score, int32_t *err,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

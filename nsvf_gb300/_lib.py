@@ -42,6 +42,8 @@ def _load():
         "nsvf_composite": ([i64, i32, P, P, P, P, P, P, P, i32, P], i32),
         "nsvf_composite_backward": ([i64, i32, P, P, P, P, P, P, P, P, P, i32, P], i32),
         "nsvf_mlp_forward_bf16": ([i64, P, P, P, P, P, P], i32),
+        "nsvf_field_samples_bf16": ([i64, P, P, i64, i64, f32, P, P, P, P, P, P, P, P], i32),
+        "nsvf_prune_scores_bf16": ([i64, i32, i32, f32, i64, f32, P, P, P, P, P, P, P, P], i32),
         "nsvf_sample_count": ([i64, i32, P, P, P, P, P, P, P, P], i32),
         "nsvf_sample_compact": ([i64, i32, P, P, P, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
         "nsvf_composite_segments": ([i64, P, P, P, P, P, f32, P, f32, P, P, P, i32, P], i32),
@@ -71,5 +73,6 @@ def exported_symbols():
         "nsvf_uniform_ray_sampling", "nsvf_inverse_cdf_sampling", "nsvf_build_octree",
         "nsvf_trilinear_embed", "nsvf_trilinear_embed_backward", "nsvf_composite",
         "nsvf_composite_backward", "nsvf_mlp_forward_bf16", "nsvf_sample_count",
-        "nsvf_sample_compact", "nsvf_composite_segments",
+        "nsvf_sample_compact", "nsvf_composite_segments", "nsvf_field_samples_bf16",
+        "nsvf_prune_scores_bf16",
     ]

@@ -46,14 +46,72 @@ struct __align__(128) MlpSmem {
   int abort;
 };
 
+// Where a tile's 128 rows come from and where their outputs go.
+enum Mode : int {
+  kEmbIn = 0,      // rows = embeddings emb[n, 32]; out[n] = (sigma, r, g, b)
+  kSamplesIn = 1,  // rows = samples (voxel id, xyz): trilinear interpolation in
+                   // the input stage; out[n] = (sigma, r, g, b)
+  kPrune = 2,      // rows = bits^3 points per voxel; per-voxel score reduced
+                   // with atomics into score[v]
+};
+
 struct MlpParams {
-  const float *emb;                  // [ns, 32] fp32
+  const float *emb;                  // kEmbIn: [ns, 32] fp32
+  const int32_t *vox;                // kSamplesIn: [ns] voxel ids
+  const float4 *xyzd;                // kSamplesIn: [ns] (x, y, z, .)
+  const float *centers;              // [n_vox, 3] voxel centres
+  const int32_t *feats;              // [n_vox, 8] corner ids
+  const float4 *values;              // [n_keys, 32] corner embeddings (fp32)
+  int64_t n_vox, n_keys;
+  float voxel_size;
+  int bits;                          // kPrune: points per axis
+  float step;                        // kPrune: rule 1 step
+  int rule;                          // kPrune: 0 = min exp(-relu s), 1 = max 1-exp(-relu(s) step)
+  unsigned int *score;               // kPrune: [n_vox] float bits
   const __nv_bfloat16 *w[5];         // row-major [N, K]: 128x32, 3x 128x128, 4x128
   const float *b[5];                 // [128] x4, [4]
   float *out;                        // [ns, 4]: sigma, r, g, b
-  int64_t ns;
+  int64_t ns;                        // rows
   int32_t *err;
 };
+
+// The trilinear weights of the interpolation kernel (interp.cu), same
+// operations in the same order, so a sample's FP32 embedding is identical.
+__device__ __forceinline__ float corner_weight(const float q[3], int k) {
+  float a = (k & 4) ? q[0] : 1.0f - q[0];
+  float b = (k & 2) ? q[1] : 1.0f - q[1];
+  float c = (k & 1) ? q[2] : 1.0f - q[2];
+  return a * b * c;
+}
+
+// emb[32] of a point x in voxel v (ids checked; out-of-range reads skipped).
+__device__ __forceinline__ void interp_point(const MlpParams &p, int64_t v, float x, float y,
+                                             float z, float (&e)[32], bool &bad) {
+#pragma unroll
+  for (int i = 0; i < 32; ++i) e[i] = 0.0f;
+  if (v < 0 || v >= p.n_vox) { bad = true; return; }
+  const float *c = p.centers + v * 3;
+  float q[3] = {(x - c[0]) / p.voxel_size + 0.5f, (y - c[1]) / p.voxel_size + 0.5f,
+                (z - c[2]) / p.voxel_size + 0.5f};
+  const int4 f0 = reinterpret_cast<const int4 *>(p.feats)[v * 2];
+  const int4 f1 = reinterpret_cast<const int4 *>(p.feats)[v * 2 + 1];
+  const int keys[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    int64_t key = keys[k];
+    if (key < 0 || key >= p.n_keys) { bad = true; continue; }
+    float w = corner_weight(q, k);
+    const float4 *src = p.values + key * 8;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float4 val = __ldg(src + j);
+      e[4 * j + 0] = fmaf(w, val.x, e[4 * j + 0]);
+      e[4 * j + 1] = fmaf(w, val.y, e[4 * j + 1]);
+      e[4 * j + 2] = fmaf(w, val.z, e[4 * j + 2]);
+      e[4 * j + 3] = fmaf(w, val.w, e[4 * j + 3]);
+    }
+  }
+}
 
 // Copy a row-major [rows, K] bf16 matrix into the K-major core-matrix layout
 // (rows >= valid_rows are zero).
@@ -80,6 +138,7 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const __nv_bfloat16
   }
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   MlpSmem &S = *reinterpret_cast<MlpSmem *>(smem_raw);
@@ -143,24 +202,47 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       int64_t tile = (2 * i + g) * G + b;
       if (tile >= n_tiles) break;
       int64_t r = tile * TILE + row;
-      // input tile: fp32 embedding row -> bf16, K-major
+      // input tile -> bf16, K-major
       {
-        float4 x[8];
+        float e[32];
+        bool bad = false;
         if (r < p.ns) {
-          const float4 *src = reinterpret_cast<const float4 *>(p.emb + r * E);
+          if (MODE == kEmbIn) {
+            const float4 *src = reinterpret_cast<const float4 *>(p.emb + r * E);
 #pragma unroll
-          for (int j = 0; j < 8; ++j) x[j] = __ldg(src + j);
+            for (int j = 0; j < 8; ++j) {
+              float4 x = __ldg(src + j);
+              e[4 * j] = x.x; e[4 * j + 1] = x.y; e[4 * j + 2] = x.z; e[4 * j + 3] = x.w;
+            }
+          } else if (MODE == kSamplesIn) {
+            float4 x = p.xyzd[r];
+            interp_point(p, p.vox[r], x.x, x.y, x.z, e, bad);
+          } else {
+            // point i of voxel v: offset_points order (x slowest), offset
+            // ((2 i_d + 1) - bits) / (bits - 1) times half a voxel
+            int64_t P = (int64_t)p.bits * p.bits * p.bits;
+            int64_t v = r / P, i = r % P;
+            int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits),
+                iz = (int)(i % p.bits);
+            const float *c = p.centers + v * 3;
+            float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
+            float x = c[0] + ((float)(2 * ix + 1 - p.bits) / den) * hv;
+            float y = c[1] + ((float)(2 * iy + 1 - p.bits) / den) * hv;
+            float z = c[2] + ((float)(2 * iz + 1 - p.bits) / den) * hv;
+            interp_point(p, v, x, y, z, e, bad);
+          }
         } else {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) x[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int j = 0; j < 32; ++j) e[j] = 0.0f;
         }
+        if (bad && p.err) atomicOr(p.err, 4);
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           uint4 v;
-          v.x = pack_bf16x2(x[2 * c].x, x[2 * c].y);
-          v.y = pack_bf16x2(x[2 * c].z, x[2 * c].w);
-          v.z = pack_bf16x2(x[2 * c + 1].x, x[2 * c + 1].y);
-          v.w = pack_bf16x2(x[2 * c + 1].z, x[2 * c + 1].w);
+          v.x = pack_bf16x2(e[8 * c + 0], e[8 * c + 1]);
+          v.y = pack_bf16x2(e[8 * c + 2], e[8 * c + 3]);
+          v.z = pack_bf16x2(e[8 * c + 4], e[8 * c + 5]);
+          v.w = pack_bf16x2(e[8 * c + 6], e[8 * c + 7]);
           *reinterpret_cast<uint4 *>(ain + kmajor_off(row, c * 8, E)) = v;
         }
       }
@@ -198,9 +280,37 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       tmem_ld16(tl + 128u, v);
       tmem_wait_ld();
       fence_before_sync();
-      if (r < p.ns)
-        reinterpret_cast<float4 *>(p.out)[r] =
-            make_float4(v[0] + S.bias4[0], v[1] + S.bias4[1], v[2] + S.bias4[2], v[3] + S.bias4[3]);
+      float sigma = v[0] + S.bias4[0];
+      if (MODE != kPrune) {
+        if (r < p.ns)
+          reinterpret_cast<float4 *>(p.out)[r] =
+              make_float4(sigma, v[1] + S.bias4[1], v[2] + S.bias4[2], v[3] + S.bias4[3]);
+      } else {
+        // reference rule (fairnr/modules/encoder.py:610, 648): exp(-relu s),
+        // reduced with min; workload rule: 1 - exp(-relu(s) * step), max.
+        // Both are >= 0, so their float bits order like unsigned ints. A warp
+        // whose rows all belong to one voxel reduces before its one atomic.
+        bool live = r < p.ns;
+        int64_t vv = live ? r / ((int64_t)p.bits * p.bits * p.bits) : -1;
+        uint32_t val;
+        if (p.rule == 0) val = __float_as_uint(expf(-fmaxf(sigma, 0.0f)));
+        else val = __float_as_uint(fmaxf(1.0f - expf(-(fmaxf(sigma, 0.0f) * p.step)), 0.0f));
+        int64_t v0 = __shfl_sync(0xffffffffu, vv, 0);
+        if (__all_sync(0xffffffffu, vv == v0 && live)) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            uint32_t y = __shfl_xor_sync(0xffffffffu, val, o);
+            val = (p.rule == 0) ? min(val, y) : max(val, y);
+          }
+          if (lane == 0) {
+            if (p.rule == 0) atomicMin(p.score + v0, val);
+            else atomicMax(p.score + v0, val);
+          }
+        } else if (live) {
+          if (p.rule == 0) atomicMin(p.score + vv, val);
+          else atomicMax(p.score + vv, val);
+        }
+      }
     }
   }
   fence_before_sync();
@@ -214,22 +324,12 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
 
 int g_num_sms = 0;
 
-}  // namespace
-
-extern "C" {
-
-int nsvf_mlp_forward_bf16(int64_t n_samples, const float *emb, const void *const weights[5],
-                          const float *const biases[5], float *out, int32_t *err, void *stream) {
-  if (n_samples < 0 || !weights || !biases) return NSVF_ERR_INVALID;
-  if (n_samples == 0) return NSVF_OK;
-  if (!emb || !out) return NSVF_ERR_INVALID;
-  for (int l = 0; l < 5; ++l)
-    if (!weights[l] || !biases[l] || (((uintptr_t)weights[l]) & 15)) return NSVF_ERR_INVALID;
-  if ((((uintptr_t)emb) | ((uintptr_t)out)) & 15) return NSVF_ERR_INVALID;
+template <int MODE>
+int launch_mlp(const MlpParams &p, cudaStream_t stream) {
   static bool attr_set = false;
   size_t smem = sizeof(MlpSmem) + 1024;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(mlp_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return NSVF_ERR_CUDA;
     int dev = 0;
@@ -237,21 +337,94 @@ int nsvf_mlp_forward_bf16(int64_t n_samples, const float *emb, const void *const
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     attr_set = true;
   }
-  MlpParams p;
-  p.emb = emb;
-  for (int l = 0; l < 5; ++l) {
-    p.w[l] = (const __nv_bfloat16 *)weights[l];
-    p.b[l] = biases[l];
-  }
-  p.out = out;
-  p.ns = n_samples;
-  p.err = err;
-  int64_t n_tiles = (n_samples + TILE - 1) / TILE;
+  int64_t n_tiles = (p.ns + TILE - 1) / TILE;
   int64_t grid = (n_tiles + 1) / 2;
   if (grid > g_num_sms) grid = g_num_sms;
   if (grid < 1) grid = 1;
-  mlp_tc_kernel<<<(int)grid, kThreads, smem, (cudaStream_t)stream>>>(p);
+  mlp_tc_kernel<MODE><<<(int)grid, kThreads, smem, stream>>>(p);
   return nsvf_launch_status();
+}
+
+bool set_weights(MlpParams &p, const void *const weights[5], const float *const biases[5]) {
+  if (!weights || !biases) return false;
+  for (int l = 0; l < 5; ++l) {
+    if (!weights[l] || !biases[l] || (((uintptr_t)weights[l]) & 15)) return false;
+    p.w[l] = (const __nv_bfloat16 *)weights[l];
+    p.b[l] = biases[l];
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsvf_mlp_forward_bf16(int64_t n_samples, const float *emb, const void *const weights[5],
+                          const float *const biases[5], float *out, int32_t *err, void *stream) {
+  if (n_samples < 0) return NSVF_ERR_INVALID;
+  if (n_samples == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!emb || !out || !set_weights(p, weights, biases)) return NSVF_ERR_INVALID;
+  if ((((uintptr_t)emb) | ((uintptr_t)out)) & 15) return NSVF_ERR_INVALID;
+  p.emb = emb;
+  p.out = out;
+  p.ns = n_samples;
+  p.err = err;
+  return launch_mlp<kEmbIn>(p, (cudaStream_t)stream);
+}
+
+int nsvf_field_samples_bf16(int64_t n_samples, const int32_t *voxel, const float *xyz_dist,
+                            int64_t n_voxels, int64_t n_keys, float voxel_size,
+                            const float *centers, const int32_t *feats, const float *values,
+                            const void *const weights[5], const float *const biases[5],
+                            float *out, int32_t *err, void *stream) {
+  if (n_samples < 0 || n_voxels < 1 || n_keys < 1) return NSVF_ERR_INVALID;
+  if (n_samples == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!voxel || !xyz_dist || !centers || !feats || !values || !out ||
+      !set_weights(p, weights, biases))
+    return NSVF_ERR_INVALID;
+  if ((((uintptr_t)xyz_dist) | ((uintptr_t)values) | ((uintptr_t)out) | ((uintptr_t)feats)) & 15)
+    return NSVF_ERR_INVALID;
+  p.vox = voxel;
+  p.xyzd = (const float4 *)xyz_dist;
+  p.centers = centers;
+  p.feats = feats;
+  p.values = (const float4 *)values;
+  p.n_vox = n_voxels;
+  p.n_keys = n_keys;
+  p.voxel_size = voxel_size;
+  p.out = out;
+  p.ns = n_samples;
+  p.err = err;
+  return launch_mlp<kSamplesIn>(p, (cudaStream_t)stream);
+}
+
+int nsvf_prune_scores_bf16(int64_t n_voxels, int bits, int rule, float step, int64_t n_keys,
+                           float voxel_size, const float *centers, const int32_t *feats,
+                           const float *values, const void *const weights[5],
+                           const float *const biases[5], uint32_t *score, int32_t *err,
+                           void *stream) {
+  if (n_voxels < 0 || bits < 2 || bits > 64 || (rule != 0 && rule != 1) || n_keys < 1)
+    return NSVF_ERR_INVALID;
+  if (n_voxels == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!centers || !feats || !values || !score || !set_weights(p, weights, biases))
+    return NSVF_ERR_INVALID;
+  if ((((uintptr_t)values) | ((uintptr_t)feats)) & 15) return NSVF_ERR_INVALID;
+  p.centers = centers;
+  p.feats = feats;
+  p.values = (const float4 *)values;
+  p.n_vox = n_voxels;
+  p.n_keys = n_keys;
+  p.voxel_size = voxel_size;
+  p.bits = bits;
+  p.rule = rule;
+  p.step = step;
+  p.score = score;
+  p.ns = n_voxels * (int64_t)bits * bits * bits;
+  p.err = err;
+  return launch_mlp<kPrune>(p, (cudaStream_t)stream);
 }
 
 }  // extern "C"

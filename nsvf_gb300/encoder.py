@@ -305,6 +305,25 @@ class SparseVoxelEncoder(nn.Module):
                           for i in range(0, points.size(0), chunk_size)], 0)
 
     @torch.no_grad()
+    def pruning_fused(self, mlp, th=0.5, bits=8, rule=1, apply=True):
+        """Self-pruning in one tensor-core kernel (nsvf_prune_scores_bf16):
+        sigma at bits^3 points per voxel with the BF16 field. rule 0 is the
+        reference's (keep = 1 - min exp(-relu sigma) > th, bits 16 there);
+        rule 1 keeps voxels with max(1 - exp(-relu(sigma) * step)) >= th.
+        Returns the keep mask over the currently kept voxels."""
+        states = self.precompute(id=None)
+        centers = states['voxel_center_xyz'].float().contiguous()
+        feats = states['voxel_vertex_idx'].int().contiguous()
+        values = states['voxel_vertex_emb'].detach().float().contiguous()
+        score = mlp.prune_scores(centers, feats, values, float(self.voxel_size), bits=bits,
+                                 rule=rule, step=float(self.step_size))
+        keep = ((1 - score) > th) if rule == 0 else (score >= th)
+        if apply:
+            self.keep.masked_scatter_(self.keep.bool(), keep.long())
+            self.clean_runtime_caches()
+        return keep
+
+    @torch.no_grad()
     def splitting(self):
         states = self.precompute(id=None)
         feats, points, values = states['voxel_vertex_idx'], states['voxel_center_xyz'], states['voxel_vertex_emb']

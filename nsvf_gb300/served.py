@@ -7,8 +7,9 @@ For one frame of rays of a resident scene:
 3. nsvf_sample_count / nsvf_sample_compact -- the inverse-CDF walk
    (deterministic jitter, the reference's launch layout) writing only the
    valid samples, compacted per ray
-4. nsvf_trilinear_embed       -- corner-embedding interpolation
-5. nsvf_mlp_forward_bf16      -- tcgen05 BF16 field MLP, FP32 accumulation
+4. nsvf_field_samples_bf16    -- corner-embedding interpolation fused into the
+                                 tcgen05 BF16 field MLP (FP32 accumulation);
+                                 embeddings and activations stay on chip
 6. nsvf_composite_segments    -- compensated transmittance compositing and
                                  the background fill, straight into the frame
 
@@ -61,8 +62,10 @@ class SceneState:
 def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     """ray_start [3] (shared origin) or [R, 3], ray_dir [R, 3] (FP32, on the
     scene's device) -> dict(colors [R, 3], depths [R], missed [R]).
-    mlp: "tc" (tcgen05 BF16 kernel), "bf16_emulated" (torch emulation of the
-    kernel's rounding) or "fp32" (the field's FP32 torch forward)."""
+    mlp: "tc" (interpolation fused into the tcgen05 BF16 MLP), "tc_unfused"
+    (interpolation kernel, then the MLP kernel), "bf16_emulated" (torch
+    emulation of the kernel's rounding) or "fp32" (the field's FP32 torch
+    forward)."""
     dev = scene.device
     R = ray_dir.shape[0]
     rd = ray_dir.float().contiguous()
@@ -109,14 +112,18 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
                                       layout.data_ptr(), _p(ro_h), 3, _p(rd_h), _p(offset),
                                       _p(vox), _p(xyzd), _p(depth), _p(ext.error_word(dev)),
                                       stream), "sample_compact")
-    emb = trilinear_embed(vox, xyzd[:, :3], scene.centers, scene.feats, scene.values,
-                          scene.voxel_size)
     if mlp == "tc":
-        field = scene.mlp(emb)
-    elif mlp == "bf16_emulated":
-        field = scene.mlp.reference_bf16(emb).contiguous()
+        field = scene.mlp.field_samples(vox, xyzd, scene.centers, scene.feats, scene.values,
+                                        scene.voxel_size)
     else:
-        field = scene.field.mlp(emb).float().contiguous()
+        emb = trilinear_embed(vox, xyzd[:, :3], scene.centers, scene.feats, scene.values,
+                              scene.voxel_size)
+        if mlp == "tc_unfused":
+            field = scene.mlp(emb)
+        elif mlp == "bf16_emulated":
+            field = scene.mlp.reference_bf16(emb).contiguous()
+        else:
+            field = scene.field.mlp(emb).float().contiguous()
     with ext._timed("composite_segments", dev):
         check(LIB.nsvf_composite_segments(
             n, _p(offset), _p(field), _p(xyzd), _p(depth), _p(pix), 7.0, scene.bg,

@@ -41,3 +41,69 @@ def test_mlp_repeated_calls_are_deterministic(cuda):
     a = mlp(emb)
     b = mlp(emb)
     assert torch.equal(a, b)
+
+
+def test_fused_interpolation_equals_unfused(golden, cuda):
+    """Interpolation fused into the MLP input stage gives bit-identical
+    outputs to the interpolation kernel followed by the MLP kernel."""
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.functional import trilinear_embed
+    from nsvf_gb300.mlp import TensorCoreMLP
+    g = golden
+    hit = g["svo_hits"][0]
+    d = g["svo_det_sampled_point_depth"]
+    mask = g["svo_det_sampled_point_voxel_idx"] != -1
+    xyz = (g["ray_start"][None, None] + g["ray_dir"][hit][:, None] * d[..., None]).astype(np.float32)[mask]
+    n = xyz.shape[0]
+    xyzd = torch.zeros(n, 4, device=cuda)
+    xyzd[:, :3] = torch.from_numpy(xyz).to(cuda)
+    vox = torch.from_numpy(g["svo_det_sampled_point_voxel_idx"][mask]).to(cuda).int()
+    centers = torch.from_numpy(g["svo_centers_shifted"]).to(cuda)
+    feats = torch.from_numpy(g["feats"]).to(cuda).int()
+    values = torch.from_numpy(g["embed"]).to(cuda)
+    field = StandInField(weights=[(torch.from_numpy(g["W%d" % i]), torch.from_numpy(g["b%d" % i]))
+                                  for i in range(5)]).to(cuda)
+    mlp = TensorCoreMLP(field)
+    fused = mlp.field_samples(vox, xyzd, centers, feats, values, float(g["voxel_size"]))
+    emb = trilinear_embed(vox, xyzd[:, :3], centers, feats, values, float(g["voxel_size"]))
+    assert torch.equal(fused, mlp(emb))
+
+
+@pytest.mark.parametrize("rule,bits", [(0, 16), (1, 8)])
+def test_prune_scores_against_reference(golden, golden_prune, cuda, rule, bits):
+    """Fused pruning scores vs a torch composition of the same steps (points
+    from offset_points, FP32 interpolation kernel, BF16-emulated MLP), and the
+    keep mask vs the reference's FP32 mask away from the threshold."""
+    from nsvf_gb300 import geometry
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.functional import trilinear_embed
+    from nsvf_gb300.mlp import TensorCoreMLP
+    g, gp = golden, golden_prune
+    vs = float(g["voxel_size"])
+    centers = torch.from_numpy(g["svo_centers_shifted"]).to(cuda)
+    feats = torch.from_numpy(g["feats"]).to(cuda).int()
+    values = torch.from_numpy(g["embed"]).to(cuda)
+    field = StandInField(weights=[(torch.from_numpy(g["W%d" % i]), torch.from_numpy(g["b%d" % i]))
+                                  for i in range(5)]).to(cuda)
+    mlp = TensorCoreMLP(field)
+    step = float(gp["step"])
+    score = mlp.prune_scores(centers, feats, values, vs, bits=bits, rule=rule, step=step)
+    pts = geometry.offset_points(centers, torch.tensor(vs / 2.0, device=cuda), bits=bits)
+    idx = torch.arange(centers.size(0), device=cuda)[:, None].expand(*pts.shape[:2]).reshape(-1)
+    emb = trilinear_embed(idx, pts.reshape(-1, 3), centers, feats, values, vs)
+    sig = mlp.reference_bf16(emb)[:, 0].reshape(centers.size(0), -1)
+    if rule == 0:
+        ref = torch.exp(-torch.relu(sig)).min(-1)[0]
+        ref_keep = gp["keep16"]
+        margin = np.abs((1 - gp["minscore16"]) - 0.5)
+        keep = ((1 - score) > 0.5).cpu().numpy()
+    else:
+        ref = (1 - torch.exp(-torch.relu(sig) * step)).max(-1)[0]
+        th = float(gp["th8"])
+        ref_keep = gp["keep8"]
+        margin = np.abs(gp["maxalpha8"] - th)
+        keep = (score >= th).cpu().numpy()
+    np.testing.assert_allclose(score.cpu().numpy(), ref.cpu().numpy(), rtol=2e-3, atol=2e-4)
+    far = margin > 0.02
+    assert np.array_equal(keep[far], ref_keep[far])
+    assert far.sum() > 0.8 * far.size
