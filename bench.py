@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--path", default="plain", choices=["plain", "served"])
     ap.add_argument("--cpu-rays", type=int, default=16384,
                     help="rays of the frame in the CPU baseline sample")
+    ap.add_argument("--size", type=int, default=800,
+                    help="frame side in pixels (800 = the c2 workload; smaller for profiling)")
     return ap.parse_args()
 
 
@@ -71,9 +73,9 @@ def make_scene(dev):
                 weights=weights)
 
 
-def frame_rays(index):
+def frame_rays(index, size=800):
     from nsvf_gb300 import scenes
-    rs, rd = scenes.frame_view(index % 100)
+    rs, rd = scenes.frame_view(index % 100, size=size)
     return rs, rd
 
 
@@ -156,7 +158,7 @@ def run_ours(a):
     n_frames = a.warmup + a.steps
     host = []
     for i in range(n_frames):
-        rs, rd = frame_rays(i + 7 * rank)
+        rs, rd = frame_rays(i + 7 * rank, a.size)
         rdt = torch.from_numpy(rd).pin_memory()
         rst = torch.from_numpy(rs).pin_memory()
         host.append((rst, rdt))
@@ -237,7 +239,8 @@ def run_ours(a):
     if rank != 0:
         dist.destroy_process_group()
         return
-    rays_total = RAYS_PER_FRAME * a.steps * world
+    rays_frame = a.size * a.size
+    rays_total = rays_frame * a.steps * world
     value = rays_total / t_dev
     ms = [x * 1e3 for x in times]
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
@@ -248,17 +251,26 @@ def run_ours(a):
     # R*24 (ray origin + direction) + Nn*48 (packed octree) + R*H*12 (sorted
     # ids/min/max) + R (hit flags).
     Nn = int(states["voxel_octree_children_idx"].shape[0])
-    alg = RAYS_PER_FRAME * 24 + Nn * 48 + RAYS_PER_FRAME * MAX_HITS * 12 + RAYS_PER_FRAME
+    alg = rays_frame * 24 + Nn * 48 + rays_frame * MAX_HITS * 12 + rays_frame
     k = kernel_ms.get("svo_intersect_sorted")
     roof = None
-    if a.path == "served" and kernel_ms.get("mlp_forward_bf16"):
+    roof_isect = None
+    if k:
+        ach = alg / (k["avg_ms"] / 1e3) / 1e9
+        roof_isect = {"kernel": "svo_intersect_sorted (pack + svo_kernel<SORTED>)", "bound": "hbm",
+                      "achieved": round(ach, 1), "peak": hbm_peak, "unit": "GB/s",
+                      "frac": round(ach / hbm_peak, 4),
+                      "peak_source": "measured" if peaks else "fallback",
+                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": round(k["avg_ms"], 4)}
+    if a.path == "served" and kernel_ms.get("field_samples_bf16"):
         # the tensor-core MLP dominates the served path: 107,520 FLOP per
         # sample (2 * (32*128 + 3*128*128 + 128*4)) x samples per launch
-        km = kernel_ms["mlp_forward_bf16"]
+        km = kernel_ms["field_samples_bf16"]
         flops = 107520.0 * out_samples[0] / max(1, km["launches"]) if out_samples[0] else 0
         ach = flops / (km["avg_ms"] / 1e3) / 1e12
         tpk = peaks["bf16_tflops"] if peaks else 1900.0
-        roof = {"kernel": "mlp_forward_bf16", "bound": "tensor", "achieved": round(ach, 1),
+        roof = {"kernel": "field_samples_bf16 (mlp_tc_kernel<kSamplesIn>)", "bound": "tensor",
+                "achieved": round(ach, 1),
                 "peak": tpk, "unit": "TFLOP/s", "frac": round(ach / tpk, 4),
                 "peak_source": "measured (bf16 burst)" if peaks else "fallback",
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": km["avg_ms"],
@@ -277,15 +289,18 @@ def run_ours(a):
         "p50_ms": round(float(np.percentile(ms, 50)), 3), "p99_ms": round(float(np.percentile(ms, 99)), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 MLP / f32 geometry" if a.path == "served" else "f32",
         "data": "synthetic (seeded scene, embeddings, MLP and cameras)",
-        "config": {"workload": "c2: 125,476-voxel sphere+torus shell, 800x800 frame, SVO, "
-                               "max_hits 64, step 1/512, 4x128 MLP", "path": a.path,
+        "config": {"workload": "c2: 125,476-voxel sphere+torus shell, %dx%d frame, SVO, "
+                               "max_hits 64, step 1/512, 4x128 MLP" % (a.size, a.size),
+                   "path": a.path,
                    "voxels": int(sc["points"].shape[0]), "octree_nodes": Nn,
+                   "samples_per_frame": (out_samples[0] // a.steps) if out_samples[0] else None,
                    "l2": "flushed (256 MB write) between timed frames", "parallelism": "replicas"},
-        "e2e": {"value": round(RAYS_PER_FRAME * a.steps * world / t_e2e, 1), "unit": "rays/s",
+        "e2e": {"value": round(rays_frame * a.steps * world / t_e2e, 1), "unit": "rays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "kernels_ms": kernel_ms,
         "roofline": roof,
+        "roofline_intersection": roof_isect,
         "cpu_baseline": cpu,
         "clocks": clk,
     }

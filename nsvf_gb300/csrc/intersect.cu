@@ -86,99 +86,184 @@ __global__ void pack_octree_kernel(int64_t total, float hv, const float *__restr
   kids[k * 2 + 1] = make_int4(c[4], c[5], c[6], c[7]);
 }
 
-constexpr int kSvoStack = 256;
+constexpr int kSvoLevels = 16;
 
-// Depth-first traversal with the reference's visiting order. The reference
-// pushes every existing child untested and tests a node when it pops it; here
-// the children of a hit node are tested when the node is expanded and only
-// the hit ones are pushed (children 0..7, so child 7 is popped first). The
-// set of tests and the order of emitted leaves are the same; the stack holds
-// at most 1 + 7 * levels entries instead of 1 + 7 * levels + untested ones.
+// Depth-first traversal in the reference's visiting order (children 7..0 of
+// every hit node, fairnr/clib/src/intersect_gpu.cu:200-235), without a
+// per-thread stack of node ids in local memory: a node's children are tested
+// when the node is expanded, and each level of the descent keeps only
+// (node id, 8-bit mask of its hit children not yet visited) in shared
+// memory. The set of slab tests and the order of emitted leaves are the
+// reference's. Hits are written straight into the ray's output row.
+//
+// Returns the number of hits (<= n_max); sets `bad` for a malformed octree.
+__device__ __forceinline__ uint32_t child_hitmask(const float4 *__restrict__ box,
+                                                  const int4 *__restrict__ kids, int k, int n,
+                                                  float ox, float oy, float oz, float ix,
+                                                  float iy, float iz, bool &bad) {
+  int4 ka = kids[k * 2 + 0], kc = kids[k * 2 + 1];
+  int ch[8] = {ka.x, ka.y, ka.z, ka.w, kc.x, kc.y, kc.z, kc.w};
+  uint32_t m = 0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    int c = ch[u];
+    if (c > -1) {
+      if (c >= n) { bad = true; continue; }
+      float4 cb = box[c];
+      float lo, hi;
+      if (nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, fabsf(cb.w), lo, hi)) m |= 1u << u;
+    }
+  }
+  return m;
+}
+
+__device__ __forceinline__ int svo_traverse(const float4 *__restrict__ box,
+                                            const int4 *__restrict__ kids, int n, int n_max,
+                                            float ox, float oy, float oz, float ix, float iy,
+                                            float iz, int *s_node, uint8_t *s_mask,
+                                            int32_t *__restrict__ I, float *__restrict__ LO,
+                                            float *__restrict__ HI, bool &bad) {
+  const int t = threadIdx.x;
+  int cnt = 0;
+  float4 rb = box[n - 1];
+  float lo, hi;
+  if (!nsvf_slab(ox, oy, oz, ix, iy, iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi)) return 0;
+  if (rb.w < 0.0f) {  // a single-leaf octree
+    I[0] = n - 1; LO[0] = lo; HI[0] = hi;
+    return 1;
+  }
+  int level = 0;
+  s_node[0 * kRayBlock + t] = n - 1;
+  s_mask[0 * kRayBlock + t] = (uint8_t)child_hitmask(box, kids, n - 1, n, ox, oy, oz, ix, iy, iz, bad);
+  int64_t steps = 0;
+  while (level >= 0 && cnt < n_max) {
+    if (++steps > 8 * (int64_t)n) { bad = true; break; }  // a cycle
+    uint32_t m = s_mask[level * kRayBlock + t];
+    if (m == 0) { --level; continue; }
+    int u = 31 - __clz(m);                // highest child first (popped first in the reference)
+    s_mask[level * kRayBlock + t] = (uint8_t)(m & ~(1u << u));
+    int parent = s_node[level * kRayBlock + t];
+    int c = reinterpret_cast<const int *>(kids + parent * 2)[u];
+    float4 cb = box[c];
+    if (cb.w < 0.0f) {                    // leaf: its interval (same inputs, same bits)
+      nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, -cb.w, lo, hi);
+      I[cnt] = c; LO[cnt] = lo; HI[cnt] = hi;
+      ++cnt;
+      continue;
+    }
+    if (level + 1 >= kSvoLevels) { bad = true; break; }
+    ++level;
+    s_node[level * kRayBlock + t] = c;
+    s_mask[level * kRayBlock + t] = (uint8_t)child_hitmask(box, kids, c, n, ox, oy, oz, ix, iy, iz, bad);
+  }
+  return cnt;
+}
+
+// Warp-cooperative stable sort of one row of n_max <= 32*E slots by
+// (min_depth, slot): bitonic network over 32*E keys, lanes hold E keys each
+// (element j at lane j % 32, register j / 32). Unique keys make any sorting
+// network stable, which is torch's sort of the reference up to tie order.
+template <int E>
+__device__ __forceinline__ void warp_sort_row(int32_t *__restrict__ I, float *__restrict__ LO,
+                                              float *__restrict__ HI, int n_max, int lane) {
+  float k1[E], hv[E];
+  int k2[E], id[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    int j = e * 32 + lane;
+    if (j < n_max) { k1[e] = LO[j]; k2[e] = j; id[e] = I[j]; hv[e] = HI[j]; }
+    else { k1[e] = __int_as_float(0x7f800000); k2[e] = j; id[e] = -1; hv[e] = 0.f; }
+  }
+  constexpr int N = 32 * E;
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll
+    for (int s = k >> 1; s > 0; s >>= 1) {
+      if (s >= 32) {
+        const int r = s / 32;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          int pe = e ^ r;
+          if (pe > e) {
+            int j = e * 32 + lane;
+            bool asc = (j & k) == 0;
+            bool gt = (k1[e] > k1[pe]) || (k1[e] == k1[pe] && k2[e] > k2[pe]);
+            if (gt == asc) {
+              float a = k1[e]; k1[e] = k1[pe]; k1[pe] = a;
+              int b = k2[e]; k2[e] = k2[pe]; k2[pe] = b;
+              int c = id[e]; id[e] = id[pe]; id[pe] = c;
+              float d = hv[e]; hv[e] = hv[pe]; hv[pe] = d;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          int j = e * 32 + lane;
+          float o1 = __shfl_xor_sync(0xffffffffu, k1[e], s);
+          int o2 = __shfl_xor_sync(0xffffffffu, k2[e], s);
+          int oi = __shfl_xor_sync(0xffffffffu, id[e], s);
+          float oh = __shfl_xor_sync(0xffffffffu, hv[e], s);
+          bool asc = (j & k) == 0;
+          bool lower = (j & s) == 0;
+          bool other_less = (o1 < k1[e]) || (o1 == k1[e] && o2 < k2[e]);
+          // the lower index keeps the smaller key when ascending
+          bool take = (lower == asc) ? other_less : !other_less;
+          if (take) { k1[e] = o1; k2[e] = o2; id[e] = oi; hv[e] = oh; }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    int j = e * 32 + lane;
+    if (j < n_max) { I[j] = id[e]; LO[j] = k1[e]; HI[j] = hv[e]; }
+  }
+}
+
 template <bool SORTED>
 __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int64_t rays, int m, int b_pts, int n, int n_max, const float *__restrict__ ray_start,
     const float *__restrict__ ray_dir, const float4 *__restrict__ box_all,
     const int4 *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
     float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
+  __shared__ int s_node[kSvoLevels * kRayBlock];
+  __shared__ uint8_t s_mask[kSvoLevels * kRayBlock];
   int64_t r = blockIdx.x * (int64_t)kRayBlock + threadIdx.x;
-  if (r >= rays) return;
-  int64_t g = (b_pts == 1) ? 0 : r / m;
-  const float4 *box = box_all + g * n;
-  const int4 *kids = kids_all + g * n * 2;
-  float ox = ray_start[r * 3 + 0], oy = ray_start[r * 3 + 1], oz = ray_start[r * 3 + 2];
-  float ix = nsvf_rcp(ray_dir[r * 3 + 0]), iy = nsvf_rcp(ray_dir[r * 3 + 1]),
-        iz = nsvf_rcp(ray_dir[r * 3 + 2]);
-  int32_t *I = idx + r * n_max;
-  float *LO = min_depth + r * n_max, *HI = max_depth + r * n_max;
-
-  // SORTED keeps the hits in (thread-local) arrays and insertion-sorts them.
-  constexpr int kMaxSorted = SORTED ? 128 : 1;
-  int32_t hid[kMaxSorted];
-  float hlo[kMaxSorted], hhi[kMaxSorted];
-
+  int lane = threadIdx.x & 31;
   int cnt = 0;
-  int stack[kSvoStack];
-  int sp = 0;
-  {
-    float4 rb = box[n - 1];
-    float lo, hi;
-    if (nsvf_slab(ox, oy, oz, ix, iy, iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi))
-      stack[sp++] = n - 1;
-  }
-  // A well-formed octree pops every node at most once per ray; more pops, a
-  // child id outside [0, n) or a full stack mean a malformed input, which is
-  // reported through `err` instead of looping or reading out of bounds.
-  int64_t pops = 0;
   bool bad = false;
-  while (sp > 0 && cnt < n_max) {
-    if (++pops > n) { bad = true; break; }
-    int k = stack[--sp];
-    float4 kb = box[k];
-    if (kb.w < 0.0f) {  // leaf: recompute its interval (same inputs, same bits)
-      float lo, hi;
-      nsvf_slab(ox, oy, oz, ix, iy, iz, kb.x, kb.y, kb.z, -kb.w, lo, hi);
-      if (SORTED) {
-        int p = cnt;
-        while (p > 0 && hlo[p - 1] > lo) {
-          hid[p] = hid[p - 1]; hlo[p] = hlo[p - 1]; hhi[p] = hhi[p - 1]; --p;
-        }
-        hid[p] = k; hlo[p] = lo; hhi[p] = hi;
-      } else {
-        I[cnt] = k; LO[cnt] = lo; HI[cnt] = hi;
-      }
-      ++cnt;
-      continue;
-    }
-    int4 ka = kids[k * 2 + 0], kc = kids[k * 2 + 1];
-    int ch[8] = {ka.x, ka.y, ka.z, ka.w, kc.x, kc.y, kc.z, kc.w};
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      int c = ch[u];
-      if (c > -1) {
-        if (c >= n) { bad = true; continue; }
-        float4 cb = box[c];
-        float lo, hi;
-        if (nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, fabsf(cb.w), lo, hi)) {
-          if (sp < kSvoStack) stack[sp++] = c;
-          else bad = true;
-        }
-      }
-    }
+  if (r < rays) {
+    int64_t g = (b_pts == 1) ? 0 : r / m;
+    const float4 *box = box_all + g * n;
+    const int4 *kids = kids_all + g * n * 2;
+    float ox = ray_start[r * 3 + 0], oy = ray_start[r * 3 + 1], oz = ray_start[r * 3 + 2];
+    float ix = nsvf_rcp(ray_dir[r * 3 + 0]), iy = nsvf_rcp(ray_dir[r * 3 + 1]),
+          iz = nsvf_rcp(ray_dir[r * 3 + 2]);
+    int32_t *I = idx + r * n_max;
+    float *LO = min_depth + r * n_max, *HI = max_depth + r * n_max;
+    cnt = svo_traverse(box, kids, n, n_max, ox, oy, oz, ix, iy, iz, s_node, s_mask, I, LO, HI, bad);
+    float pad = SORTED ? NSVF_MAX_DEPTH_F : 0.0f;
+    for (int l = cnt; l < n_max; ++l) { I[l] = -1; LO[l] = pad; HI[l] = pad; }
+    if (SORTED) hits[r] = cnt > 0;
   }
   if (bad && err) atomicOr(err, 1);
   if (SORTED) {
-    // Emulate "misses -> 10000, sort all n_max slots by min_depth" with ties
-    // resolved by slot: hits with lo <= 10000 first, then the misses, then
-    // any hit beyond 10000.
-    int split = 0;
-    while (split < cnt && !(hlo[split] > NSVF_MAX_DEPTH_F)) ++split;
-    int o = 0;
-    for (int p = 0; p < split; ++p, ++o) { I[o] = hid[p]; LO[o] = hlo[p]; HI[o] = hhi[p]; }
-    for (int p = cnt; p < n_max; ++p, ++o) { I[o] = -1; LO[o] = NSVF_MAX_DEPTH_F; HI[o] = NSVF_MAX_DEPTH_F; }
-    for (int p = split; p < cnt; ++p, ++o) { I[o] = hid[p]; LO[o] = hlo[p]; HI[o] = hhi[p]; }
-    hits[r] = cnt > 0;
-  } else {
-    for (int l = cnt; l < n_max; ++l) { I[l] = -1; LO[l] = 0.0f; HI[l] = 0.0f; }
+    // each warp sorts the rows of its rays that hold a hit
+    __syncwarp();
+    int64_t r0 = r - lane;
+    unsigned todo = __ballot_sync(0xffffffffu, cnt > 0);
+    while (todo) {
+      int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      int64_t rr = r0 + src;
+      int32_t *I = idx + rr * n_max;
+      float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
+      if (n_max <= 32) warp_sort_row<1>(I, LO, HI, n_max, lane);
+      else if (n_max <= 64) warp_sort_row<2>(I, LO, HI, n_max, lane);
+      else warp_sort_row<4>(I, LO, HI, n_max, lane);
+      __syncwarp();
+    }
   }
 }
 
