@@ -87,91 +87,68 @@ __global__ void pack_octree_kernel(int64_t total, float hv, const float *__restr
 }
 
 constexpr int kSvoLevels = 16;
+constexpr int kRaysPerWarp = 4;                       // 8 lanes per ray
+constexpr int kRaysPerBlock = kRayBlock / 8;          // 16
 
-// Depth-first traversal in the reference's visiting order (children 7..0 of
-// every hit node, fairnr/clib/src/intersect_gpu.cu:200-235), without a
-// per-thread stack of node ids in local memory: a node's children are tested
-// when the node is expanded, and each level of the descent keeps only
-// (node id, 8-bit mask of its hit children not yet visited) in shared
-// memory. The set of slab tests and the order of emitted leaves are the
-// reference's. Hits are written straight into the ray's output row.
+// Warp-cooperative depth-first traversal in the reference's visiting order
+// (children 7..0 of every hit node, fairnr/clib/src/intersect_gpu.cu:200-235).
 //
-// Returns the number of hits (<= n_max); sets `bad` for a malformed octree.
-__device__ __forceinline__ uint32_t child_hitmask(const float4 *__restrict__ box,
-                                                  const int4 *__restrict__ kids, int k, int n,
-                                                  float ox, float oy, float oz, float ix,
-                                                  float iy, float iz, bool &bad) {
-  int4 ka = kids[k * 2 + 0], kc = kids[k * 2 + 1];
-  int ch[8] = {ka.x, ka.y, ka.z, ka.w, kc.x, kc.y, kc.z, kc.w};
-  uint32_t m = 0;
-#pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    int c = ch[u];
-    if (c > -1) {
-      if (c >= n) { bad = true; continue; }
-      float4 cb = box[c];
-      float lo, hi;
-      if (nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, fabsf(cb.w), lo, hi)) m |= 1u << u;
-    }
-  }
-  return m;
-}
+// A warp walks 4 rays; the 8 lanes of a ray's group each own one child slot.
+// Expanding a node = each lane loads its child id and box and runs the slab
+// test; a ballot gives the node's 8-bit mask of hit children. The descent
+// keeps, per level, (node id, mask of hit children not yet visited) in shared
+// memory; the group's lane 0 picks the next child (highest index first).
+// When every hit child of a node is a leaf -- always the case for trees made
+// by build_octree, whose leaves all sit under depth-0 nodes -- the DFS visits
+// them consecutively, so the group emits them at once, lane j writing at
+// cnt + (number of hit leaves with a higher index). Mixed children fall back
+// to visiting leaves one at a time. The emitted order, the n_max cutoff and
+// every (lo, hi) are the reference's. Hits go straight into the output row.
+struct GroupCtx {
+  const float4 *box;
+  const int4 *kids;
+  int n, n_max;
+  float ox, oy, oz, ix, iy, iz;
+};
 
-__device__ __forceinline__ int svo_traverse(const float4 *__restrict__ box,
-                                            const int4 *__restrict__ kids, int n, int n_max,
-                                            float ox, float oy, float oz, float ix, float iy,
-                                            float iz, int *s_node, uint8_t *s_mask,
-                                            int32_t *__restrict__ I, float *__restrict__ LO,
-                                            float *__restrict__ HI, bool &bad) {
-  const int t = threadIdx.x;
-  int cnt = 0;
-  float4 rb = box[n - 1];
-  float lo, hi;
-  if (!nsvf_slab(ox, oy, oz, ix, iy, iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi)) return 0;
-  if (rb.w < 0.0f) {  // a single-leaf octree
-    I[0] = n - 1; LO[0] = lo; HI[0] = hi;
-    return 1;
-  }
-  int level = 0;
-  s_node[0 * kRayBlock + t] = n - 1;
-  s_mask[0 * kRayBlock + t] = (uint8_t)child_hitmask(box, kids, n - 1, n, ox, oy, oz, ix, iy, iz, bad);
-  int64_t steps = 0;
-  while (level >= 0 && cnt < n_max) {
-    if (++steps > 8 * (int64_t)n) { bad = true; break; }  // a cycle
-    uint32_t m = s_mask[level * kRayBlock + t];
-    if (m == 0) { --level; continue; }
-    int u = 31 - __clz(m);                // highest child first (popped first in the reference)
-    s_mask[level * kRayBlock + t] = (uint8_t)(m & ~(1u << u));
-    int parent = s_node[level * kRayBlock + t];
-    int c = reinterpret_cast<const int *>(kids + parent * 2)[u];
-    float4 cb = box[c];
-    if (cb.w < 0.0f) {                    // leaf: its interval (same inputs, same bits)
-      nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, -cb.w, lo, hi);
-      I[cnt] = c; LO[cnt] = lo; HI[cnt] = hi;
-      ++cnt;
-      continue;
+// Each lane of the group tests child `j` of node k. Returns the group's
+// 8-bit masks of hit children and of hit leaves; this lane's (lo, hi, id).
+__device__ __forceinline__ void expand_node(const GroupCtx &c, int k, int j, uint32_t gshift,
+                                            uint32_t &hitmask, uint32_t &leafmask, float &lo,
+                                            float &hi, int &cid, bool &bad) {
+  cid = reinterpret_cast<const int *>(c.kids + (int64_t)k * 2)[j];
+  bool hit = false, leaf = false;
+  if (cid > -1) {
+    if (cid >= c.n) {
+      bad = true;
+    } else {
+      float4 b = c.box[cid];
+      hit = nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, b.x, b.y, b.z, fabsf(b.w), lo, hi);
+      leaf = b.w < 0.0f;
     }
-    if (level + 1 >= kSvoLevels) { bad = true; break; }
-    ++level;
-    s_node[level * kRayBlock + t] = c;
-    s_mask[level * kRayBlock + t] = (uint8_t)child_hitmask(box, kids, c, n, ox, oy, oz, ix, iy, iz, bad);
   }
-  return cnt;
+  uint32_t hb = __ballot_sync(0xffffffffu, hit);
+  uint32_t lb = __ballot_sync(0xffffffffu, hit && leaf);
+  hitmask = (hb >> gshift) & 0xffu;
+  leafmask = (lb >> gshift) & 0xffu;
 }
 
 // Warp-cooperative stable sort of one row of n_max <= 32*E slots by
-// (min_depth, slot): bitonic network over 32*E keys, lanes hold E keys each
-// (element j at lane j % 32, register j / 32). Unique keys make any sorting
-// network stable, which is torch's sort of the reference up to tie order.
+// (min_depth, slot); slots >= cnt are the misses (id -1, depth 10000), the
+// reference's masked_fill before its sort. Bitonic network over 32*E keys,
+// element j at lane j % 32, register j / 32. Unique keys make any sorting
+// network stable. Writes the whole row.
 template <int E>
 __device__ __forceinline__ void warp_sort_row(int32_t *__restrict__ I, float *__restrict__ LO,
-                                              float *__restrict__ HI, int n_max, int lane) {
+                                              float *__restrict__ HI, int n_max, int cnt,
+                                              int lane) {
   float k1[E], hv[E];
   int k2[E], id[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     int j = e * 32 + lane;
-    if (j < n_max) { k1[e] = LO[j]; k2[e] = j; id[e] = I[j]; hv[e] = HI[j]; }
+    if (j < cnt) { k1[e] = LO[j]; k2[e] = j; id[e] = I[j]; hv[e] = HI[j]; }
+    else if (j < n_max) { k1[e] = NSVF_MAX_DEPTH_F; k2[e] = j; id[e] = -1; hv[e] = NSVF_MAX_DEPTH_F; }
     else { k1[e] = __int_as_float(0x7f800000); k2[e] = j; id[e] = -1; hv[e] = 0.f; }
   }
   constexpr int N = 32 * E;
@@ -207,7 +184,6 @@ __device__ __forceinline__ void warp_sort_row(int32_t *__restrict__ I, float *__
           bool asc = (j & k) == 0;
           bool lower = (j & s) == 0;
           bool other_less = (o1 < k1[e]) || (o1 == k1[e] && o2 < k2[e]);
-          // the lower index keeps the smaller key when ascending
           bool take = (lower == asc) ? other_less : !other_less;
           if (take) { k1[e] = o1; k2[e] = o2; id[e] = oi; hv[e] = oh; }
         }
@@ -227,43 +203,129 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     const float *__restrict__ ray_dir, const float4 *__restrict__ box_all,
     const int4 *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
     float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
-  __shared__ int s_node[kSvoLevels * kRayBlock];
-  __shared__ uint8_t s_mask[kSvoLevels * kRayBlock];
-  int64_t r = blockIdx.x * (int64_t)kRayBlock + threadIdx.x;
-  int lane = threadIdx.x & 31;
-  int cnt = 0;
+  __shared__ int s_node[kSvoLevels * kRaysPerBlock];
+  __shared__ uint8_t s_mask[kSvoLevels * kRaysPerBlock];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = lane >> 3, j = lane & 7;           // ray slot in the warp, child slot
+  const uint32_t gshift = 8u * grp;
+  const int slot = warp * kRaysPerWarp + grp;        // ray slot in the block
+  const int64_t r = (int64_t)blockIdx.x * kRaysPerBlock + slot;
+  const bool live = r < rays;
   bool bad = false;
-  if (r < rays) {
-    int64_t g = (b_pts == 1) ? 0 : r / m;
-    const float4 *box = box_all + g * n;
-    const int4 *kids = kids_all + g * n * 2;
-    float ox = ray_start[r * 3 + 0], oy = ray_start[r * 3 + 1], oz = ray_start[r * 3 + 2];
-    float ix = nsvf_rcp(ray_dir[r * 3 + 0]), iy = nsvf_rcp(ray_dir[r * 3 + 1]),
-          iz = nsvf_rcp(ray_dir[r * 3 + 2]);
-    int32_t *I = idx + r * n_max;
-    float *LO = min_depth + r * n_max, *HI = max_depth + r * n_max;
-    cnt = svo_traverse(box, kids, n, n_max, ox, oy, oz, ix, iy, iz, s_node, s_mask, I, LO, HI, bad);
-    float pad = SORTED ? NSVF_MAX_DEPTH_F : 0.0f;
-    for (int l = cnt; l < n_max; ++l) { I[l] = -1; LO[l] = pad; HI[l] = pad; }
-    if (SORTED) hits[r] = cnt > 0;
-  }
-  if (bad && err) atomicOr(err, 1);
-  if (SORTED) {
-    // each warp sorts the rows of its rays that hold a hit
-    __syncwarp();
-    int64_t r0 = r - lane;
-    unsigned todo = __ballot_sync(0xffffffffu, cnt > 0);
-    while (todo) {
-      int src = __ffs(todo) - 1;
-      todo &= todo - 1;
-      int64_t rr = r0 + src;
-      int32_t *I = idx + rr * n_max;
-      float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
-      if (n_max <= 32) warp_sort_row<1>(I, LO, HI, n_max, lane);
-      else if (n_max <= 64) warp_sort_row<2>(I, LO, HI, n_max, lane);
-      else warp_sort_row<4>(I, LO, HI, n_max, lane);
-      __syncwarp();
+  int cnt = 0;
+
+  GroupCtx c;
+  c.n = n;
+  c.n_max = n_max;
+  const int64_t rr = live ? r : 0;
+  const int64_t g = (b_pts == 1) ? 0 : rr / m;
+  c.box = box_all + g * n;
+  c.kids = kids_all + g * n * 2;
+  c.ox = ray_start[rr * 3 + 0]; c.oy = ray_start[rr * 3 + 1]; c.oz = ray_start[rr * 3 + 2];
+  c.ix = nsvf_rcp(ray_dir[rr * 3 + 0]); c.iy = nsvf_rcp(ray_dir[rr * 3 + 1]);
+  c.iz = nsvf_rcp(ray_dir[rr * 3 + 2]);
+  int32_t *I = idx + rr * n_max;
+  float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
+
+  // root
+  int level = -1;
+  {
+    float4 rb = c.box[n - 1];
+    float lo, hi;
+    bool rh = live && nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi);
+    if (rh && rb.w < 0.0f) {            // a single-leaf octree
+      if (j == 0) { I[0] = n - 1; LO[0] = lo; HI[0] = hi; }
+      cnt = 1;
+    } else if (rh) {
+      level = 0;
     }
+  }
+  int node = n - 1;                      // the node to expand next (valid when `expand`)
+  bool expand = level == 0;
+  int64_t steps = 0;
+  // Every group runs the loop until all groups of the warp are done. All
+  // warp-wide operations (ballots in expand_node, the shuffles that
+  // broadcast lane 0's stack walk) are executed by all 32 lanes every
+  // iteration; only lane-local work is predicated on `expand`.
+  while (__any_sync(0xffffffffu, expand)) {
+    uint32_t hm = 0, lm = 0;
+    float lo = 0.f, hi = 0.f;
+    int cid = -1;
+    int k = expand ? node : 0;
+    expand_node(c, k, j, gshift, hm, lm, lo, hi, cid, bad);
+    if (expand && ++steps > 8 * (int64_t)n) { bad = true; expand = false; }
+    int next = -1;
+    if (expand) {
+      if (hm != 0 && hm == lm) {
+        // all hit children are leaves: emit them now, highest index first
+        int before = __popc(hm >> (j + 1));
+        if (((hm >> j) & 1u) && cnt + before < n_max) {
+          I[cnt + before] = cid; LO[cnt + before] = lo; HI[cnt + before] = hi;
+        }
+        cnt = min(n_max, cnt + __popc(hm));
+        hm = 0;                           // nothing to descend into
+      } else if (j == 0) {
+        s_node[level * kRaysPerBlock + slot] = k;
+        s_mask[level * kRaysPerBlock + slot] = (uint8_t)hm;
+      }
+      if (hm == 0) --level;               // this node is finished (or its leaves emitted)
+      // find the next internal node to expand (lane 0 of the group walks the
+      // level stack; a leaf met on the way -- mixed children -- is emitted)
+      if (j == 0) {
+        while (level >= 0 && cnt < n_max) {
+          uint32_t m2 = s_mask[level * kRaysPerBlock + slot];
+          if (m2 == 0) { --level; continue; }
+          int u = 31 - __clz(m2);
+          s_mask[level * kRaysPerBlock + slot] = (uint8_t)(m2 & ~(1u << u));
+          int parent = s_node[level * kRaysPerBlock + slot];
+          int ch = reinterpret_cast<const int *>(c.kids + (int64_t)parent * 2)[u];
+          float4 cb = c.box[ch];
+          if (cb.w < 0.0f) {
+            float a, b2;
+            nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, cb.x, cb.y, cb.z, -cb.w, a, b2);
+            I[cnt] = ch; LO[cnt] = a; HI[cnt] = b2;
+            ++cnt;
+            continue;
+          }
+          if (level + 1 >= kSvoLevels) { bad = true; level = -1; break; }
+          next = ch;
+          break;
+        }
+      }
+    }
+    next = __shfl_sync(0xffffffffu, next, lane & ~7);
+    cnt = __shfl_sync(0xffffffffu, cnt, lane & ~7);
+    level = __shfl_sync(0xffffffffu, level, lane & ~7);
+    if (expand) {
+      if (next >= 0 && cnt < n_max) {
+        ++level;
+        node = next;
+      } else {
+        expand = false;
+      }
+    }
+  }
+  if (live && SORTED && j == 0) hits[r] = cnt > 0;
+  if (bad && err) atomicOr(err, 1);
+  __syncwarp();
+  // rows: sorted variant sorts (and pads) every row with a hit and pads the
+  // empty ones; the raw variant pads with (-1, 0, 0)
+  for (int q = 0; q < kRaysPerWarp; ++q) {
+    int cq = __shfl_sync(0xffffffffu, cnt, q * 8);
+    bool lq = __shfl_sync(0xffffffffu, (int)live, q * 8) != 0;
+    if (!lq) continue;
+    int64_t rq = (int64_t)blockIdx.x * kRaysPerBlock + warp * kRaysPerWarp + q;
+    int32_t *Iq = idx + rq * n_max;
+    float *Lq = min_depth + rq * n_max, *Hq = max_depth + rq * n_max;
+    if (SORTED && cq > 0) {
+      if (n_max <= 32) warp_sort_row<1>(Iq, Lq, Hq, n_max, cq, lane);
+      else if (n_max <= 64) warp_sort_row<2>(Iq, Lq, Hq, n_max, cq, lane);
+      else warp_sort_row<4>(Iq, Lq, Hq, n_max, cq, lane);
+    } else {
+      float pad = SORTED ? NSVF_MAX_DEPTH_F : 0.0f;
+      for (int l = cq + lane; l < n_max; l += 32) { Iq[l] = -1; Lq[l] = pad; Hq[l] = pad; }
+    }
+    __syncwarp();
   }
 }
 
@@ -366,11 +428,11 @@ static int svo_launch(bool sorted, int b, int b_pts, int n, int m, float voxelsi
   int64_t rays = (int64_t)b * m;
   if (rays == 0) return nsvf_launch_status();
   if (sorted)
-    svo_kernel<true><<<nsvf_grid(rays, kRayBlock), kRayBlock, 0, s>>>(
+    svo_kernel<true><<<nsvf_grid(rays, kRaysPerBlock), kRayBlock, 0, s>>>(
         rays, m, b_pts, n, n_max, ray_start, ray_dir, box, kids, idx, min_depth, max_depth, hits,
         err);
   else
-    svo_kernel<false><<<nsvf_grid(rays, kRayBlock), kRayBlock, 0, s>>>(
+    svo_kernel<false><<<nsvf_grid(rays, kRaysPerBlock), kRayBlock, 0, s>>>(
         rays, m, b_pts, n, n_max, ray_start, ray_dir, box, kids, idx, min_depth, max_depth, hits,
         err);
   return nsvf_launch_status();

@@ -71,7 +71,8 @@ struct MlpParams {
   const __nv_bfloat16 *w[5];         // row-major [N, K]: 128x32, 3x 128x128, 4x128
   const float *b[5];                 // [128] x4, [4]
   float *out;                        // [ns, 4]: sigma, r, g, b
-  int64_t ns;                        // rows
+  int64_t ns;                        // rows (the capacity when ns_dev is set)
+  const int64_t *ns_dev;             // optional: row count read on the device
   int32_t *err;
 };
 
@@ -164,7 +165,15 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
   fence_after_sync();
   const uint32_t tmem = S.tmem_base;
   volatile int *abort = &S.abort;
-  const int64_t n_tiles = (p.ns + TILE - 1) / TILE;
+  // With ns_dev the row count comes from device memory (a count produced by
+  // an earlier kernel on the stream), clamped to the buffers' capacity p.ns.
+  int64_t ns = p.ns;
+  if (p.ns_dev) {
+    int64_t d = *p.ns_dev;
+    if (d > ns && tid == 0 && p.err) atomicOr(p.err, 2);
+    ns = d < 0 ? 0 : (d < ns ? d : ns);
+  }
+  const int64_t n_tiles = (ns + TILE - 1) / TILE;
   const int64_t G = gridDim.x, b = blockIdx.x;
 
   if (warp == 8) {
@@ -191,6 +200,9 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
     }
     __syncwarp();
   } else {
+    // The epilogue warps take every wait result warp-uniformly (__all_sync),
+    // so the .sync.aligned tcgen05.ld and the warp shuffles below always run
+    // with all 32 lanes, also when a timeout makes the CTA unwind.
     const int g = warp >> 2, q = warp & 3;
     const int row = q * 32 + lane;
     const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + 256u * g;
@@ -206,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       {
         float e[32];
         bool bad = false;
-        if (r < p.ns) {
+        if (r < ns) {
           if (MODE == kEmbIn) {
             const float4 *src = reinterpret_cast<const float4 *>(p.emb + r * E);
 #pragma unroll
@@ -249,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       fence_async_smem();
       mbar_arrive(&S.act_ready[g]);
       for (int layer = 0; layer < 4; ++layer) {
-        if (!mbar_wait(&S.mma_done[g], ph, abort)) { ok = false; break; }
+        if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g], ph, abort))) { ok = false; break; }
         ph ^= 1u;
         fence_after_sync();
         const float *bias = S.bias[layer];
@@ -273,7 +285,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
         mbar_arrive(&S.act_ready[g]);
       }
       if (!ok) break;
-      if (!mbar_wait(&S.mma_done[g], ph, abort)) { ok = false; break; }
+      if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g], ph, abort))) { ok = false; break; }
       ph ^= 1u;
       fence_after_sync();
       float v[16];
@@ -282,7 +294,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       fence_before_sync();
       float sigma = v[0] + S.bias4[0];
       if (MODE != kPrune) {
-        if (r < p.ns)
+        if (r < ns)
           reinterpret_cast<float4 *>(p.out)[r] =
               make_float4(sigma, v[1] + S.bias4[1], v[2] + S.bias4[2], v[3] + S.bias4[3]);
       } else {
@@ -290,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
         // reduced with min; workload rule: 1 - exp(-relu(s) * step), max.
         // Both are >= 0, so their float bits order like unsigned ints. A warp
         // whose rows all belong to one voxel reduces before its one atomic.
-        bool live = r < p.ns;
+        bool live = r < ns;
         int64_t vv = live ? r / ((int64_t)p.bits * p.bits * p.bits) : -1;
         uint32_t val;
         if (p.rule == 0) val = __float_as_uint(expf(-fmaxf(sigma, 0.0f)));
@@ -325,7 +337,17 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
 int g_num_sms = 0;
 
 template <int MODE>
+int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_override);
+
+template <int MODE>
 int launch_mlp(const MlpParams &p, cudaStream_t stream) {
+  return launch_mlp_grid<MODE>(p, stream, 0);
+}
+
+// grid_override < 0: one CTA per SM (the row count is only known on the
+// device); 0: sized from p.ns.
+template <int MODE>
+int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_override) {
   static bool attr_set = false;
   size_t smem = sizeof(MlpSmem) + 1024;
   if (!attr_set) {
@@ -338,7 +360,7 @@ int launch_mlp(const MlpParams &p, cudaStream_t stream) {
     attr_set = true;
   }
   int64_t n_tiles = (p.ns + TILE - 1) / TILE;
-  int64_t grid = (n_tiles + 1) / 2;
+  int64_t grid = grid_override < 0 ? g_num_sms : (n_tiles + 1) / 2;
   if (grid > g_num_sms) grid = g_num_sms;
   if (grid < 1) grid = 1;
   mlp_tc_kernel<MODE><<<(int)grid, kThreads, smem, stream>>>(p);
@@ -398,6 +420,35 @@ int nsvf_field_samples_bf16(int64_t n_samples, const int32_t *voxel, const float
   p.ns = n_samples;
   p.err = err;
   return launch_mlp<kSamplesIn>(p, (cudaStream_t)stream);
+}
+
+int nsvf_field_samples_bf16_dev(int64_t capacity, const int64_t *n_samples_dev,
+                                const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
+                                int64_t n_keys, float voxel_size, const float *centers,
+                                const int32_t *feats, const float *values,
+                                const void *const weights[5], const float *const biases[5],
+                                float *out, int32_t *err, void *stream) {
+  if (capacity < 0 || !n_samples_dev || n_voxels < 1 || n_keys < 1) return NSVF_ERR_INVALID;
+  if (capacity == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!voxel || !xyz_dist || !centers || !feats || !values || !out ||
+      !set_weights(p, weights, biases))
+    return NSVF_ERR_INVALID;
+  if ((((uintptr_t)xyz_dist) | ((uintptr_t)values) | ((uintptr_t)out) | ((uintptr_t)feats)) & 15)
+    return NSVF_ERR_INVALID;
+  p.vox = voxel;
+  p.xyzd = (const float4 *)xyz_dist;
+  p.centers = centers;
+  p.feats = feats;
+  p.values = (const float4 *)values;
+  p.n_vox = n_voxels;
+  p.n_keys = n_keys;
+  p.voxel_size = voxel_size;
+  p.out = out;
+  p.ns = capacity;
+  p.ns_dev = n_samples_dev;
+  p.err = err;
+  return launch_mlp_grid<kSamplesIn>(p, (cudaStream_t)stream, -1);
 }
 
 int nsvf_prune_scores_bf16(int64_t n_voxels, int bits, int rule, float step, int64_t n_keys,

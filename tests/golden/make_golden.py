@@ -195,6 +195,24 @@ def main():
             res = renderer(enc, field, rsh, rdh, dict(samples), st)
         for k in ["colors", "depths", "missed", "probs"]:
             g["render_%s" % k] = res[k].detach().numpy()
+        # training step gradients (reference autograd): loss against a target
+        # rendered from a second seeded embedding set
+        embed2 = scenes.voxel_embeddings(1000, 32, std=1.0, seed=7)
+        enc2 = make_encoder(ref, pts, vs, True, embed2)
+        st2 = enc2.precompute(id=None)
+        with torch.no_grad():
+            tgt = renderer(enc2, field, rsh, rdh, dict(samples), st2)["colors"]
+        enc.values.weight.grad = None
+        field.zero_grad()
+        st_g = enc.precompute(id=None)
+        res_g = renderer(enc, field, rsh, rdh, dict(samples), st_g)
+        loss = ((res_g["colors"] - tgt) ** 2).sum()
+        loss.backward()
+        g["grad_target_colors"] = tgt.numpy()
+        g["grad_loss"] = np.float64(loss.item())
+        g["grad_values"] = enc.values.weight.grad.numpy()
+        g["grad_W0"] = field.layers[0].weight.grad.numpy()
+        g["grad_W4"] = field.layers[4].weight.grad.numpy()
 
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **g)
 
