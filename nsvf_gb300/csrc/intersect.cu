@@ -9,6 +9,7 @@
 // every ray batch reads ONE copy of the voxels/octree, which stays resident in
 // L2 (c2 scene: 277,580 nodes x 48 B = 13 MB of a 129 MB L2).
 #include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -453,6 +454,56 @@ int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, i
                               void *stream) {
   return svo_launch(true, b, b_pts, n, m, voxelsize, n_max, ray_start, ray_dir, points, children,
                     idx, min_depth, max_depth, hits, err, workspace, stream);
+}
+
+// ------------------------------------------------------------------------
+// SVO intersection without any device allocation.
+//
+// For callers that cannot allocate device memory on the call path -- a
+// real-time render loop or a host engine that pre-partitions GPU memory and
+// hands this library only its own input and output buffers, or code that is
+// about to be captured into a CUDA graph -- the packed-octree scratch that
+// nsvf_svo_intersect takes as `workspace` lives here in a file-scope device
+// array instead. Its size is fixed: NSVF_NOALLOC_MAX_NODES nodes (b_pts * n)
+// at 48 bytes each, 24 MiB, which every GPU that loads this library holds
+// until the process exits. Host code only sees a stand-in for the array's
+// name, never its device address, so the address is looked up once per
+// device with cudaGetSymbolAddress (with that device current) and cached.
+static __device__ __align__(256) unsigned char g_svo_noalloc_scratch[(size_t)NSVF_NOALLOC_MAX_NODES * 48];
+
+static void *noalloc_scratch_for_current_device(int *status) {
+  static std::mutex mu;
+  static void *addr[256] = {nullptr};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    *status = NSVF_ERR_CUDA;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_svo_noalloc_scratch) != cudaSuccess || !p) {
+      *status = NSVF_ERR_CUDA;
+      return nullptr;
+    }
+    addr[dev] = p;
+  }
+  return addr[dev];
+}
+
+int nsvf_svo_intersect_noalloc(int b, int b_pts, int n, int m, float voxelsize, int n_max,
+                               const float *ray_start, const float *ray_dir, const float *points,
+                               const int32_t *children, int32_t *idx, float *min_depth,
+                               float *max_depth, int32_t *err, void *stream) {
+  if (b_pts < 1 || n < 1 || (int64_t)b_pts * n > (int64_t)NSVF_NOALLOC_MAX_NODES)
+    return (b_pts >= 1 && n >= 1) ? NSVF_ERR_CAPACITY : NSVF_ERR_INVALID;
+  int status = NSVF_OK;
+  void *scratch = noalloc_scratch_for_current_device(&status);
+  if (!scratch) return status;
+  // the pack kernel rewrites all b_pts * n scratch entries before the
+  // traversal reads them, so nothing left by an earlier call is read
+  return svo_launch(false, b, b_pts, n, m, voxelsize, n_max, ray_start, ray_dir, points, children,
+                    idx, min_depth, max_depth, nullptr, err, scratch, stream);
 }
 
 int nsvf_ball_intersect(int b, int b_pts, int n, int m, float radius, int n_max,
