@@ -256,6 +256,67 @@ int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *fi
                             void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Synchronisation-free chunk chain (served rendering under CUDA graphs)     */
+
+/* pinhole_rays: rays of `n` pixels of a pinhole frame from 18 camera floats
+ * in device memory: origin[3], camera-to-world rotation R[3][3] (row-major,
+ * columns right/down/forward), focal, cx, cy, width, first pixel, pixel
+ * count. Ray t = pixel first + t (row-major), direction normalize(R ((j + .5
+ * - cx) / f, (i + .5 - cy) / f, 1)); rays t >= count point away from the
+ * scene. The frame-to-ray step of the reference's reader
+ * (fairnr/modules/reader.py:92-119, fairnr/data/geometry.py:116-122). */
+int nsvf_pinhole_rays(int64_t n, const float *cam, float *ray_start, float *ray_dir,
+                      void *stream);
+
+/* compact_hits: given hits[n] (uint8) and scan = their inclusive prefix sum
+ * (int32), writes the hit rays' indices in order to pix and their number to
+ * *n_hit (both on the device). */
+int nsvf_compact_hits(int64_t n, const uint8_t *hits, const int32_t *scan, int64_t *pix,
+                      int64_t *n_hit, void *stream);
+
+/* gather_probs: for rows i < *n_hit, copies the sorted hit list of ray pix[i]
+ * ([., max_hits] idx/min/max) and builds its sampling distribution as
+ * fairnr/models/nsvf.py:65-74: d = max - min on hit slots, probs = d / sum d,
+ * steps = sum d / step_size (sum in slot order). */
+int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
+                      const int64_t *pix, const int32_t *idx, const float *min_depth,
+                      const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
+                      float *probs, float *steps, void *stream);
+
+/* sample_count_dev / sample_compact_dev: nsvf_sample_count /
+ * nsvf_sample_compact with the row count *n_rows_dev read on the device
+ * (rows past it: count 0) and the reference wrapper's layout for that many
+ * rows; ray_index (may be NULL) maps row i to its ray's origin/direction;
+ * samples past sample_cap are not written (err bit 1). */
+int nsvf_sample_count_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                          const int32_t *pts_idx, const float *min_depth, const float *max_depth,
+                          const float *probs, const float *steps, int32_t *count, void *stream);
+int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                            const int32_t *pts_idx, const float *min_depth,
+                            const float *max_depth, const float *probs, const float *steps,
+                            const float *ray_start, int64_t ray_start_stride,
+                            const float *ray_dir, const int64_t *ray_index,
+                            const int64_t *offset, int64_t sample_cap, int32_t *voxel,
+                            float *xyz_dist, float *depth, int32_t *err, void *stream);
+
+/* composite_segments_dev: nsvf_composite_segments over *n_rays_dev rays. */
+int nsvf_composite_segments_dev(int64_t rays_cap, const int64_t *n_rays_dev,
+                                const int64_t *offset, const float *field, const float *xyz_dist,
+                                const float *depth, const int64_t *pixel, float sigma_scale,
+                                const float bg[3], float bg_depth, float *out_color,
+                                float *out_depth, float *out_missed, int kahan, void *stream);
+
+/* field_samples_bf16_dev: nsvf_field_samples_bf16 on *n_samples_dev samples
+ * (at most `capacity`; a larger count sets err bit 1), one persistent CTA
+ * per SM. */
+int nsvf_field_samples_bf16_dev(int64_t capacity, const int64_t *n_samples_dev,
+                                const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
+                                int64_t n_keys, float voxel_size, const float *centers,
+                                const int32_t *feats, const float *values,
+                                const void *const weights[5], const float *const biases[5],
+                                float *out, int32_t *err, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Field MLP on the tensor cores                                             */
 
 /* mlp_forward_bf16: the workloads' field MLP 32 -> 128 -> 128 -> 128 -> 128

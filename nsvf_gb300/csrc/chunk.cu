@@ -1,0 +1,113 @@
+// Small kernels that make the served chain free of host synchronisation, so
+// that a whole ray chunk can be captured into one CUDA graph:
+//   * pinhole ray generation from camera parameters in device memory;
+//   * order-preserving compaction of the hit rays (count stays on device);
+//   * gather of the hit rays' sorted hit lists with their sampling
+//     distribution (probs, steps: fairnr/models/nsvf.py:65-74).
+#include "common.cuh"
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// cam[18] = (origin xyz, camera-to-world rotation R[3][3] row-major with
+// columns right/down/forward, focal, cx, cy, width, first pixel, pixel
+// count), read on the device so a captured graph can render any chunk of
+// any frame. Ray t is pixel first + t (row-major) and looks along
+// normalize(R ((j + .5 - cx) / f, (i + .5 - cy) / f, 1)); rays t >= count
+// repeat the last pixel with the direction reversed, away from the scene.
+__global__ void pinhole_kernel(int64_t n, const float *__restrict__ cam, float *__restrict__ ro,
+                               float *__restrict__ rd) {
+  int64_t t = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (t >= n) return;
+  float f = cam[12], cx = cam[13], cy = cam[14];
+  int64_t W = (int64_t)cam[15];
+  int64_t first = (int64_t)cam[16], count = (int64_t)cam[17];
+  if (count < 1) count = 1;
+  int64_t pix = first + (t < count ? t : count - 1);
+  float j = (float)(pix % W) + 0.5f, i = (float)(pix / W) + 0.5f;
+  float a = (j - cx) / f, b = (i - cy) / f;
+  float x = cam[3] * a + cam[4] * b + cam[5];
+  float y = cam[6] * a + cam[7] * b + cam[8];
+  float z = cam[9] * a + cam[10] * b + cam[11];
+  float inv = rsqrtf(x * x + y * y + z * z);
+  if (t >= count) inv = -inv;
+  ro[t * 3 + 0] = cam[0]; ro[t * 3 + 1] = cam[1]; ro[t * 3 + 2] = cam[2];
+  rd[t * 3 + 0] = x * inv; rd[t * 3 + 1] = y * inv; rd[t * 3 + 2] = z * inv;
+}
+
+// scan = inclusive prefix sum of hits: hit ray r goes to pix[scan[r] - 1].
+__global__ void compact_hits_kernel(int64_t n, const uint8_t *__restrict__ hits,
+                                    const int32_t *__restrict__ scan, int64_t *__restrict__ pix,
+                                    int64_t *__restrict__ n_hit) {
+  int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (r >= n) return;
+  if (hits[r]) pix[scan[r] - 1] = r;
+  if (r == n - 1) *n_hit = scan[r];
+}
+
+// Row i < n_hit: copy the hit list of ray pix[i] and build its sampling
+// distribution: d = max - min where the slot is a hit, probs = d / sum(d),
+// steps = sum(d) / step (sum in slot order).
+__global__ void gather_probs_kernel(int64_t cap, const int64_t *__restrict__ n_hit, int H,
+                                    float step, const int64_t *__restrict__ pix,
+                                    const int32_t *__restrict__ idx, const float *__restrict__ lo,
+                                    const float *__restrict__ hi, int32_t *__restrict__ I,
+                                    float *__restrict__ L, float *__restrict__ U,
+                                    float *__restrict__ probs, float *__restrict__ steps) {
+  int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  int64_t n = *n_hit;
+  if (i >= cap || i >= n) return;
+  int64_t r = pix[i];
+  float tot = 0.0f;
+  for (int k = 0; k < H; ++k) {
+    int32_t id = idx[r * H + k];
+    float a = lo[r * H + k], b = hi[r * H + k];
+    I[i * H + k] = id; L[i * H + k] = a; U[i * H + k] = b;
+    tot += (id == -1) ? 0.0f : (b - a);
+  }
+  for (int k = 0; k < H; ++k) {
+    float d = (I[i * H + k] == -1) ? 0.0f : (U[i * H + k] - L[i * H + k]);
+    probs[i * H + k] = d / tot;
+  }
+  steps[i] = tot / step;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsvf_pinhole_rays(int64_t n, const float *cam, float *ray_start, float *ray_dir,
+                      void *stream) {
+  if (n < 0 || !cam) return NSVF_ERR_INVALID;
+  if (n == 0) return NSVF_OK;
+  if (!ray_start || !ray_dir) return NSVF_ERR_INVALID;
+  pinhole_kernel<<<nsvf_grid(n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(n, cam, ray_start,
+                                                                          ray_dir);
+  return nsvf_launch_status();
+}
+
+int nsvf_compact_hits(int64_t n, const uint8_t *hits, const int32_t *scan, int64_t *pix,
+                      int64_t *n_hit, void *stream) {
+  if (n < 1 || !hits || !scan || !pix || !n_hit) return NSVF_ERR_INVALID;
+  compact_hits_kernel<<<nsvf_grid(n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(n, hits, scan, pix,
+                                                                               n_hit);
+  return nsvf_launch_status();
+}
+
+int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
+                      const int64_t *pix, const int32_t *idx, const float *min_depth,
+                      const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
+                      float *probs, float *steps, void *stream) {
+  if (cap < 0 || max_hits < 1 || !n_hit) return NSVF_ERR_INVALID;
+  if (cap == 0) return NSVF_OK;
+  if (!pix || !idx || !min_depth || !max_depth || !out_idx || !out_min || !out_max || !probs ||
+      !steps)
+    return NSVF_ERR_INVALID;
+  gather_probs_kernel<<<nsvf_grid(cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      cap, n_hit, max_hits, step_size, pix, idx, min_depth, max_depth, out_idx, out_min, out_max,
+      probs, steps);
+  return nsvf_launch_status();
+}
+
+}  // extern "C"

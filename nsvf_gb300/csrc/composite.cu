@@ -172,9 +172,13 @@ __global__ void __launch_bounds__(kWarps * 32) composite_segments_kernel(
     const float4 *__restrict__ xyzd, const float *__restrict__ depth,
     const int64_t *__restrict__ pix, float sigma_scale, float bg_r, float bg_g, float bg_b,
     float bg_depth, float *__restrict__ out_color, float *__restrict__ out_depth,
-    float *__restrict__ out_missed, int kahan) {
+    float *__restrict__ out_missed, int kahan, const int64_t *__restrict__ n_dev) {
   int lane = threadIdx.x & 31;
   int64_t r = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
+  if (n_dev) {
+    int64_t nd = *n_dev;
+    if (nd < rays) rays = nd < 0 ? 0 : nd;
+  }
   if (r >= rays) return;
   int64_t a = offset[r], n = offset[r + 1] - a;
   Prefix carry{0.f, 0.f};
@@ -223,7 +227,23 @@ int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *fi
     return NSVF_ERR_INVALID;
   composite_segments_kernel<<<nsvf_grid(rays, kWarps), kWarps * 32, 0, (cudaStream_t)stream>>>(
       rays, offset, (const float4 *)field, (const float4 *)xyz_dist, depth, pixel, sigma_scale,
-      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan);
+      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan, nullptr);
+  return nsvf_launch_status();
+}
+
+int nsvf_composite_segments_dev(int64_t rays_cap, const int64_t *n_rays_dev,
+                                const int64_t *offset, const float *field, const float *xyz_dist,
+                                const float *depth, const int64_t *pixel, float sigma_scale,
+                                const float bg[3], float bg_depth, float *out_color,
+                                float *out_depth, float *out_missed, int kahan, void *stream) {
+  if (rays_cap < 0 || !bg || !n_rays_dev) return NSVF_ERR_INVALID;
+  if (rays_cap == 0) return NSVF_OK;
+  if (!offset || !field || !xyz_dist || !depth || !pixel || !out_color || !out_depth ||
+      !out_missed || ((((uintptr_t)field) | ((uintptr_t)xyz_dist)) & 15))
+    return NSVF_ERR_INVALID;
+  composite_segments_kernel<<<nsvf_grid(rays_cap, kWarps), kWarps * 32, 0, (cudaStream_t)stream>>>(
+      rays_cap, offset, (const float4 *)field, (const float4 *)xyz_dist, depth, pixel, sigma_scale,
+      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan, n_rays_dev);
   return nsvf_launch_status();
 }
 

@@ -29,19 +29,24 @@ constexpr int E = 32;       // embedding width (first layer K)
 constexpr int HID = 128;    // hidden width
 constexpr int NOUT = 16;    // N of the last MMA (4 outputs used)
 constexpr int TILE = 128;   // samples per MMA tile (M)
-constexpr int kThreads = 9 * 32;
+constexpr int NB = 4;       // input tile ring depth
+constexpr int kMmaWarp = 8;
+constexpr int kLoaderWarp0 = 9;                 // warps 9..16: two loader warpgroups
+constexpr int kThreads = 17 * 32;
 constexpr uint32_t kTmemCols = 512;
 
 struct __align__(128) MlpSmem {
   __nv_bfloat16 w0[HID * E];
   __nv_bfloat16 wh[3][HID * HID];
   __nv_bfloat16 w4[NOUT * HID];
-  __nv_bfloat16 ain[2][TILE * E];
+  __nv_bfloat16 ain[NB][TILE * E];
   __nv_bfloat16 ah[2][TILE * HID];
   float bias[4][HID];
   float bias4[NOUT];
-  uint64_t mma_done[2];
-  uint64_t act_ready[2];
+  uint64_t mma_done[2][5];   // per slot and layer: one phase per tile
+  uint64_t act_ready[2];     // epilogue -> MMA: hidden activations written
+  uint64_t in_full[NB];      // loaders -> MMA: input tile written
+  uint64_t in_empty[NB];     // MMA -> loaders: first layer done reading
   uint32_t tmem_base;
   int abort;
 };
@@ -139,6 +144,60 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const __nv_bfloat16
   }
 }
 
+// bf16x2 of (relu(lo), relu(hi)) with round-to-nearest-even, one instruction
+__device__ __forceinline__ uint32_t pack_relu_bf16x2(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %2, %1;\n" : "=r"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+
+// The input row `r` of a tile (embedding, interpolated sample or pruning
+// point) as 32 FP32 values; rows >= ns are zero.
+template <int MODE>
+__device__ __forceinline__ void input_row(const MlpParams &p, int64_t r, int64_t ns, float (&e)[32],
+                                          bool &bad) {
+  if (r >= ns) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) e[j] = 0.0f;
+    return;
+  }
+  if (MODE == kEmbIn) {
+    const float4 *src = reinterpret_cast<const float4 *>(p.emb + r * E);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float4 x = __ldg(src + j);
+      e[4 * j] = x.x; e[4 * j + 1] = x.y; e[4 * j + 2] = x.z; e[4 * j + 3] = x.w;
+    }
+  } else if (MODE == kSamplesIn) {
+    float4 x = p.xyzd[r];
+    interp_point(p, p.vox[r], x.x, x.y, x.z, e, bad);
+  } else {
+    // point i of voxel v: offset_points order (x slowest), offset
+    // ((2 i_d + 1) - bits) / (bits - 1) times half a voxel
+    int64_t P = (int64_t)p.bits * p.bits * p.bits;
+    int64_t v = r / P, i = r % P;
+    int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits), iz = (int)(i % p.bits);
+    const float *c = p.centers + v * 3;
+    float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
+    float x = c[0] + ((float)(2 * ix + 1 - p.bits) / den) * hv;
+    float y = c[1] + ((float)(2 * iy + 1 - p.bits) / den) * hv;
+    float z = c[2] + ((float)(2 * iz + 1 - p.bits) / den) * hv;
+    interp_point(p, v, x, y, z, e, bad);
+  }
+}
+
+// Persistent CTA (one per SM), 17 warps:
+//   warps 0-3, 4-7  epilogue warpgroups of tile slots 0 and 1 (TMEM columns
+//                   [256 g, 256 g + 144)): bias + ReLU + bf16 of each hidden
+//                   layer back to shared memory, and the output stage;
+//   warp 8          TMEM allocation; lane 0 issues all tcgen05.mma;
+//   warps 9-16      two loader warpgroups that build the input tiles (the
+//                   embedding gathers and interpolation) into a ring of NB
+//                   buffers ahead of the MMAs.
+// The CTA's tiles are b, b + G, b + 2G, ...: local tile i uses slot i % 2,
+// ring buffer i % NB and loader group i % 2. Each mbarrier completes exactly
+// one phase per use and every waiter consumes it before the next phase can
+// complete, so parity waits are unambiguous.
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -151,14 +210,18 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
   if (tid < NOUT) S.bias4[tid] = tid < 4 ? p.b[4][tid] : 0.0f;
   if (tid == 0) {
-    mbar_init(&S.mma_done[0], 1);
-    mbar_init(&S.mma_done[1], 1);
-    mbar_init(&S.act_ready[0], 128);
-    mbar_init(&S.act_ready[1], 128);
+    for (int g = 0; g < 2; ++g) {
+      for (int l = 0; l < 5; ++l) mbar_init(&S.mma_done[g][l], 1);
+      mbar_init(&S.act_ready[g], 128);
+    }
+    for (int q = 0; q < NB; ++q) {
+      mbar_init(&S.in_full[q], 128);
+      mbar_init(&S.in_empty[q], 1);
+    }
     S.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 8) tmem_alloc(&S.tmem_base, kTmemCols);
+  if (warp == kMmaWarp) tmem_alloc(&S.tmem_base, kTmemCols);
   fence_async_smem();
   fence_before_sync();
   __syncthreads();
@@ -175,118 +238,109 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
   }
   const int64_t n_tiles = (ns + TILE - 1) / TILE;
   const int64_t G = gridDim.x, b = blockIdx.x;
+  auto tile_of = [&](int64_t i) { return b + i * G; };
 
-  if (warp == 8) {
+  if (warp == kMmaWarp) {
     if (lane == 0) {
-      uint32_t ph[2] = {0u, 0u};
+      uint32_t ph_act[2] = {0u, 0u};
       bool ok = true;
-      for (int64_t i = 0; ok; ++i) {
-        bool has[2] = {(2 * i) * G + b < n_tiles, (2 * i + 1) * G + b < n_tiles};
+      for (int64_t i = 0; ok; i += 2) {
+        bool has[2] = {tile_of(i) < n_tiles, tile_of(i + 1) < n_tiles};
         if (!has[0]) break;
         for (int layer = 0; layer < 5 && ok; ++layer) {
           for (int g = 0; g < 2 && ok; ++g) {
             if (!has[g]) continue;
-            if (!mbar_wait(&S.act_ready[g], ph[g], abort)) { ok = false; break; }
-            ph[g] ^= 1u;
-            fence_after_sync();
+            int64_t ii = i + g;
             uint32_t d = tmem + 256u * g;
-            if (layer == 0) issue_layer(d, S.ain[g], S.w0, E, HID);
-            else if (layer < 4) issue_layer(d, S.ah[g], S.wh[layer - 1], HID, HID);
-            else issue_layer(d + 128u, S.ah[g], S.w4, HID, NOUT);
-            mma_commit(&S.mma_done[g]);
+            if (layer == 0) {
+              int q = (int)(ii % NB);
+              if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
+              fence_after_sync();
+              issue_layer(d, S.ain[q], S.w0, E, HID);
+              mma_commit(&S.mma_done[g][0]);
+              mma_commit(&S.in_empty[q]);
+            } else {
+              if (!mbar_wait(&S.act_ready[g], ph_act[g], abort)) { ok = false; break; }
+              ph_act[g] ^= 1u;
+              fence_after_sync();
+              if (layer < 4) issue_layer(d, S.ah[g], S.wh[layer - 1], HID, HID);
+              else issue_layer(d + 128u, S.ah[g], S.w4, HID, NOUT);
+              mma_commit(&S.mma_done[g][layer]);
+            }
           }
         }
       }
     }
     __syncwarp();
-  } else {
-    // The epilogue warps take every wait result warp-uniformly (__all_sync),
-    // so the .sync.aligned tcgen05.ld and the warp shuffles below always run
-    // with all 32 lanes, also when a timeout makes the CTA unwind.
-    const int g = warp >> 2, q = warp & 3;
-    const int row = q * 32 + lane;
-    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + 256u * g;
-    uint8_t *ah = reinterpret_cast<uint8_t *>(S.ah[g]);
-    uint8_t *ain = reinterpret_cast<uint8_t *>(S.ain[g]);
-    uint32_t ph = 0;
-    bool ok = true;
-    for (int64_t i = 0; ok; ++i) {
-      int64_t tile = (2 * i + g) * G + b;
+  } else if (warp >= kLoaderWarp0) {
+    // loaders: every wait result is taken warp-uniformly
+    const int L = (warp - kLoaderWarp0) >> 2;
+    const int row = ((warp - kLoaderWarp0) & 3) * 32 + lane;
+    for (int64_t i = L;; i += 2) {
+      int64_t tile = tile_of(i);
       if (tile >= n_tiles) break;
-      int64_t r = tile * TILE + row;
-      // input tile -> bf16, K-major
-      {
-        float e[32];
-        bool bad = false;
-        if (r < ns) {
-          if (MODE == kEmbIn) {
-            const float4 *src = reinterpret_cast<const float4 *>(p.emb + r * E);
+      int q = (int)(i % NB);
+      // the first round finds every buffer free (parity of the phase before
+      // the barrier's first)
+      uint32_t par = (uint32_t)(((i / NB) & 1) ^ 1);
+      if (!__all_sync(0xffffffffu, mbar_wait(&S.in_empty[q], par, abort))) break;
+      float e[32];
+      bool bad = false;
+      input_row<MODE>(p, tile * TILE + row, ns, e, bad);
+      if (bad && p.err) atomicOr(p.err, 4);
+      uint8_t *ain = reinterpret_cast<uint8_t *>(S.ain[q]);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              float4 x = __ldg(src + j);
-              e[4 * j] = x.x; e[4 * j + 1] = x.y; e[4 * j + 2] = x.z; e[4 * j + 3] = x.w;
-            }
-          } else if (MODE == kSamplesIn) {
-            float4 x = p.xyzd[r];
-            interp_point(p, p.vox[r], x.x, x.y, x.z, e, bad);
-          } else {
-            // point i of voxel v: offset_points order (x slowest), offset
-            // ((2 i_d + 1) - bits) / (bits - 1) times half a voxel
-            int64_t P = (int64_t)p.bits * p.bits * p.bits;
-            int64_t v = r / P, i = r % P;
-            int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits),
-                iz = (int)(i % p.bits);
-            const float *c = p.centers + v * 3;
-            float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
-            float x = c[0] + ((float)(2 * ix + 1 - p.bits) / den) * hv;
-            float y = c[1] + ((float)(2 * iy + 1 - p.bits) / den) * hv;
-            float z = c[2] + ((float)(2 * iz + 1 - p.bits) / den) * hv;
-            interp_point(p, v, x, y, z, e, bad);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) e[j] = 0.0f;
-        }
-        if (bad && p.err) atomicOr(p.err, 4);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          uint4 v;
-          v.x = pack_bf16x2(e[8 * c + 0], e[8 * c + 1]);
-          v.y = pack_bf16x2(e[8 * c + 2], e[8 * c + 3]);
-          v.z = pack_bf16x2(e[8 * c + 4], e[8 * c + 5]);
-          v.w = pack_bf16x2(e[8 * c + 6], e[8 * c + 7]);
-          *reinterpret_cast<uint4 *>(ain + kmajor_off(row, c * 8, E)) = v;
-        }
+      for (int c = 0; c < 4; ++c) {
+        uint4 v;
+        v.x = pack_bf16x2(e[8 * c + 0], e[8 * c + 1]);
+        v.y = pack_bf16x2(e[8 * c + 2], e[8 * c + 3]);
+        v.z = pack_bf16x2(e[8 * c + 4], e[8 * c + 5]);
+        v.w = pack_bf16x2(e[8 * c + 6], e[8 * c + 7]);
+        *reinterpret_cast<uint4 *>(ain + kmajor_off(row, c * 8, E)) = v;
       }
       fence_async_smem();
-      mbar_arrive(&S.act_ready[g]);
+      mbar_arrive(&S.in_full[q]);
+    }
+  } else {
+    // Epilogue warpgroups. Every wait result is taken warp-uniformly
+    // (__all_sync), so the .sync.aligned tcgen05.ld and the warp shuffles
+    // below always run with all 32 lanes, also when a timeout makes the CTA
+    // unwind.
+    const int g = warp >> 2, q4 = warp & 3;
+    const int row = q4 * 32 + lane;
+    const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + 256u * g;
+    uint8_t *ah = reinterpret_cast<uint8_t *>(S.ah[g]);
+    bool ok = true;
+    for (int64_t i = g; ok; i += 2) {
+      int64_t tile = tile_of(i);
+      if (tile >= n_tiles) break;
+      const uint32_t par = (uint32_t)((i >> 1) & 1);
+      int64_t r = tile * TILE + row;
       for (int layer = 0; layer < 4; ++layer) {
-        if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g], ph, abort))) { ok = false; break; }
-        ph ^= 1u;
+        if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) { ok = false; break; }
         fence_after_sync();
         const float *bias = S.bias[layer];
 #pragma unroll 1
-        for (int c = 0; c < HID; c += 16) {
-          float v[16];
-          tmem_ld16(tl + c, v);
+        for (int c = 0; c < HID; c += 32) {
+          float v[32];
+          tmem_ld16(tl + c, *reinterpret_cast<float(*)[16]>(v));
+          tmem_ld16(tl + c + 16, *reinterpret_cast<float(*)[16]>(v + 16));
           tmem_wait_ld();
-          uint32_t pk[8];
+          uint32_t pk[16];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            float a0 = fmaxf(v[2 * j] + bias[c + 2 * j], 0.0f);
-            float a1 = fmaxf(v[2 * j + 1] + bias[c + 2 * j + 1], 0.0f);
-            pk[j] = pack_bf16x2(a0, a1);
-          }
-          *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c, HID)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-          *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8, HID)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+          for (int j = 0; j < 16; ++j)
+            pk[j] = pack_relu_bf16x2(v[2 * j] + bias[c + 2 * j], v[2 * j + 1] + bias[c + 2 * j + 1]);
+#pragma unroll
+          for (int h = 0; h < 4; ++h)
+            *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8 * h, HID)) =
+                make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
         }
         fence_before_sync();
         fence_async_smem();
         mbar_arrive(&S.act_ready[g]);
       }
       if (!ok) break;
-      if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g], ph, abort))) { ok = false; break; }
-      ph ^= 1u;
+      if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) { ok = false; break; }
       fence_after_sync();
       float v[16];
       tmem_ld16(tl + 128u, v);
@@ -328,7 +382,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
   fence_before_sync();
   __syncthreads();
   if (tid == 0 && S.abort && p.err) atomicOr(p.err, 8);
-  if (warp == 8) {
+  if (warp == kMmaWarp) {
     fence_after_sync();
     tmem_dealloc(tmem, kTmemCols);
   }

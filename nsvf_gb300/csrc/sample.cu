@@ -142,13 +142,32 @@ struct CountEmit {
   }
 };
 
+// With n_dev the number of rows (hit rays) is read on the device and the
+// launch layout is the reference wrapper's for that many rays (200 blocks,
+// 800-column launches); rows past it get count 0.
+__device__ __forceinline__ bool dyn_rows(const int64_t *n_dev, int64_t cap, int64_t &rows,
+                                         int64_t &K, int64_t &C, int64_t &N, int64_t &G) {
+  if (!n_dev) return false;
+  int64_t n = *n_dev;
+  rows = n < 0 ? 0 : (n < cap ? n : cap);
+  N = rows;
+  G = 200;
+  K = (N + G - 1) / G;
+  if (K < 1) K = 1;
+  C = 800;
+  return true;
+}
+
 __global__ void __launch_bounds__(kBlock) icdf_count_kernel(
     int64_t rows, int H, const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
     const float *__restrict__ max_depth, const float *__restrict__ probs,
     const float *__restrict__ steps, int64_t K, int64_t C, int64_t N, int64_t G,
-    int32_t *__restrict__ count) {
+    const int64_t *__restrict__ n_dev, int32_t *__restrict__ count) {
   int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (r >= rows) return;
+  int64_t cap = rows;
+  dyn_rows(n_dev, cap, rows, K, C, N, G);
+  if (r >= cap) return;
+  if (r >= rows) { count[r] = 0; return; }
   int64_t tail, nxt;
   icdf_rows(r, K, C, N, G, tail, nxt);
   CountEmit em{0};
@@ -182,17 +201,27 @@ __global__ void __launch_bounds__(kBlock) icdf_compact_kernel(
     int64_t rows, int H, const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
     const float *__restrict__ max_depth, const float *__restrict__ probs,
     const float *__restrict__ steps, int64_t K, int64_t C, int64_t N, int64_t G,
-    const float *__restrict__ ray_start, int64_t ray_start_stride,
-    const float *__restrict__ ray_dir, const int64_t *__restrict__ offset,
-    int32_t *__restrict__ vox, float4 *__restrict__ xyzd, float *__restrict__ depth,
-    int32_t *__restrict__ err) {
+    const int64_t *__restrict__ n_dev, const float *__restrict__ ray_start,
+    int64_t ray_start_stride, const float *__restrict__ ray_dir,
+    const int64_t *__restrict__ ray_index, const int64_t *__restrict__ offset,
+    int64_t sample_cap, int32_t *__restrict__ vox, float4 *__restrict__ xyzd,
+    float *__restrict__ depth, int32_t *__restrict__ err) {
   int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  int64_t cap = rows;
+  dyn_rows(n_dev, cap, rows, K, C, N, G);
   if (r >= rows) return;
   int64_t tail, nxt;
   icdf_rows(r, K, C, N, G, tail, nxt);
-  const float *o = ray_start + r * ray_start_stride;
-  CompactEmit em{vox, xyzd, depth, o[0], o[1], o[2], ray_dir[r * 3], ray_dir[r * 3 + 1],
-                 ray_dir[r * 3 + 2], offset[r], offset[r + 1]};
+  // the ray's origin/direction: row r of the ray arrays, or row ray_index[r]
+  int64_t rr = ray_index ? ray_index[r] : r;
+  const float *o = ray_start + rr * ray_start_stride;
+  int64_t end = offset[r + 1];
+  if (end > sample_cap) {
+    if (err) atomicOr(err, 2);
+    end = sample_cap;
+  }
+  CompactEmit em{vox, xyzd, depth, o[0], o[1], o[2], ray_dir[rr * 3], ray_dir[rr * 3 + 1],
+                 ray_dir[rr * 3 + 2], offset[r] < end ? offset[r] : end, end};
   bool overflow = icdf_walk(H, pts_idx + r * H, pts_idx + tail * H, pts_idx, nxt,
                             min_depth + r * H, max_depth + r * H, probs + r * H, steps[r],
                             nullptr, 0, -1.0f, em);
@@ -291,7 +320,7 @@ int nsvf_sample_count(int64_t rows, int max_hits, const int32_t *pts_idx, const 
   int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
   if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
   icdf_count_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, count);
+      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count);
   return nsvf_launch_status();
 }
 
@@ -310,8 +339,42 @@ int nsvf_sample_compact(int64_t rows, int max_hits, const int32_t *pts_idx,
   int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
   if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
   icdf_compact_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, ray_start,
-      ray_start_stride, ray_dir, offset, voxel, (float4 *)xyz_dist, depth, err);
+      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, ray_start,
+      ray_start_stride, ray_dir, nullptr, offset, INT64_MAX, voxel, (float4 *)xyz_dist, depth,
+      err);
+  return nsvf_launch_status();
+}
+
+int nsvf_sample_count_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                          const int32_t *pts_idx, const float *min_depth, const float *max_depth,
+                          const float *probs, const float *steps, int32_t *count, void *stream) {
+  if (rows_cap < 0 || max_hits < 1 || !n_rows_dev) return NSVF_ERR_INVALID;
+  if (rows_cap == 0) return NSVF_OK;
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !count) return NSVF_ERR_INVALID;
+  icdf_count_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+      count);
+  return nsvf_launch_status();
+}
+
+int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                            const int32_t *pts_idx, const float *min_depth,
+                            const float *max_depth, const float *probs, const float *steps,
+                            const float *ray_start, int64_t ray_start_stride,
+                            const float *ray_dir, const int64_t *ray_index,
+                            const int64_t *offset, int64_t sample_cap, int32_t *voxel,
+                            float *xyz_dist, float *depth, int32_t *err, void *stream) {
+  if (rows_cap < 0 || max_hits < 1 || !n_rows_dev || sample_cap < 0 ||
+      (ray_start_stride != 0 && ray_start_stride != 3))
+    return NSVF_ERR_INVALID;
+  if (rows_cap == 0) return NSVF_OK;
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !ray_start || !ray_dir ||
+      !offset || !voxel || !xyz_dist || !depth || (((uintptr_t)xyz_dist) & 15))
+    return NSVF_ERR_INVALID;
+  icdf_compact_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+      ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
+      (float4 *)xyz_dist, depth, err);
   return nsvf_launch_status();
 }
 
