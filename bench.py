@@ -46,6 +46,8 @@ def parse():
                     help="rays of the frame in the CPU baseline sample")
     ap.add_argument("--size", type=int, default=800,
                     help="frame side in pixels (800 = the c2 workload; smaller for profiling)")
+    ap.add_argument("--serve-requests", type=int, default=200,
+                    help="requests of the multi-scene serving run (c5); 0 skips it")
     return ap.parse_args()
 
 
@@ -77,6 +79,131 @@ def frame_rays(index, size=800):
     from nsvf_gb300 import scenes
     rs, rd = scenes.frame_view(index % 100, size=size)
     return rs, rd
+
+
+def prune_bench(dev, sc, bits=8, th=0.5):
+    """The c2 pruning pass: sigma at bits^3 points per voxel, keep voxels with
+    max(1 - exp(-relu(sigma) * step)) >= th. Fused BF16 tensor-core kernel
+    (nsvf_prune_scores_bf16) vs the FP32 path (offset_points, the FP32
+    interpolation kernel, the field's FP32 MLP), with the masks compared."""
+    import torch
+    from nsvf_gb300 import geometry
+    from nsvf_gb300.functional import trilinear_embed
+    from nsvf_gb300.mlp import TensorCoreMLP
+    enc, field, states = sc["enc"], sc["field"], sc["states"]
+    centers = states["voxel_center_xyz"].float().contiguous()
+    feats = states["voxel_vertex_idx"].int().contiguous()
+    values = states["voxel_vertex_emb"].detach().float().contiguous()
+    vs, step = float(enc.voxel_size), float(enc.step_size)
+    mlp = TensorCoreMLP(field)
+    V = centers.shape[0]
+    mlp.prune_scores(centers[:256], feats[:256], values, vs, bits=bits, rule=1, step=step)
+    torch.cuda.synchronize(dev)
+    s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record()
+    score = mlp.prune_scores(centers, feats, values, vs, bits=bits, rule=1, step=step)
+    e0.record()
+    torch.cuda.synchronize(dev)
+    keep_bf16 = score >= th
+    s1, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s1.record()
+    alpha = torch.empty(V, device=dev)
+    hv = torch.tensor(vs / 2.0, device=dev)
+    chunk = 8192
+    with torch.no_grad():
+        for i in range(0, V, chunk):
+            c = centers[i:i + chunk]
+            pts = geometry.offset_points(c, hv, bits=bits).reshape(-1, 3)
+            idx = torch.arange(i, i + c.shape[0], device=dev)[:, None].expand(-1, bits ** 3).reshape(-1)
+            emb = trilinear_embed(idx, pts, centers, feats, values, vs)
+            sig = field.mlp(emb)[:, 0].reshape(-1, bits ** 3)
+            alpha[i:i + c.shape[0]] = (1 - torch.exp(-torch.relu(sig) * step)).max(-1)[0]
+    e1.record()
+    torch.cuda.synchronize(dev)
+    keep_fp32 = alpha >= th
+    return {"workload": "c2 pruning pass: %d voxels x %d^3 points, keep max(1-exp(-relu(s)*step)) >= %g"
+                        % (V, bits, th),
+            "bf16_fused_ms": round(s0.elapsed_time(e0), 3), "fp32_ms": round(s1.elapsed_time(e1), 3),
+            "tflop": round(107520.0 * V * bits ** 3 / 1e12, 2),
+            "bf16_tflops_achieved": round(107520.0 * V * bits ** 3 / (s0.elapsed_time(e0) / 1e3) / 1e12, 1),
+            "kept_bf16": int(keep_bf16.sum()), "kept_fp32": int(keep_fp32.sum()),
+            "mask_mismatches": int((keep_bf16 != keep_fp32).sum()),
+            "max_abs_alpha_diff": float((score - alpha).abs().max())}
+
+
+def serve_bench(dev, n_requests, rate=200.0, seed=0):
+    """The c5 serving workload: eight resident seeded scenes (sphere/torus/box
+    unions, 10k-400k voxels), each with its own 4x128 MLP; Poisson arrivals at
+    `rate`/s, each request one scene at a random camera on the radius-4 sphere
+    and a resolution in {128, 256, 512, 800}^2. Served BF16 path (continuous
+    batching of 64k-ray chunks on 3 streams, CUDA graphs) vs the plain FP32
+    drop-in path rendering a prefix of the same requests one at a time."""
+    import torch
+    from nsvf_gb300 import scenes
+    from nsvf_gb300.encoder import SparseVoxelEncoder
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.renderer import VolumeRenderer, render_rays
+    from nsvf_gb300.serving import SceneStore, Server, poisson_requests
+    t_setup = time.perf_counter()
+    store = SceneStore(dev, 64 << 30)
+    plain = {}
+    voxels = []
+    for sid, (p, vs) in enumerate(scenes.serving_scenes()):
+        args = argparse.Namespace(voxel_size=vs, max_hits=MAX_HITS, raymarching_stepsize_ratio=0.125,
+                                  voxel_embed_dim=32, use_octree=True, deterministic_step=True,
+                                  chunk_size=256)
+        enc = SparseVoxelEncoder(args, points=p)
+        with torch.no_grad():
+            enc.values.weight.copy_(scenes.voxel_embeddings(enc.values.weight.shape[0], 32, 0.01,
+                                                            seed=10 + sid))
+        field = StandInField(weights=scenes.stand_in_mlp_weights(seed=20 + sid))
+        enc, field = enc.to(dev).eval(), field.to(dev).eval()
+        store.add(sid, enc, field)
+        plain[sid] = (enc, field, VolumeRenderer(args).eval(), enc.precompute(id=None))
+        voxels.append(int(p.shape[0]))
+    server = Server(store, chunk_rays=65536, slots=3, max_inflight=8, frame_budget_bytes=1 << 30)
+    server.warm(list(store.scenes))
+    server.reserve_host_buffers(800 * 800, 8)
+    reqs = poisson_requests(n_requests, rate, list(store.scenes), [128, 256, 512, 800], seed=seed)
+    torch.cuda.synchronize(dev)
+    setup_s = time.perf_counter() - t_setup
+    t0 = time.perf_counter()
+    out = server.run(reqs, real_time=True)
+    wall = time.perf_counter() - t0
+    lat = np.array([r.latency() for r in out]) * 1e3
+    rays = sum(r.rays for r in out)
+    # plain FP32 drop-in path on a prefix of the same requests, one at a time
+    n_plain = min(len(reqs), 16)
+    t_plain = []
+    rays_plain = 0
+    for r in reqs[:n_plain]:
+        enc, field, ren, st = plain[r.scene_id]
+        rs, rd = scenes.pinhole_rays(r.cam, r.width, r.height, r.focal)
+        rs_t = torch.from_numpy(rs).to(dev).reshape(1, 1, 1, 3)
+        rd_t = torch.from_numpy(rd).to(dev).reshape(1, 1, -1, 3)
+        torch.cuda.synchronize(dev)
+        ts = time.perf_counter()
+        with torch.no_grad():
+            o = render_rays(enc, field, ren, rs_t, rd_t, encoder_states=st)
+        o["colors"].cpu()
+        t_plain.append(time.perf_counter() - ts)
+        rays_plain += r.rays
+    tp = np.array(t_plain) * 1e3
+    return {
+        "workload": "c5: 8 resident scenes (%d-%d voxels), Poisson %g req/s, resolutions "
+                    "{128,256,512,800}^2, %d requests" % (min(voxels), max(voxels), rate, n_requests),
+        "served_bf16": {"rays_per_s": round(rays / wall, 1), "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                        "p99_ms": round(float(np.percentile(lat, 99)), 2),
+                        "offered_rays_per_s": round(rays / reqs[-1].arrival, 1),
+                        "wall_s": round(wall, 3), "chunk_rays": 65536, "slots": 3,
+                        "cuda_graphs": True},
+        "plain_fp32_sequential": {"rays_per_s": round(rays_plain / tp.sum() * 1e3, 1),
+                                  "p50_ms": round(float(np.percentile(tp, 50)), 2),
+                                  "p99_ms": round(float(np.percentile(tp, 99)), 2),
+                                  "requests": n_plain,
+                                  "note": "render time per request, no queueing"},
+        "setup_s": round(setup_s, 1),
+    }
 
 
 # ------------------------------------------------------------- clocks ------
@@ -283,6 +410,8 @@ def run_ours(a):
                 "algorithmic_bytes_per_launch": alg, "avg_launch_ms": round(k["avg_ms"], 4),
                 "traffic": None}
     cpu = cpu_baseline(a.cpu_rays, threads=1)
+    serving = serve_bench(dev, a.serve_requests) if a.serve_requests > 0 and world == 1 else None
+    pruning = prune_bench(dev, sc) if world == 1 else None
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(statistics.mean(ms), 3),
@@ -302,6 +431,8 @@ def run_ours(a):
         "roofline": roof,
         "roofline_intersection": roof_isect,
         "cpu_baseline": cpu,
+        "serving": serving,
+        "pruning": pruning,
         "clocks": clk,
     }
     print(json.dumps(line))

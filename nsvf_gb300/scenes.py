@@ -79,7 +79,7 @@ def serving_scenes(seed=5):
     roughly 10k and 400k voxels."""
     rng = np.random.RandomState(seed)
     out = []
-    sizes = [1 / 24, 1 / 32, 1 / 48, 1 / 64, 1 / 80, 1 / 96, 1 / 112, 1 / 128]
+    sizes = [1 / 24, 1 / 32, 1 / 48, 1 / 64, 1 / 80, 1 / 96, 1 / 106, 1 / 116]
     for k, vs in enumerate(sizes):
         r = 0.35 + 0.25 * rng.rand()
         R, rt = 0.55 + 0.2 * rng.rand(), 0.1 + 0.1 * rng.rand()
