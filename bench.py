@@ -41,7 +41,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--path", default="plain", choices=["plain", "served"])
+    ap.add_argument("--path", default="served", choices=["plain", "served"],
+                    help="served: the fused BF16 path (the headline); plain: the drop-in FP32 path")
+    ap.add_argument("--plain-steps", type=int, default=3,
+                    help="frames of the plain FP32 path timed beside the served path")
     ap.add_argument("--cpu-rays", type=int, default=16384,
                     help="rays of the frame in the CPU baseline sample")
     ap.add_argument("--size", type=int, default=800,
@@ -176,6 +179,12 @@ def serve_bench(dev, n_requests, rate=200.0, seed=0):
     n_plain = min(len(reqs), 16)
     t_plain = []
     rays_plain = 0
+    for sid, (enc, field, ren, st) in plain.items():      # warm every scene's plain path once
+        rs, rd = scenes.pinhole_rays(scenes.sphere_cameras(1, 4.0, 99)[0], 64, 64, 80.0)
+        with torch.no_grad():
+            render_rays(enc, field, ren, torch.from_numpy(rs).to(dev).reshape(1, 1, 1, 3),
+                        torch.from_numpy(rd).to(dev).reshape(1, 1, -1, 3), encoder_states=st)
+    torch.cuda.synchronize(dev)
     for r in reqs[:n_plain]:
         enc, field, ren, st = plain[r.scene_id]
         rs, rd = scenes.pinhole_rays(r.cam, r.width, r.height, r.focal)
@@ -363,6 +372,26 @@ def run_ours(a):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_e2e = float(t.item())
 
+    # the plain FP32 drop-in path on the same cameras, for the BF16-vs-FP32 ratio
+    plain_fp32 = None
+    if a.path == "served" and a.plain_steps > 0:
+        def plain_step(rs, rd):
+            with torch.no_grad():
+                return render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3),
+                                   encoder_states=states)
+        plain_step(*dev_in[0])
+        pt = []
+        for i in range(min(a.plain_steps, a.steps)):
+            flush.zero_()
+            s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_.record()
+            plain_step(*dev_in[a.warmup + i])
+            e_.record()
+            torch.cuda.synchronize()
+            pt.append(s_.elapsed_time(e_))
+        plain_fp32 = {"value": round(a.size * a.size * len(pt) / (sum(pt) / 1e3), 1), "unit": "rays/s",
+                      "ms_per_step": round(sum(pt) / len(pt), 3), "steps": len(pt)}
+
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -430,6 +459,8 @@ def run_ours(a):
         "kernels_ms": kernel_ms,
         "roofline": roof,
         "roofline_intersection": roof_isect,
+        "plain_fp32": plain_fp32,
+        "speedup_vs_plain_fp32": (round(value / plain_fp32["value"], 2) if plain_fp32 else None),
         "cpu_baseline": cpu,
         "serving": serving,
         "pruning": pruning,

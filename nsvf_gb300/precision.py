@@ -1,0 +1,100 @@
+"""Precision study: images of the served (BF16 field) and drop-in (FP32)
+paths against a float64 render of the same samples.
+
+The float64 render is the validation oracle on the GPU (FP64 is used nowhere
+else). It takes the drop-in path's own geometry, which is FP32 and
+bit-identical to the reference's operation sequence: hit lists, sample
+depths, distances and voxel ids. It recomputes interpolation, the field MLP
+and compositing in float64 with torch:
+
+  emb = sum_k w_k values[feats[v, k]]     (fairnr/modules/encoder.py:584-590)
+  fe  = relu(sigma) * dist * 7            (fairnr/modules/renderer.py:117-121)
+  p_i = (1 - exp(-fe_i)) exp(-sum_{j<i} fe_j), colour = sum p c + missed * bg.
+
+`report()` gives the max and RMS RGB error and the max depth error (hit
+pixels) of each path against it.
+"""
+import torch
+
+from .renderer import render_rays
+from .served import SceneState, render_frame
+
+
+@torch.no_grad()
+def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
+    """Float64 colours [R, 3] and depths [R] of the rays (ray_start [3],
+    ray_dir [R, 3] on the encoder's device)."""
+    dev = ray_dir.device
+    R = ray_dir.shape[0]
+    st = encoder.precompute(id=None)
+    rs4 = ray_start.reshape(1, 1, 1, 3)
+    rd4 = ray_dir.reshape(1, 1, -1, 3)
+    _, _, inter, hits = encoder.ray_intersect(rs4, rd4, {k: (v.unsqueeze(0) if v is not None else None)
+                                                         for k, v in st.items()})
+    d = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
+    inter['probs'] = d / d.sum(-1, keepdim=True)
+    inter['steps'] = d.sum(-1) / encoder.step_size
+    hits = hits.reshape(-1)
+    pix = hits.nonzero().squeeze(1)
+    sub = {k: v.reshape(-1, v.shape[-1])[pix] for k, v in inter.items() if k != 'steps'}
+    sub['steps'] = inter['steps'].reshape(-1)[pix]
+    samples = encoder.ray_sample(sub)
+    centers = st['voxel_center_xyz'].double()
+    feats = st['voxel_vertex_idx']
+    values = st['voxel_vertex_emb'].double()
+    W = [(l.weight.double(), l.bias.double()) for l in field.layers]
+    bg = field.bg_color.bg_color.double()
+    colors = bg.expand(R, 3).clone()
+    depths = torch.full((R,), float(field.bg_color.depth), dtype=torch.float64, device=dev)
+    vs = float(encoder.voxel_size)
+    cc = torch.tensor([-1.0, 1.0], dtype=torch.float64, device=dev)
+    ox, oy, oz = torch.meshgrid([cc, cc, cc], indexing="ij")
+    q = (torch.stack([ox.reshape(-1), oy.reshape(-1), oz.reshape(-1)], 1) * .5 + .5)[None]
+    o64 = ray_start.double().reshape(1, 1, 3)
+    for a in range(0, pix.numel(), chunk):
+        b = min(pix.numel(), a + chunk)
+        vid = samples['sampled_point_voxel_idx'][a:b].long()
+        t = samples['sampled_point_depth'][a:b].double()
+        dist = samples['sampled_point_distance'][a:b].double()
+        mask = vid.ne(-1)
+        rd = ray_dir[pix[a:b]].double()
+        xyz = o64 + rd[:, None, :] * t[..., None]
+        v = vid[mask]
+        p = ((xyz[mask] - centers[v]) / vs + .5)[:, None, :]
+        w = (p * q + (1 - p) * (1 - q)).prod(-1)
+        emb = (w[..., None] * values[feats[v]]).sum(1)
+        x = emb
+        for li, (Wl, bl) in enumerate(W):
+            x = x @ Wl.t() + bl
+            if li < len(W) - 1:
+                x = torch.relu(x)
+        sig = torch.zeros(mask.shape, dtype=torch.float64, device=dev)
+        rgb = torch.zeros(mask.shape + (3,), dtype=torch.float64, device=dev)
+        sig[mask] = x[:, 0]
+        rgb[mask] = x[:, 1:4]
+        fe = torch.relu(sig) * dist * 7.0 * mask
+        sh = torch.cat([fe.new_zeros(fe.shape[0], 1), fe[:, :-1]], 1)
+        pr = (1 - torch.exp(-fe)) * torch.exp(-torch.cumsum(sh, 1))
+        missed = 1 - pr.sum(-1)
+        colors[pix[a:b]] = (rgb * pr[..., None]).sum(1) + missed[:, None] * bg
+        depths[pix[a:b]] = (t.masked_fill(~mask, 0) * pr).sum(-1) + missed * float(field.bg_color.depth)
+    return colors, depths, hits
+
+
+def report(encoder, field, renderer, ray_start, ray_dir):
+    """Errors of the served BF16 and the drop-in FP32 frame against float64."""
+    ref_c, ref_d, hits = fp64_render(encoder, field, ray_start, ray_dir)
+    scene = SceneState(encoder, field)
+    served = render_frame(scene, ray_start, ray_dir)
+    with torch.no_grad():
+        plain = render_rays(encoder, field, renderer, ray_start.reshape(1, 1, 1, 3),
+                            ray_dir.reshape(1, 1, -1, 3))
+    out = {}
+    for name, c, d in [("served_bf16", served["colors"], served["depths"]),
+                       ("plain_fp32", plain["colors"].reshape(-1, 3), plain["depths"].reshape(-1))]:
+        e = (c.double() - ref_c).abs()
+        de = (d.double() - ref_d).abs()[hits]
+        out[name] = {"max_rgb_err": float(e.max()), "rms_rgb_err": float(e.pow(2).mean().sqrt()),
+                     "max_depth_err_hit_pixels": float(de.max()) if de.numel() else 0.0}
+    out["hit_pixels"] = int(hits.sum())
+    return out
