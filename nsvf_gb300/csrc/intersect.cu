@@ -204,8 +204,13 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     const float *__restrict__ ray_dir, const float4 *__restrict__ box_all,
     const int4 *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
     float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
-  __shared__ int s_node[kSvoLevels * kRaysPerBlock];
+  // Per ray and level of the descent: the expanded node's 8 child ids (lane
+  // j writes child j), and the masks of its hit children not visited yet and
+  // of those that are leaves. Picking the next child is then shared-memory
+  // work only.
+  __shared__ int s_child[kSvoLevels * kRaysPerBlock * 8];
   __shared__ uint8_t s_mask[kSvoLevels * kRaysPerBlock];
+  __shared__ uint8_t s_leaf[kSvoLevels * kRaysPerBlock];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = lane >> 3, j = lane & 7;           // ray slot in the warp, child slot
   const uint32_t gshift = 8u * grp;
@@ -265,23 +270,28 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
         }
         cnt = min(n_max, cnt + __popc(hm));
         hm = 0;                           // nothing to descend into
-      } else if (j == 0) {
-        s_node[level * kRaysPerBlock + slot] = k;
-        s_mask[level * kRaysPerBlock + slot] = (uint8_t)hm;
+      } else {
+        const int base = level * kRaysPerBlock + slot;
+        s_child[base * 8 + j] = cid;
+        if (j == 0) { s_mask[base] = (uint8_t)hm; s_leaf[base] = (uint8_t)lm; }
       }
       if (hm == 0) --level;               // this node is finished (or its leaves emitted)
+    }
+    __syncwarp();                         // all 32 lanes: s_child writes -> lane 0's reads
+    if (expand) {
       // find the next internal node to expand (lane 0 of the group walks the
-      // level stack; a leaf met on the way -- mixed children -- is emitted)
+      // level stack in shared memory; a leaf met on the way -- mixed children
+      // -- is emitted with its interval recomputed from its box)
       if (j == 0) {
         while (level >= 0 && cnt < n_max) {
-          uint32_t m2 = s_mask[level * kRaysPerBlock + slot];
+          const int base = level * kRaysPerBlock + slot;
+          uint32_t m2 = s_mask[base];
           if (m2 == 0) { --level; continue; }
           int u = 31 - __clz(m2);
-          s_mask[level * kRaysPerBlock + slot] = (uint8_t)(m2 & ~(1u << u));
-          int parent = s_node[level * kRaysPerBlock + slot];
-          int ch = reinterpret_cast<const int *>(c.kids + (int64_t)parent * 2)[u];
-          float4 cb = c.box[ch];
-          if (cb.w < 0.0f) {
+          s_mask[base] = (uint8_t)(m2 & ~(1u << u));
+          int ch = s_child[base * 8 + u];
+          if ((s_leaf[base] >> u) & 1u) {
+            float4 cb = c.box[ch];
             float a, b2;
             nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, cb.x, cb.y, cb.z, -cb.w, a, b2);
             I[cnt] = ch; LO[cnt] = a; HI[cnt] = b2;
