@@ -84,16 +84,25 @@ def frame_rays(index, size=800):
     return rs, rd
 
 
+PRUNE_SIGMA_SCALE = 3.6e5
+
+
 def prune_bench(dev, sc, bits=8, th=0.5):
     """The c2 pruning pass: sigma at bits^3 points per voxel, keep voxels with
     max(1 - exp(-relu(sigma) * step)) >= th. Fused BF16 tensor-core kernel
     (nsvf_prune_scores_bf16) vs the FP32 path (offset_points, the FP32
     interpolation kernel, the field's FP32 MLP), with the masks compared."""
     import torch
-    from nsvf_gb300 import geometry
+    from nsvf_gb300 import geometry, scenes
+    from nsvf_gb300.field import StandInField
     from nsvf_gb300.functional import trilinear_embed
     from nsvf_gb300.mlp import TensorCoreMLP
-    enc, field, states = sc["enc"], sc["field"], sc["states"]
+    enc, states = sc["enc"], sc["states"]
+    # The frame's field is nearly transparent at this step (every alpha far
+    # below 0.5, so every voxel would be dropped); the pruning pass uses the
+    # same MLP with its density row scaled so that about half of the c2
+    # voxels reach the threshold.
+    field = StandInField(weights=scenes.stand_in_mlp_weights(seed=2, sigma_scale=PRUNE_SIGMA_SCALE)).to(dev).eval()
     centers = states["voxel_center_xyz"].float().contiguous()
     feats = states["voxel_vertex_idx"].int().contiguous()
     values = states["voxel_vertex_emb"].detach().float().contiguous()
@@ -124,8 +133,9 @@ def prune_bench(dev, sc, bits=8, th=0.5):
     e1.record()
     torch.cuda.synchronize(dev)
     keep_fp32 = alpha >= th
-    return {"workload": "c2 pruning pass: %d voxels x %d^3 points, keep max(1-exp(-relu(s)*step)) >= %g"
-                        % (V, bits, th),
+    return {"workload": "c2 pruning pass: %d voxels x %d^3 points, keep max(1-exp(-relu(s)*step)) >= %g; "
+                        "density row of the field scaled by %g" % (V, bits, th, PRUNE_SIGMA_SCALE),
+            "alpha_fp32_median": float(alpha.median()),
             "bf16_fused_ms": round(s0.elapsed_time(e0), 3), "fp32_ms": round(s1.elapsed_time(e1), 3),
             "tflop": round(107520.0 * V * bits ** 3 / 1e12, 2),
             "bf16_tflops_achieved": round(107520.0 * V * bits ** 3 / (s0.elapsed_time(e0) / 1e3) / 1e12, 1),

@@ -80,14 +80,14 @@ int nsvf_svo_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_ma
  * engine that pre-partitions GPU memory and passes only its own input and
  * output buffers): instead of a caller-provided workspace it uses a scratch
  * array inside this library, fixed at NSVF_NOALLOC_MAX_NODES octree nodes
- * (b_pts * n, 48 bytes each: 24 MiB, held by every GPU that loads the library
- * until the process exits). Larger octrees are rejected with
+ * (b_pts * n, 176 bytes each: 44 MiB, held by every GPU that loads the
+ * library until the process exits). Larger octrees are rejected with
  * NSVF_ERR_CAPACITY. It allocates nothing: the first call on a device looks
  * the array's device address up (cudaGetSymbolAddress, once per device), so
  * make that first call before any stream capture. All calls share the one
  * array: calls that overlap on the GPU (other streams, other threads) race
  * and must be serialised by the caller. */
-#define NSVF_NOALLOC_MAX_NODES (1 << 19)
+#define NSVF_NOALLOC_MAX_NODES (1 << 18)
 int nsvf_svo_intersect_noalloc(int b, int b_pts, int n, int m, float voxelsize, int n_max,
                                const float *ray_start, const float *ray_dir, const float *points,
                                const int32_t *children, int32_t *idx, float *min_depth,

@@ -7,7 +7,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libnsvf_gb300.so")
+# NSVF_GB300_LIB names a library built elsewhere (same sources, another
+# output directory); by default the in-tree build is loaded.
+LIB_PATH = os.environ.get("NSVF_GB300_LIB") or os.path.join(HERE, "_build", "libnsvf_gb300.so")
 
 NSVF_OK = 0
 

@@ -66,25 +66,37 @@ __global__ void __launch_bounds__(kRayBlock) aabb_kernel(
 
 // ----------------------------------------------------------------- SVO ----
 
-// Packed octree node: box = (cx, cy, cz, +-half) with a negative half marking
-// a leaf (children[8] == 1), kids = the 8 child ids.
-struct PackedTree {
-  float4 *box;   // [b_pts * n]
-  int4 *kids;    // [b_pts * n * 2]
-};
-
-__global__ void pack_octree_kernel(int64_t total, float hv, const float *__restrict__ points,
-                                   const int32_t *__restrict__ children, float4 *__restrict__ box,
-                                   int4 *__restrict__ kids) {
-  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= total) return;
-  const int32_t *c = children + k * 9;
-  int size = c[8];
+// Packed octree, per point set of n nodes: for node k, its 8 children side
+// by side -- ids kids[8k + j] and boxes cbox[8k + j] -- and the root's own
+// box at cbox[8n]. A box is (cx, cy, cz, +half) for an internal node and
+// (cx, cy, cz, -half) for a leaf (children[8] == 1); absent children get a
+// zero box. Expanding a node is then two independent loads per lane, and a
+// node's whole child set lies in two 128-byte lines.
+__device__ __forceinline__ float4 node_box(const float *__restrict__ P,
+                                           const int32_t *__restrict__ C, int k, float hv) {
+  int size = C[(int64_t)k * 9 + 8];
   float h = __fmul_rn(hv, (float)size);
-  box[k] = make_float4(points[k * 3 + 0], points[k * 3 + 1], points[k * 3 + 2],
-                       size == 1 ? -h : h);
-  kids[k * 2 + 0] = make_int4(c[0], c[1], c[2], c[3]);
-  kids[k * 2 + 1] = make_int4(c[4], c[5], c[6], c[7]);
+  return make_float4(P[(int64_t)k * 3 + 0], P[(int64_t)k * 3 + 1], P[(int64_t)k * 3 + 2],
+                     size == 1 ? -h : h);
+}
+
+__global__ void pack_octree_kernel(int64_t total, int n, float hv, const float *__restrict__ points,
+                                   const int32_t *__restrict__ children, float4 *__restrict__ cbox,
+                                   int32_t *__restrict__ kids) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;   // (point set, node, child)
+  if (t >= total * 8) return;
+  const int j = (int)(t & 7);
+  const int64_t gk = t >> 3, g = gk / n;
+  const int k = (int)(gk - g * n);
+  const int32_t *C = children + g * (int64_t)n * 9;
+  const float *P = points + g * (int64_t)n * 3;
+  float4 *B = cbox + g * ((int64_t)n * 8 + 1);
+  int cid = C[(int64_t)k * 9 + j];
+  float4 cb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (cid > -1 && cid < n) cb = node_box(P, C, cid, hv);
+  B[(int64_t)k * 8 + j] = cb;
+  kids[t] = cid;
+  if (k == n - 1 && j == 0) B[(int64_t)n * 8] = node_box(P, C, n - 1, hv);
 }
 
 constexpr int kSvoLevels = 16;
@@ -95,44 +107,20 @@ constexpr int kRaysPerBlock = kRayBlock / 8;          // 16
 // (children 7..0 of every hit node, fairnr/clib/src/intersect_gpu.cu:200-235).
 //
 // A warp walks 4 rays; the 8 lanes of a ray's group each own one child slot.
-// Expanding a node = each lane loads its child id and box and runs the slab
-// test; a ballot gives the node's 8-bit mask of hit children. The descent
-// keeps, per level, (node id, mask of hit children not yet visited) in shared
-// memory; the group's lane 0 picks the next child (highest index first).
+// Expanding a node = lane j loads child j's id and box and runs the slab
+// test; ballots give the node's 8-bit masks of hit children and hit leaves.
+// The descent stack is spread over the group: lane j keeps, for levels j and
+// j + 8, the mask of hit children not visited yet (and which of them are
+// leaves); the child ids of each level sit in shared memory. The next node
+// to expand -- the highest unvisited child of the deepest non-empty level --
+// comes from two ballots and a shuffle, the same on all 8 lanes.
 // When every hit child of a node is a leaf -- always the case for trees made
 // by build_octree, whose leaves all sit under depth-0 nodes -- the DFS visits
 // them consecutively, so the group emits them at once, lane j writing at
-// cnt + (number of hit leaves with a higher index). Mixed children fall back
-// to visiting leaves one at a time. The emitted order, the n_max cutoff and
-// every (lo, hi) are the reference's. Hits go straight into the output row.
-struct GroupCtx {
-  const float4 *box;
-  const int4 *kids;
-  int n, n_max;
-  float ox, oy, oz, ix, iy, iz;
-};
-
-// Each lane of the group tests child `j` of node k. Returns the group's
-// 8-bit masks of hit children and of hit leaves; this lane's (lo, hi, id).
-__device__ __forceinline__ void expand_node(const GroupCtx &c, int k, int j, uint32_t gshift,
-                                            uint32_t &hitmask, uint32_t &leafmask, float &lo,
-                                            float &hi, int &cid, bool &bad) {
-  cid = reinterpret_cast<const int *>(c.kids + (int64_t)k * 2)[j];
-  bool hit = false, leaf = false;
-  if (cid > -1) {
-    if (cid >= c.n) {
-      bad = true;
-    } else {
-      float4 b = c.box[cid];
-      hit = nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, b.x, b.y, b.z, fabsf(b.w), lo, hi);
-      leaf = b.w < 0.0f;
-    }
-  }
-  uint32_t hb = __ballot_sync(0xffffffffu, hit);
-  uint32_t lb = __ballot_sync(0xffffffffu, hit && leaf);
-  hitmask = (hb >> gshift) & 0xffu;
-  leafmask = (lb >> gshift) & 0xffu;
-}
+// cnt + (number of hit leaves with a higher index). A leaf met on the stack
+// (a node with both leaf and internal children) is emitted on its own. The
+// emitted order, the n_max cutoff and every (lo, hi) are the reference's.
+// Hits go straight into the output row.
 
 // Warp-cooperative stable sort of one row of n_max <= 32*E slots by
 // (min_depth, slot); slots >= cnt are the misses (id -1, depth 10000), the
@@ -201,18 +189,17 @@ __device__ __forceinline__ void warp_sort_row(int32_t *__restrict__ I, float *__
 template <bool SORTED>
 __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int64_t rays, int m, int b_pts, int n, int n_max, const float *__restrict__ ray_start,
-    const float *__restrict__ ray_dir, const float4 *__restrict__ box_all,
-    const int4 *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
+    const float *__restrict__ ray_dir, const float4 *__restrict__ cbox_all,
+    const int32_t *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
     float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
-  // Per ray and level of the descent: the expanded node's 8 child ids (lane
-  // j writes child j), and the masks of its hit children not visited yet and
-  // of those that are leaves. Picking the next child is then shared-memory
-  // work only.
+  // per ray and stack level: the expanded node's 8 child ids (lane j writes
+  // child j) and the node's id
   __shared__ int s_child[kSvoLevels * kRaysPerBlock * 8];
-  __shared__ uint8_t s_mask[kSvoLevels * kRaysPerBlock];
-  __shared__ uint8_t s_leaf[kSvoLevels * kRaysPerBlock];
+  __shared__ int s_node[kSvoLevels * kRaysPerBlock];
+  const uint32_t full = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = lane >> 3, j = lane & 7;           // ray slot in the warp, child slot
+  const int g0 = lane & ~7;                          // the group's first lane
   const uint32_t gshift = 8u * grp;
   const int slot = warp * kRaysPerWarp + grp;        // ray slot in the block
   const int64_t r = (int64_t)blockIdx.x * kRaysPerBlock + slot;
@@ -220,25 +207,22 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   bool bad = false;
   int cnt = 0;
 
-  GroupCtx c;
-  c.n = n;
-  c.n_max = n_max;
   const int64_t rr = live ? r : 0;
   const int64_t g = (b_pts == 1) ? 0 : rr / m;
-  c.box = box_all + g * n;
-  c.kids = kids_all + g * n * 2;
-  c.ox = ray_start[rr * 3 + 0]; c.oy = ray_start[rr * 3 + 1]; c.oz = ray_start[rr * 3 + 2];
-  c.ix = nsvf_rcp(ray_dir[rr * 3 + 0]); c.iy = nsvf_rcp(ray_dir[rr * 3 + 1]);
-  c.iz = nsvf_rcp(ray_dir[rr * 3 + 2]);
+  const float4 *CB = cbox_all + g * ((int64_t)n * 8 + 1);
+  const int32_t *KD = kids_all + g * (int64_t)n * 8;
+  const float ox = ray_start[rr * 3 + 0], oy = ray_start[rr * 3 + 1], oz = ray_start[rr * 3 + 2];
+  const float ix = nsvf_rcp(ray_dir[rr * 3 + 0]), iy = nsvf_rcp(ray_dir[rr * 3 + 1]),
+              iz = nsvf_rcp(ray_dir[rr * 3 + 2]);
   int32_t *I = idx + rr * n_max;
   float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
 
   // root
   int level = -1;
   {
-    float4 rb = c.box[n - 1];
+    float4 rb = CB[(int64_t)n * 8];
     float lo, hi;
-    bool rh = live && nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi);
+    bool rh = live && nsvf_slab(ox, oy, oz, ix, iy, iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi);
     if (rh && rb.w < 0.0f) {            // a single-leaf octree
       if (j == 0) { I[0] = n - 1; LO[0] = lo; HI[0] = hi; }
       cnt = 1;
@@ -246,74 +230,110 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
       level = 0;
     }
   }
+  // lane j's share of the stack: bits [0, 8) level j, bits [8, 16) level j + 8
+  uint32_t stk = 0, stl = 0;            // unvisited hit children; those that are leaves
   int node = n - 1;                      // the node to expand next (valid when `expand`)
   bool expand = level == 0;
   int64_t steps = 0;
   // Every group runs the loop until all groups of the warp are done. All
-  // warp-wide operations (ballots in expand_node, the shuffles that
-  // broadcast lane 0's stack walk) are executed by all 32 lanes every
-  // iteration; only lane-local work is predicated on `expand`.
-  while (__any_sync(0xffffffffu, expand)) {
-    uint32_t hm = 0, lm = 0;
-    float lo = 0.f, hi = 0.f;
+  // warp-wide operations run on all 32 lanes every iteration; only
+  // lane-local work is predicated on `expand` / `pick`. Every value the
+  // group steers by (level, cnt, node, top, t, u) is the same on its 8 lanes.
+  while (__any_sync(full, expand)) {
+    // 1. expand `node`: lane j tests child j
+    bool hit = false;
+    float lo = 0.0f, hi = 0.0f, bw = 0.0f;
     int cid = -1;
-    int k = expand ? node : 0;
-    expand_node(c, k, j, gshift, hm, lm, lo, hi, cid, bad);
+    if (expand) {
+      const int64_t kb = (int64_t)node * 8 + j;
+      cid = KD[kb];
+      if (cid > -1) {
+        if (cid >= n) {
+          bad = true;
+        } else {
+          float4 b = CB[kb];
+          bw = b.w;
+          hit = nsvf_slab(ox, oy, oz, ix, iy, iz, b.x, b.y, b.z, fabsf(b.w), lo, hi);
+        }
+      }
+    }
+    const uint32_t hm = (__ballot_sync(full, hit) >> gshift) & 0xffu;
+    const uint32_t lm = (__ballot_sync(full, hit && bw < 0.0f) >> gshift) & 0xffu;
     if (expand && ++steps > 8 * (int64_t)n) { bad = true; expand = false; }
-    int next = -1;
+    int top = level - 1;                  // deepest stack level that may hold children
     if (expand) {
       if (hm != 0 && hm == lm) {
         // all hit children are leaves: emit them now, highest index first
         int before = __popc(hm >> (j + 1));
-        if (((hm >> j) & 1u) && cnt + before < n_max) {
+        if (hit && cnt + before < n_max) {
           I[cnt + before] = cid; LO[cnt + before] = lo; HI[cnt + before] = hi;
         }
         cnt = min(n_max, cnt + __popc(hm));
-        hm = 0;                           // nothing to descend into
-      } else {
+      } else if (hm != 0) {
         const int base = level * kRaysPerBlock + slot;
         s_child[base * 8 + j] = cid;
-        if (j == 0) { s_mask[base] = (uint8_t)hm; s_leaf[base] = (uint8_t)lm; }
+        if (j == 0) s_node[base] = node;
+        if (j == (level & 7)) {
+          const int sh = (level >> 3) * 8;
+          stk = (stk & ~(0xffu << sh)) | (hm << sh);
+          stl = (stl & ~(0xffu << sh)) | (lm << sh);
+        }
+        top = level;
       }
-      if (hm == 0) --level;               // this node is finished (or its leaves emitted)
     }
-    __syncwarp();                         // all 32 lanes: s_child writes -> lane 0's reads
-    if (expand) {
-      // find the next internal node to expand (lane 0 of the group walks the
-      // level stack in shared memory; a leaf met on the way -- mixed children
-      // -- is emitted with its interval recomputed from its box)
-      if (j == 0) {
-        while (level >= 0 && cnt < n_max) {
-          const int base = level * kRaysPerBlock + slot;
-          uint32_t m2 = s_mask[base];
-          if (m2 == 0) { --level; continue; }
-          int u = 31 - __clz(m2);
-          s_mask[base] = (uint8_t)(m2 & ~(1u << u));
-          int ch = s_child[base * 8 + u];
-          if ((s_leaf[base] >> u) & 1u) {
-            float4 cb = c.box[ch];
-            float a, b2;
-            nsvf_slab(c.ox, c.oy, c.oz, c.ix, c.iy, c.iz, cb.x, cb.y, cb.z, -cb.w, a, b2);
-            I[cnt] = ch; LO[cnt] = a; HI[cnt] = b2;
+    __syncwarp();                         // s_child / s_node writes -> the group's reads
+    // 2. the next node to expand: the highest unvisited child of the deepest
+    // non-empty level <= top. A leaf found there is emitted and the pick
+    // repeats.
+    bool pick = expand && cnt < n_max;
+    int next = -1;
+    while (__any_sync(full, pick)) {
+      const uint32_t nz0 = __ballot_sync(full, pick && j <= top && (stk & 0xffu) != 0);
+      const uint32_t nz1 = __ballot_sync(full, pick && j + 8 <= top && (stk >> 8) != 0);
+      const uint32_t L = ((nz0 >> gshift) & 0xffu) | (((nz1 >> gshift) & 0xffu) << 8);
+      const int t = (pick && L != 0) ? 31 - __clz(L) : -1;
+      uint32_t mine = 0, isleaf = 0;
+      int u = 0;
+      if (t >= 0 && j == (t & 7)) {
+        const int sh = (t >> 3) * 8;
+        mine = (stk >> sh) & 0xffu;
+        u = 31 - __clz(mine);
+        isleaf = (stl >> (sh + u)) & 1u;
+        stk &= ~(1u << (sh + u));
+      }
+      const int src = g0 + (t >= 0 ? (t & 7) : 0);
+      u = __shfl_sync(full, u, src);
+      isleaf = __shfl_sync(full, isleaf, src);
+      if (pick) {
+        if (t < 0) {
+          pick = false;                   // the stack is empty: the ray is done
+        } else {
+          const int base = t * kRaysPerBlock + slot;
+          const int ch = s_child[base * 8 + u];
+          top = t;
+          if (isleaf) {
+            if (j == 0) {
+              float4 cb = CB[(int64_t)s_node[base] * 8 + u];
+              float a, b2;
+              nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, -cb.w, a, b2);
+              I[cnt] = ch; LO[cnt] = a; HI[cnt] = b2;
+            }
             ++cnt;
-            continue;
+            if (cnt >= n_max) pick = false;
+          } else if (t + 1 >= kSvoLevels) {
+            bad = true;
+            pick = false;
+          } else {
+            next = ch;
+            level = t + 1;
+            pick = false;
           }
-          if (level + 1 >= kSvoLevels) { bad = true; level = -1; break; }
-          next = ch;
-          break;
         }
       }
     }
-    next = __shfl_sync(0xffffffffu, next, lane & ~7);
-    cnt = __shfl_sync(0xffffffffu, cnt, lane & ~7);
-    level = __shfl_sync(0xffffffffu, level, lane & ~7);
     if (expand) {
-      if (next >= 0 && cnt < n_max) {
-        ++level;
-        node = next;
-      } else {
-        expand = false;
-      }
+      if (next >= 0) node = next;
+      else expand = false;
     }
   }
   if (live && SORTED && j == 0) hits[r] = cnt > 0;
@@ -415,8 +435,11 @@ int nsvf_aabb_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_m
   return nsvf_launch_status();
 }
 
+// Packed octree per point set: (8n + 1) boxes of 16 bytes, then (for all
+// sets) 8n child ids of 4 bytes.
 int64_t nsvf_svo_workspace_bytes(int b_pts, int n) {
-  return (int64_t)b_pts * n * (int64_t)(sizeof(float4) + 2 * sizeof(int4));
+  return (int64_t)b_pts * (((int64_t)n * 8 + 1) * (int64_t)sizeof(float4) +
+                           (int64_t)n * 8 * (int64_t)sizeof(int32_t));
 }
 
 static int svo_launch(bool sorted, int b, int b_pts, int n, int m, float voxelsize, int n_max,
@@ -431,20 +454,21 @@ static int svo_launch(bool sorted, int b, int b_pts, int n, int m, float voxelsi
   if (((uintptr_t)workspace) & 15) return NSVF_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   int64_t total = (int64_t)b_pts * n;
-  float4 *box = (float4 *)workspace;
-  int4 *kids = (int4 *)(box + total);
+  float4 *cbox = (float4 *)workspace;
+  int32_t *kids = (int32_t *)(cbox + (int64_t)b_pts * ((int64_t)n * 8 + 1));
   float hv = voxelsize * 0.5f;
-  pack_octree_kernel<<<nsvf_grid(total, 256), 256, 0, s>>>(total, hv, points, children, box, kids);
+  pack_octree_kernel<<<nsvf_grid(total * 8, 256), 256, 0, s>>>(total, n, hv, points, children,
+                                                               cbox, kids);
   nsvf_count_launch();
   int64_t rays = (int64_t)b * m;
   if (rays == 0) return nsvf_launch_status();
   if (sorted)
     svo_kernel<true><<<nsvf_grid(rays, kRaysPerBlock), kRayBlock, 0, s>>>(
-        rays, m, b_pts, n, n_max, ray_start, ray_dir, box, kids, idx, min_depth, max_depth, hits,
+        rays, m, b_pts, n, n_max, ray_start, ray_dir, cbox, kids, idx, min_depth, max_depth, hits,
         err);
   else
     svo_kernel<false><<<nsvf_grid(rays, kRaysPerBlock), kRayBlock, 0, s>>>(
-        rays, m, b_pts, n, n_max, ray_start, ray_dir, box, kids, idx, min_depth, max_depth, hits,
+        rays, m, b_pts, n, n_max, ray_start, ray_dir, cbox, kids, idx, min_depth, max_depth, hits,
         err);
   return nsvf_launch_status();
 }
@@ -475,11 +499,12 @@ int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, i
 // about to be captured into a CUDA graph -- the packed-octree scratch that
 // nsvf_svo_intersect takes as `workspace` lives here in a file-scope device
 // array instead. Its size is fixed: NSVF_NOALLOC_MAX_NODES nodes (b_pts * n)
-// at 48 bytes each, 24 MiB, which every GPU that loads this library holds
-// until the process exits. Host code only sees a stand-in for the array's
+// at 176 bytes each (160 for the packed node, 16 for a point set's root box
+// in the worst case of one node per set), 44 MiB, which every GPU that loads
+// this library holds until the process exits. Host code only sees a stand-in for the array's
 // name, never its device address, so the address is looked up once per
 // device with cudaGetSymbolAddress (with that device current) and cached.
-static __device__ __align__(256) unsigned char g_svo_noalloc_scratch[(size_t)NSVF_NOALLOC_MAX_NODES * 48];
+static __device__ __align__(256) unsigned char g_svo_noalloc_scratch[(size_t)NSVF_NOALLOC_MAX_NODES * 176];
 
 static void *noalloc_scratch_for_current_device(int *status) {
   static std::mutex mu;

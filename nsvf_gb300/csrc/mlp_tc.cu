@@ -8,10 +8,12 @@
 // memory (108 KB) and streams 128-sample tiles through them: the hidden
 // activations never leave the SM.
 //
-// CTA = 9 warps. Warps 0-3 and 4-7 are two epilogue warpgroups, each owning
+// CTA = 17 warps. Warps 0-3 and 4-7 are two epilogue warpgroups, each owning
 // one tile slot (TMEM columns [256*g, 256*g + 144)) so that one slot's
 // epilogue overlaps the other slot's MMAs. Warp 8 allocates TMEM and one of
-// its lanes issues the tcgen05.mma instructions. Per layer:
+// its lanes issues the tcgen05.mma instructions. Warps 9-16 are two loader
+// warpgroups that build the input tiles (embedding gathers and trilinear
+// interpolation) into a ring of shared-memory buffers. Per layer:
 //   epilogue g writes A (bf16, K-major) to smem -> fence.proxy.async ->
 //   arrives on act_ready[g] -> MMA thread issues the K/16 MMAs ->
 //   tcgen05.commit arrives on mma_done[g] -> epilogue g reads D with
@@ -41,6 +43,11 @@ struct __align__(128) MlpSmem {
   __nv_bfloat16 w4[NOUT * HID];
   __nv_bfloat16 ain[NB][TILE * E];
   __nv_bfloat16 ah[2][TILE * HID];
+  // per loader warp: its 32 rows' corner keys (kSkipKey = skip) and
+  // trilinear weights, written by the row's lane and read by the 8 lanes
+  // that gather the row
+  int meta_key[8][32 * 8];
+  float meta_w[8][32 * 8];
   float bias[4][HID];
   float bias4[NOUT];
   uint64_t mma_done[2][5];   // per slot and layer: one phase per tile
@@ -91,34 +98,6 @@ __device__ __forceinline__ float corner_weight(const float q[3], int k) {
 }
 
 // emb[32] of a point x in voxel v (ids checked; out-of-range reads skipped).
-__device__ __forceinline__ void interp_point(const MlpParams &p, int64_t v, float x, float y,
-                                             float z, float (&e)[32], bool &bad) {
-#pragma unroll
-  for (int i = 0; i < 32; ++i) e[i] = 0.0f;
-  if (v < 0 || v >= p.n_vox) { bad = true; return; }
-  const float *c = p.centers + v * 3;
-  float q[3] = {(x - c[0]) / p.voxel_size + 0.5f, (y - c[1]) / p.voxel_size + 0.5f,
-                (z - c[2]) / p.voxel_size + 0.5f};
-  const int4 f0 = reinterpret_cast<const int4 *>(p.feats)[v * 2];
-  const int4 f1 = reinterpret_cast<const int4 *>(p.feats)[v * 2 + 1];
-  const int keys[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    int64_t key = keys[k];
-    if (key < 0 || key >= p.n_keys) { bad = true; continue; }
-    float w = corner_weight(q, k);
-    const float4 *src = p.values + key * 8;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      float4 val = __ldg(src + j);
-      e[4 * j + 0] = fmaf(w, val.x, e[4 * j + 0]);
-      e[4 * j + 1] = fmaf(w, val.y, e[4 * j + 1]);
-      e[4 * j + 2] = fmaf(w, val.z, e[4 * j + 2]);
-      e[4 * j + 3] = fmaf(w, val.w, e[4 * j + 3]);
-    }
-  }
-}
-
 // Copy a row-major [rows, K] bf16 matrix into the K-major core-matrix layout
 // (rows >= valid_rows are zero).
 __device__ void stage_weights(__nv_bfloat16 *dst, const __nv_bfloat16 *src, int rows,
@@ -151,39 +130,142 @@ __device__ __forceinline__ uint32_t pack_relu_bf16x2(float lo, float hi) {
   return d;
 }
 
-// The input row `r` of a tile (embedding, interpolated sample or pruning
-// point) as 32 FP32 values; rows >= ns are zero.
+constexpr int kSkipKey = -1;
+
+// Input stage, pass 1 (lane = row r): the row's voxel, its 8 corner keys and
+// trilinear weights (interpolated sample or pruning point). Rows >= ns and
+// invalid voxels / corner ids get kSkipKey (they contribute nothing; invalid
+// ids set `bad`). The weights are the interpolation kernel's, same
+// operations in the same order.
+// A sample row's voxel id and position, loaded one tile ahead of its use.
+struct SampleRow {
+  int32_t vox;
+  float4 xyz;
+};
+
 template <int MODE>
-__device__ __forceinline__ void input_row(const MlpParams &p, int64_t r, int64_t ns, float (&e)[32],
-                                          bool &bad) {
-  if (r >= ns) {
-#pragma unroll
-    for (int j = 0; j < 32; ++j) e[j] = 0.0f;
-    return;
+__device__ __forceinline__ SampleRow load_sample(const MlpParams &p, int64_t r, int64_t ns) {
+  SampleRow s;
+  s.vox = -1;
+  s.xyz = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (MODE == kSamplesIn && r < ns) {
+    s.vox = p.vox[r];
+    s.xyz = p.xyzd[r];
   }
-  if (MODE == kEmbIn) {
-    const float4 *src = reinterpret_cast<const float4 *>(p.emb + r * E);
+  return s;
+}
+
+template <int MODE>
+__device__ __forceinline__ void row_meta(const MlpParams &p, int64_t r, int64_t ns,
+                                         const SampleRow &smp, int *__restrict__ key,
+                                         float *__restrict__ w, bool &bad) {
+  int k8[8];
+  float w8[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      float4 x = __ldg(src + j);
-      e[4 * j] = x.x; e[4 * j + 1] = x.y; e[4 * j + 2] = x.z; e[4 * j + 3] = x.w;
+  for (int k = 0; k < 8; ++k) { k8[k] = kSkipKey; w8[k] = 0.0f; }
+  if (r < ns) {
+    int64_t v;
+    float x, y, z;
+    if (MODE == kSamplesIn) {
+      v = smp.vox;
+      x = smp.xyz.x; y = smp.xyz.y; z = smp.xyz.z;
+    } else {
+      // point i of voxel v: offset_points order (x slowest), offset
+      // ((2 i_d + 1) - bits) / (bits - 1) times half a voxel
+      int64_t P = (int64_t)p.bits * p.bits * p.bits;
+      v = r / P;
+      int64_t i = r % P;
+      int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits), iz = (int)(i % p.bits);
+      const float *c = p.centers + v * 3;
+      float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
+      x = c[0] + ((float)(2 * ix + 1 - p.bits) / den) * hv;
+      y = c[1] + ((float)(2 * iy + 1 - p.bits) / den) * hv;
+      z = c[2] + ((float)(2 * iz + 1 - p.bits) / den) * hv;
     }
-  } else if (MODE == kSamplesIn) {
-    float4 x = p.xyzd[r];
-    interp_point(p, p.vox[r], x.x, x.y, x.z, e, bad);
-  } else {
-    // point i of voxel v: offset_points order (x slowest), offset
-    // ((2 i_d + 1) - bits) / (bits - 1) times half a voxel
-    int64_t P = (int64_t)p.bits * p.bits * p.bits;
-    int64_t v = r / P, i = r % P;
-    int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits), iz = (int)(i % p.bits);
-    const float *c = p.centers + v * 3;
-    float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
-    float x = c[0] + ((float)(2 * ix + 1 - p.bits) / den) * hv;
-    float y = c[1] + ((float)(2 * iy + 1 - p.bits) / den) * hv;
-    float z = c[2] + ((float)(2 * iz + 1 - p.bits) / den) * hv;
-    interp_point(p, v, x, y, z, e, bad);
+    if (v < 0 || v >= p.n_vox) {
+      bad = true;
+    } else {
+      const float *c = p.centers + v * 3;
+      float q[3] = {(x - c[0]) / p.voxel_size + 0.5f, (y - c[1]) / p.voxel_size + 0.5f,
+                    (z - c[2]) / p.voxel_size + 0.5f};
+      const int4 f0 = reinterpret_cast<const int4 *>(p.feats)[v * 2];
+      const int4 f1 = reinterpret_cast<const int4 *>(p.feats)[v * 2 + 1];
+      const int keys[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (keys[k] < 0 || keys[k] >= p.n_keys) {
+          bad = true;
+        } else {
+          k8[k] = keys[k];
+          w8[k] = corner_weight(q, k);
+        }
+      }
+    }
   }
+  reinterpret_cast<int4 *>(key)[0] = make_int4(k8[0], k8[1], k8[2], k8[3]);
+  reinterpret_cast<int4 *>(key)[1] = make_int4(k8[4], k8[5], k8[6], k8[7]);
+  reinterpret_cast<float4 *>(w)[0] = make_float4(w8[0], w8[1], w8[2], w8[3]);
+  reinterpret_cast<float4 *>(w)[1] = make_float4(w8[4], w8[5], w8[6], w8[7]);
+}
+
+// Input stage, pass 2 (8 lanes per row, lane cb owns channels 4cb..4cb+3):
+// sum_k w_k values[key_k][4cb..4cb+3] over the corners in order 0..7, one
+// fmaf per corner and channel -- per channel the interpolation kernel's
+// exact sequence. One load instruction reads four rows' 128-byte corner
+// rows whole. corner_loads issues the 8 loads of a row and returns the mask
+// of its valid corners; corner_blend (after the loads of the next row are
+// issued too) applies the weights.
+__device__ __forceinline__ uint32_t corner_loads(const MlpParams &p, const int *__restrict__ key,
+                                                 int cb, float4 (&val)[8]) {
+  const int4 ka = reinterpret_cast<const int4 *>(key)[0];
+  const int4 kb = reinterpret_cast<const int4 *>(key)[1];
+  const int keys[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
+  uint32_t valid = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    val[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (keys[k] != kSkipKey) {
+      val[k] = __ldg(p.values + (int64_t)keys[k] * 8 + cb);
+      valid |= 1u << k;
+    }
+  }
+  return valid;
+}
+
+__device__ __forceinline__ float4 corner_blend(const float *__restrict__ w, uint32_t valid,
+                                               const float4 (&val)[8]) {
+  const float4 wa = reinterpret_cast<const float4 *>(w)[0];
+  const float4 wb = reinterpret_cast<const float4 *>(w)[1];
+  const float ws[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+  float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (!((valid >> k) & 1u)) continue;
+    e.x = fmaf(ws[k], val[k].x, e.x);
+    e.y = fmaf(ws[k], val[k].y, e.y);
+    e.z = fmaf(ws[k], val[k].z, e.z);
+    e.w = fmaf(ws[k], val[k].w, e.w);
+  }
+  return e;
+}
+
+__device__ __forceinline__ void store_in4(uint8_t *ain, int row, int cb, float4 e) {
+  *reinterpret_cast<uint2 *>(ain + kmajor_off(row, cb * 4, E) + (cb & 1) * 8) =
+      make_uint2(pack_bf16x2(e.x, e.y), pack_bf16x2(e.z, e.w));
+}
+
+// Hidden-layer epilogue of 32 columns [c, c + 32) of one row: bias, ReLU,
+// round to bf16, store into the K-major activation tile.
+__device__ __forceinline__ void epi_chunk(const float (&v)[32], const float *__restrict__ bias,
+                                          uint8_t *ah, int row, int c) {
+  uint32_t pk[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    pk[j] = pack_relu_bf16x2(v[2 * j] + bias[c + 2 * j], v[2 * j + 1] + bias[c + 2 * j + 1]);
+#pragma unroll
+  for (int h = 0; h < 4; ++h)
+    *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8 * h, HID)) =
+        make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
 }
 
 // Persistent CTA (one per SM), 17 warps:
@@ -273,9 +355,15 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
     }
     __syncwarp();
   } else if (warp >= kLoaderWarp0) {
-    // loaders: every wait result is taken warp-uniformly
-    const int L = (warp - kLoaderWarp0) >> 2;
-    const int row = ((warp - kLoaderWarp0) & 3) * 32 + lane;
+    // loaders: every wait result is taken warp-uniformly. Warp wq of group
+    // L builds rows [32 wq, 32 wq + 32) of the group's tiles: pass 1 with
+    // lane = row, pass 2 with 8 lanes per row (4 rows at a time).
+    const int L = (warp - kLoaderWarp0) >> 2, wq = (warp - kLoaderWarp0) & 3;
+    const int rsub = lane >> 3, cb = lane & 7;
+    int *mkey = S.meta_key[warp - kLoaderWarp0];
+    float *mw = S.meta_w[warp - kLoaderWarp0];
+    // this lane's sample row of the group's next tile, loaded a tile ahead
+    SampleRow next = load_sample<MODE>(p, tile_of(L) * TILE + wq * 32 + lane, ns);
     for (int64_t i = L;; i += 2) {
       int64_t tile = tile_of(i);
       if (tile >= n_tiles) break;
@@ -284,22 +372,42 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       // the barrier's first)
       uint32_t par = (uint32_t)(((i / NB) & 1) ^ 1);
       if (!__all_sync(0xffffffffu, mbar_wait(&S.in_empty[q], par, abort))) break;
-      float e[32];
+      const int64_t r0 = tile * TILE + wq * 32;
       bool bad = false;
-      input_row<MODE>(p, tile * TILE + row, ns, e, bad);
-      if (bad && p.err) atomicOr(p.err, 4);
-      uint8_t *ain = reinterpret_cast<uint8_t *>(S.ain[q]);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        uint4 v;
-        v.x = pack_bf16x2(e[8 * c + 0], e[8 * c + 1]);
-        v.y = pack_bf16x2(e[8 * c + 2], e[8 * c + 3]);
-        v.z = pack_bf16x2(e[8 * c + 4], e[8 * c + 5]);
-        v.w = pack_bf16x2(e[8 * c + 6], e[8 * c + 7]);
-        *reinterpret_cast<uint4 *>(ain + kmajor_off(row, c * 8, E)) = v;
+      if (MODE != kEmbIn) {
+        const SampleRow cur = next;
+        next = load_sample<MODE>(p, tile_of(i + 2) * TILE + wq * 32 + lane, ns);
+        row_meta<MODE>(p, r0 + lane, ns, cur, mkey + lane * 8, mw + lane * 8, bad);
+        __syncwarp();
       }
+      uint8_t *ain = reinterpret_cast<uint8_t *>(S.ain[q]);
+      if (MODE == kEmbIn) {
+#pragma unroll 2
+        for (int it = 0; it < 8; ++it) {
+          const int row = it * 4 + rsub;
+          float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          if (r0 + row < ns) e = __ldg(reinterpret_cast<const float4 *>(p.emb + (r0 + row) * E) + cb);
+          store_in4(ain, wq * 32 + row, cb, e);
+        }
+      } else {
+        // two rows per step: both rows' 16 loads are in flight before
+        // either is blended and stored
+#pragma unroll 1
+        for (int it = 0; it < 8; it += 2) {
+          const int ra = it * 4 + rsub, rb = ra + 4;
+          float4 va[8], vb[8];
+          const uint32_t ma = corner_loads(p, mkey + ra * 8, cb, va);
+          const uint32_t mb = corner_loads(p, mkey + rb * 8, cb, vb);
+          const float4 ea = corner_blend(mw + ra * 8, ma, va);
+          const float4 eb = corner_blend(mw + rb * 8, mb, vb);
+          store_in4(ain, wq * 32 + ra, cb, ea);
+          store_in4(ain, wq * 32 + rb, cb, eb);
+        }
+      }
+      if (bad && p.err) atomicOr(p.err, 4);
       fence_async_smem();
       mbar_arrive(&S.in_full[q]);
+      __syncwarp();                     // pass 2's reads of the row table before the next pass 1
     }
   } else {
     // Epilogue warpgroups. Every wait result is taken warp-uniformly
@@ -320,21 +428,21 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
         if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) { ok = false; break; }
         fence_after_sync();
         const float *bias = S.bias[layer];
-#pragma unroll 1
-        for (int c = 0; c < HID; c += 32) {
-          float v[32];
-          tmem_ld16(tl + c, *reinterpret_cast<float(*)[16]>(v));
-          tmem_ld16(tl + c + 16, *reinterpret_cast<float(*)[16]>(v + 16));
-          tmem_wait_ld();
-          uint32_t pk[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j)
-            pk[j] = pack_relu_bf16x2(v[2 * j] + bias[c + 2 * j], v[2 * j + 1] + bias[c + 2 * j + 1]);
-#pragma unroll
-          for (int h = 0; h < 4; ++h)
-            *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8 * h, HID)) =
-                make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
-        }
+        // 32-column chunks, the next one's TMEM load in flight while this
+        // one is converted and stored
+        float va[32], vb[32];
+        tmem_ld32(tl, va);
+        tmem_wait_ld_bind(va);
+        tmem_ld32(tl + 32, vb);
+        epi_chunk(va, bias, ah, row, 0);
+        tmem_wait_ld_bind(vb);
+        tmem_ld32(tl + 64, va);
+        epi_chunk(vb, bias, ah, row, 32);
+        tmem_wait_ld_bind(va);
+        tmem_ld32(tl + 96, vb);
+        epi_chunk(va, bias, ah, row, 64);
+        tmem_wait_ld_bind(vb);
+        epi_chunk(vb, bias, ah, row, 96);
         fence_before_sync();
         fence_async_smem();
         mbar_arrive(&S.act_ready[g]);

@@ -88,6 +88,60 @@ def test_svo_matches_oracle_random_rays(cuda, voxel, n_max):
     ext.check_errors(cuda)
 
 
+def _mixed_tree(seed, depth=5, hv=0.02):
+    """A random octree whose nodes mix leaf and internal children at every
+    depth (build_octree never makes one: its leaves all hang under depth-0
+    nodes). Post-order numbering puts the root last, as the reference's
+    flattening does; children[8] is the node size (1 = leaf)."""
+    rng = np.random.RandomState(seed)
+    cen, chi = [], []
+
+    def make(c, lvl, d):
+        if lvl == 0:
+            cen.append(c)
+            chi.append([-1] * 8 + [1])
+            return len(cen) - 1
+        kids = []
+        for j in range(8):
+            s = np.array([(j >> 2) & 1, (j >> 1) & 1, j & 1]) * 2 - 1
+            cc = c + s * hv * (2 ** lvl) / 2
+            r = rng.rand()
+            if r < 0.3:
+                kids.append(-1)
+            elif r < 0.55 or d == depth:
+                kids.append(make(cc, 0, d + 1))
+            else:
+                kids.append(make(cc, lvl - 1, d + 1))
+        cen.append(c)
+        chi.append(kids + [2 ** lvl])
+        return len(cen) - 1
+
+    make(np.zeros(3), depth, 0)
+    return np.array(cen, np.float32), np.array(chi, np.int32)
+
+
+@pytest.mark.parametrize("seed,n_max", [(5, 32), (6, 8), (7, 128)])
+def test_svo_mixed_children_matches_oracle(cuda, seed, n_max):
+    """Nodes with both leaf and internal hit children: leaves met on the
+    descent stack are emitted one at a time, in the reference's DFS order."""
+    from nsvf_gb300 import ext
+    cen, chi = _mixed_tree(seed)
+    vs = 0.04
+    rng = np.random.RandomState(seed + 100)
+    o = rng.normal(size=(2000, 3))
+    o = (3 * o / np.linalg.norm(o, axis=1, keepdims=True)).astype(np.float32)
+    d = -o + rng.normal(scale=0.2, size=(2000, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    args = (_t(o[None], cuda), _t(d[None], cuda), _t(cen[None], cuda), _t(chi[None], cuda), vs, n_max)
+    ref = cpu.svo_intersect(o[None], d[None], cen[None], chi[None], vs, n_max)
+    for a, b in zip(ext.svo_intersect(*args), ref):
+        assert np.array_equal(_np(a), b)
+    assert (ref[0] != -1).sum() > 1000
+    for a, b in zip(ext.svo_intersect_sorted(*args)[:3], cpu.sort_hits(*ref)):
+        assert np.array_equal(_np(a), b)
+    ext.check_errors(cuda)
+
+
 def test_aabb_matches_oracle_many_voxels(cuda):
     """More voxels than one shared-memory tile, rays in two batch rows with
     their own voxel copies."""

@@ -18,7 +18,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-NOALLOC_MAX_NODES = 1 << 19
+NOALLOC_MAX_NODES = 1 << 18
 
 
 def _noalloc_fn():
