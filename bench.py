@@ -49,6 +49,10 @@ def parse():
                     help="rays of the frame in the CPU baseline sample")
     ap.add_argument("--size", type=int, default=800,
                     help="frame side in pixels (800 = the c2 workload; smaller for profiling)")
+    ap.add_argument("--precision", type=int, default=1,
+                    help="1: FP8-option frames and max/RMS RGB error vs an FP64 render (c2, and c4 "
+                         "with --precision-c4 1)")
+    ap.add_argument("--precision-c4", type=int, default=1)
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests of the multi-scene serving run (c5); 0 skips it")
     return ap.parse_args()
@@ -56,13 +60,13 @@ def parse():
 
 # ---------------------------------------------------------------- workload --
 
-def make_scene(dev):
+def make_scene(dev, voxel=1.0 / 64):
     import torch
     from nsvf_gb300 import scenes
     from nsvf_gb300.encoder import SparseVoxelEncoder
     from nsvf_gb300.field import StandInField
     from nsvf_gb300.renderer import VolumeRenderer
-    p, vs = scenes.scene_shell(1.0 / 64)
+    p, vs = scenes.scene_shell(voxel)
     args = argparse.Namespace(voxel_size=vs, max_hits=MAX_HITS, raymarching_stepsize_ratio=0.125,
                               voxel_embed_dim=32, use_octree=True, deterministic_step=True,
                               chunk_size=256)
@@ -85,6 +89,58 @@ def frame_rays(index, size=800):
 
 
 PRUNE_SIGMA_SCALE = 3.6e5
+
+
+def precision_bench(dev, sc, size, c4=True, frames=5):
+    """The precision workloads: (1) the served frame with E4M3 hidden layers
+    (nsvf_field_samples_fp8) timed like the BF16 frame; (2) max/RMS RGB and
+    depth error of the served BF16, served FP8 and drop-in FP32 frames
+    against a float64 render of the same samples (nsvf_gb300.precision), on
+    camera 0 of the c2 scene and, with c4, of the same shell at voxel 1/128."""
+    import torch
+    from nsvf_gb300 import ext
+    from nsvf_gb300.precision import report
+    from nsvf_gb300.served import SceneState, render_frame
+    out = {}
+    scene = SceneState(sc["enc"], sc["field"])
+    scene.mlp_fp8()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    cams = [frame_rays(i, size) for i in range(frames + 2)]
+    cams = [(torch.from_numpy(r).to(dev), torch.from_numpy(d).to(dev)) for r, d in cams]
+    for name, mlp in (("served_bf16", "tc"), ("served_fp8", "tc_fp8")):
+        with torch.no_grad():
+            for rs, rd in cams[:2]:
+                render_frame(scene, rs, rd, mlp=mlp)
+            torch.cuda.synchronize()
+            ext.KERNEL_TIMING = True
+            ext.kernel_events.clear()
+            ts = []
+            for rs, rd in cams[2:]:
+                flush.zero_()
+                s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record()
+                render_frame(scene, rs, rd, mlp=mlp)
+                e0.record()
+                torch.cuda.synchronize()
+                ts.append(s0.elapsed_time(e0))
+            ext.KERNEL_TIMING = False
+            km = ext.kernel_times_ms()
+        mk = "field_samples_fp8" if mlp == "tc_fp8" else "field_samples_bf16"
+        out[name] = {"rays_per_s": round(size * size * len(ts) / (sum(ts) / 1e3), 1),
+                     "ms_per_frame": round(sum(ts) / len(ts), 3),
+                     "mlp_ms": round(km[mk]["avg_ms"], 4) if mk in km else None}
+    out["frames"] = len(cams) - 2
+    workloads = [("c2", sc)]
+    if c4:
+        workloads.append(("c4", make_scene(dev, 1.0 / 128)))
+    for wname, s in workloads:
+        rs, rd = cams[0]
+        t0 = time.perf_counter()
+        rep_ = report(s["enc"], s["field"], s["ren"], rs, rd)
+        rep_["voxels"] = int(s["points"].shape[0])
+        rep_["seconds"] = round(time.perf_counter() - t0, 1)
+        out["errors_vs_fp64_" + wname] = rep_
+    return out
 
 
 def prune_bench(dev, sc, bits=8, th=0.5):
@@ -451,6 +507,8 @@ def run_ours(a):
     cpu = cpu_baseline(a.cpu_rays, threads=1)
     serving = serve_bench(dev, a.serve_requests) if a.serve_requests > 0 and world == 1 else None
     pruning = prune_bench(dev, sc) if world == 1 else None
+    precision = precision_bench(dev, sc, a.size, c4=bool(a.precision_c4)) \
+        if (world == 1 and a.precision and a.path == "served") else None
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(statistics.mean(ms), 3),
@@ -474,6 +532,7 @@ def run_ours(a):
         "cpu_baseline": cpu,
         "serving": serving,
         "pruning": pruning,
+        "precision": precision,
         "clocks": clk,
     }
     print(json.dumps(line))

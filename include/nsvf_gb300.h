@@ -342,6 +342,31 @@ int nsvf_field_samples_bf16(int64_t n_samples, const int32_t *voxel, const float
                             const void *const weights[5], const float *const biases[5],
                             float *out, int32_t *err, void *stream);
 
+/* field_samples_fp8: nsvf_field_samples_bf16 with the three 128x128 hidden
+ * layers in FP8 E4M3 (tcgen05 kind::f8f6f4, FP32 accumulation), the precision
+ * option for the field; the input layer and the (sigma, rgb) head stay BF16.
+ * weights[0], weights[4]: bf16 as above; weights[1..3]: E4M3 bytes of
+ * W_l * w_scale[l], row-major [128, 128], 16-byte aligned. scales (host) =
+ * {w_scale[1..3], a_scale[1..3]}, all positive and finite: the activation
+ * entering layer l is multiplied by a_scale[l] and rounded to E4M3
+ * (saturating at +-448), and layer l's accumulators are multiplied by
+ * 1 / (a_scale[l] * w_scale[l]) before its bias. No reference counterpart
+ * (the reference's field is FP32). */
+int nsvf_field_samples_fp8(int64_t n_samples, const int32_t *voxel, const float *xyz_dist,
+                           int64_t n_voxels, int64_t n_keys, float voxel_size,
+                           const float *centers, const int32_t *feats, const float *values,
+                           const void *const weights[5], const float *const biases[5],
+                           const float scales[6], float *out, int32_t *err, void *stream);
+
+/* field_samples_fp8_dev: nsvf_field_samples_fp8 on *n_samples_dev samples
+ * (at most `capacity`), one persistent CTA per SM. */
+int nsvf_field_samples_fp8_dev(int64_t capacity, const int64_t *n_samples_dev,
+                               const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
+                               int64_t n_keys, float voxel_size, const float *centers,
+                               const int32_t *feats, const float *values,
+                               const void *const weights[5], const float *const biases[5],
+                               const float scales[6], float *out, int32_t *err, void *stream);
+
 /* prune_scores_bf16: self-pruning scores (SparseVoxelEncoder.get_scores,
  * fairnr/modules/encoder.py:620-654) in one kernel: for every voxel v,
  * bits^3 points at the offset_points positions around centers[v]

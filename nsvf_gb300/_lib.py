@@ -57,6 +57,9 @@ def _load():
                                      P, P], i32),
         "nsvf_composite_segments_dev": ([i64, P, P, P, P, P, P, f32, P, f32, P, P, P, i32, P], i32),
         "nsvf_field_samples_bf16_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P], i32),
+        "nsvf_field_samples_fp8": ([i64, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P], i32),
+        "nsvf_field_samples_fp8_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P],
+                                       i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -86,5 +89,5 @@ def exported_symbols():
         "nsvf_sample_compact", "nsvf_composite_segments", "nsvf_field_samples_bf16",
         "nsvf_prune_scores_bf16", "nsvf_pinhole_rays", "nsvf_compact_hits", "nsvf_gather_probs",
         "nsvf_sample_count_dev", "nsvf_sample_compact_dev", "nsvf_composite_segments_dev",
-        "nsvf_field_samples_bf16_dev",
+        "nsvf_field_samples_bf16_dev", "nsvf_field_samples_fp8", "nsvf_field_samples_fp8_dev",
     ]

@@ -82,6 +82,14 @@ struct MlpParams {
   unsigned int *score;               // kPrune: [n_vox] float bits
   const __nv_bfloat16 *w[5];         // row-major [N, K]: 128x32, 3x 128x128, 4x128
   const float *b[5];                 // [128] x4, [4]
+  // FP8 variant: the hidden layers 1-3 as E4M3 bytes (row-major [128, 128],
+  // W * w_scale); the accumulators of layer l are multiplied by dq[l] =
+  // 1 / (a_scale[l] * w_scale[l]) before the bias, and the output of layer l
+  // (input of FP8 layer l + 1) is multiplied by qs[l] = a_scale[l + 1] before
+  // rounding to E4M3. Layer 0 (dq 1) and the head stay BF16.
+  const uint8_t *w8[3];
+  float dq[4];
+  float qs[4];
   float *out;                        // [ns, 4]: sigma, r, g, b
   int64_t ns;                        // rows (the capacity when ns_dev is set)
   const int64_t *ns_dev;             // optional: row count read on the device
@@ -108,6 +116,30 @@ __device__ void stage_weights(__nv_bfloat16 *dst, const __nv_bfloat16 *src, int 
     uint4 v = make_uint4(0, 0, 0, 0);
     if (r < valid_rows) v = *reinterpret_cast<const uint4 *>(src + (size_t)r * K + kc * 8);
     *reinterpret_cast<uint4 *>(reinterpret_cast<uint8_t *>(dst) + kmajor_off(r, kc * 8, K)) = v;
+  }
+}
+
+// Copy a row-major [rows, K] E4M3 matrix into the 8-bit K-major layout.
+__device__ void stage_weights8(uint8_t *dst, const uint8_t *src, int rows, int K) {
+  int chunks = rows * (K / 16);
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+    int r = c / (K / 16), kc = c % (K / 16);
+    uint4 v = *reinterpret_cast<const uint4 *>(src + (size_t)r * K + kc * 16);
+    *reinterpret_cast<uint4 *>(dst + kmajor_off8(r, kc * 16, K)) = v;
+  }
+}
+
+// One E4M3 layer: K / 32 MMAs of K = 32, A and B in the 8-bit K-major layout
+// (LBO 128 B, SBO (K / 16) * 128 B), each MMA 256 bytes further along K.
+__device__ __forceinline__ void issue_layer8(uint32_t d_tmem, const uint8_t *A, const uint8_t *B,
+                                             int K, int N) {
+  uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
+  uint32_t sbo = (uint32_t)(K / 16) * 128u;
+  uint32_t idesc = idesc_e4m3_f32(TILE, N);
+  for (int k = 0; k < K / 32; ++k) {
+    uint64_t ad = sdesc(a0 + 256u * k, 128u, sbo);
+    uint64_t bd = sdesc(b0 + 256u * k, 128u, sbo);
+    mma_e4m3(d_tmem, ad, bd, idesc, k > 0 ? 1u : 0u);
   }
 }
 
@@ -254,6 +286,38 @@ __device__ __forceinline__ void store_in4(uint8_t *ain, int row, int cb, float4 
       make_uint2(pack_bf16x2(e.x, e.y), pack_bf16x2(e.z, e.w));
 }
 
+// FP8 variant: dequantise (dq), bias, ReLU, scale for the next layer (qs),
+// round to E4M3 (saturating), store into the 8-bit K-major activation tile.
+__device__ __forceinline__ void epi_chunk8(const float (&v)[32], const float *__restrict__ bias,
+                                           float dq, float qs, uint8_t *ah, int row, int c) {
+  uint32_t pk[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float x0 = fmaxf(fmaf(v[4 * j + 0], dq, bias[c + 4 * j + 0]), 0.0f) * qs;
+    float x1 = fmaxf(fmaf(v[4 * j + 1], dq, bias[c + 4 * j + 1]), 0.0f) * qs;
+    float x2 = fmaxf(fmaf(v[4 * j + 2], dq, bias[c + 4 * j + 2]), 0.0f) * qs;
+    float x3 = fmaxf(fmaf(v[4 * j + 3], dq, bias[c + 4 * j + 3]), 0.0f) * qs;
+    pk[j] = pack_e4m3x2(x0, x1) | (pack_e4m3x2(x2, x3) << 16);
+  }
+  *reinterpret_cast<uint4 *>(ah + kmajor_off8(row, c, HID)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+  *reinterpret_cast<uint4 *>(ah + kmajor_off8(row, c + 16, HID)) =
+      make_uint4(pk[4], pk[5], pk[6], pk[7]);
+}
+
+// BF16 output after a dequantising FP8 layer: dq * acc + bias, ReLU, bf16.
+__device__ __forceinline__ void epi_chunk_dq(const float (&v)[32], const float *__restrict__ bias,
+                                             float dq, uint8_t *ah, int row, int c) {
+  uint32_t pk[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    pk[j] = pack_relu_bf16x2(fmaf(v[2 * j], dq, bias[c + 2 * j]),
+                             fmaf(v[2 * j + 1], dq, bias[c + 2 * j + 1]));
+#pragma unroll
+  for (int h = 0; h < 4; ++h)
+    *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8 * h, HID)) =
+        make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
+}
+
 // Hidden-layer epilogue of 32 columns [c, c + 32) of one row: bias, ReLU,
 // round to bf16, store into the K-major activation tile.
 __device__ __forceinline__ void epi_chunk(const float (&v)[32], const float *__restrict__ bias,
@@ -280,14 +344,17 @@ __device__ __forceinline__ void epi_chunk(const float (&v)[32], const float *__r
 // ring buffer i % NB and loader group i % 2. Each mbarrier completes exactly
 // one phase per use and every waiter consumes it before the next phase can
 // complete, so parity waits are unambiguous.
-template <int MODE>
+template <int MODE, bool F8>
 __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   MlpSmem &S = *reinterpret_cast<MlpSmem *>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   stage_weights(S.w0, p.w[0], HID, HID, E);
-  for (int l = 0; l < 3; ++l) stage_weights(S.wh[l], p.w[l + 1], HID, HID, HID);
+  for (int l = 0; l < 3; ++l) {
+    if (F8) stage_weights8(reinterpret_cast<uint8_t *>(S.wh[l]), p.w8[l], HID, HID);
+    else stage_weights(S.wh[l], p.w[l + 1], HID, HID, HID);
+  }
   stage_weights(S.w4, p.w[4], NOUT, 4, HID);
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
   if (tid < NOUT) S.bias4[tid] = tid < 4 ? p.b[4][tid] : 0.0f;
@@ -345,8 +412,15 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
               if (!mbar_wait(&S.act_ready[g], ph_act[g], abort)) { ok = false; break; }
               ph_act[g] ^= 1u;
               fence_after_sync();
-              if (layer < 4) issue_layer(d, S.ah[g], S.wh[layer - 1], HID, HID);
-              else issue_layer(d + 128u, S.ah[g], S.w4, HID, NOUT);
+              if (layer < 4) {
+                if (F8)
+                  issue_layer8(d, reinterpret_cast<const uint8_t *>(S.ah[g]),
+                               reinterpret_cast<const uint8_t *>(S.wh[layer - 1]), HID, HID);
+                else
+                  issue_layer(d, S.ah[g], S.wh[layer - 1], HID, HID);
+              } else {
+                issue_layer(d + 128u, S.ah[g], S.w4, HID, NOUT);
+              }
               mma_commit(&S.mma_done[g][layer]);
             }
           }
@@ -431,18 +505,34 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
         // 32-column chunks, the next one's TMEM load in flight while this
         // one is converted and stored
         float va[32], vb[32];
-        tmem_ld32(tl, va);
-        tmem_wait_ld_bind(va);
-        tmem_ld32(tl + 32, vb);
-        epi_chunk(va, bias, ah, row, 0);
-        tmem_wait_ld_bind(vb);
-        tmem_ld32(tl + 64, va);
-        epi_chunk(vb, bias, ah, row, 32);
-        tmem_wait_ld_bind(va);
-        tmem_ld32(tl + 96, vb);
-        epi_chunk(va, bias, ah, row, 64);
-        tmem_wait_ld_bind(vb);
-        epi_chunk(vb, bias, ah, row, 96);
+        if (F8) {
+          // layers 0-2 feed E4M3 layers; layer 3 feeds the BF16 head
+          const float dq = p.dq[layer], qs = p.qs[layer];
+#pragma unroll 1
+          for (int c = 0; c < HID; c += 64) {
+            tmem_ld32(tl + c, va);
+            tmem_wait_ld_bind(va);
+            tmem_ld32(tl + c + 32, vb);
+            if (layer < 3) epi_chunk8(va, bias, dq, qs, ah, row, c);
+            else epi_chunk_dq(va, bias, dq, ah, row, c);
+            tmem_wait_ld_bind(vb);
+            if (layer < 3) epi_chunk8(vb, bias, dq, qs, ah, row, c + 32);
+            else epi_chunk_dq(vb, bias, dq, ah, row, c + 32);
+          }
+        } else {
+          tmem_ld32(tl, va);
+          tmem_wait_ld_bind(va);
+          tmem_ld32(tl + 32, vb);
+          epi_chunk(va, bias, ah, row, 0);
+          tmem_wait_ld_bind(vb);
+          tmem_ld32(tl + 64, va);
+          epi_chunk(vb, bias, ah, row, 32);
+          tmem_wait_ld_bind(va);
+          tmem_ld32(tl + 96, vb);
+          epi_chunk(va, bias, ah, row, 64);
+          tmem_wait_ld_bind(vb);
+          epi_chunk(vb, bias, ah, row, 96);
+        }
         fence_before_sync();
         fence_async_smem();
         mbar_arrive(&S.act_ready[g]);
@@ -498,22 +588,22 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
 
 int g_num_sms = 0;
 
-template <int MODE>
+template <int MODE, bool F8 = false>
 int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_override);
 
-template <int MODE>
+template <int MODE, bool F8 = false>
 int launch_mlp(const MlpParams &p, cudaStream_t stream) {
-  return launch_mlp_grid<MODE>(p, stream, 0);
+  return launch_mlp_grid<MODE, F8>(p, stream, 0);
 }
 
 // grid_override < 0: one CTA per SM (the row count is only known on the
 // device); 0: sized from p.ns.
-template <int MODE>
+template <int MODE, bool F8>
 int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_override) {
   static bool attr_set = false;
   size_t smem = sizeof(MlpSmem) + 1024;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(mlp_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(mlp_tc_kernel<MODE, F8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return NSVF_ERR_CUDA;
     int dev = 0;
@@ -525,7 +615,7 @@ int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_overri
   int64_t grid = grid_override < 0 ? g_num_sms : (n_tiles + 1) / 2;
   if (grid > g_num_sms) grid = g_num_sms;
   if (grid < 1) grid = 1;
-  mlp_tc_kernel<MODE><<<(int)grid, kThreads, smem, stream>>>(p);
+  mlp_tc_kernel<MODE, F8><<<(int)grid, kThreads, smem, stream>>>(p);
   return nsvf_launch_status();
 }
 
@@ -536,6 +626,21 @@ bool set_weights(MlpParams &p, const void *const weights[5], const float *const 
     p.w[l] = (const __nv_bfloat16 *)weights[l];
     p.b[l] = biases[l];
   }
+  return true;
+}
+
+// FP8 variant: weights[0] and weights[4] bf16, weights[1..3] E4M3 bytes;
+// scales = {w_scale[1..3], a_scale[1..3]} (positive, finite).
+bool set_weights_fp8(MlpParams &p, const void *const weights[5], const float *const biases[5],
+                     const float scales[6]) {
+  if (!set_weights(p, weights, biases) || !scales) return false;
+  for (int i = 0; i < 6; ++i)
+    if (!(scales[i] > 0.0f) || !(scales[i] < 3.0e38f)) return false;
+  for (int l = 0; l < 3; ++l) p.w8[l] = (const uint8_t *)weights[l + 1];
+  p.dq[0] = 1.0f;
+  for (int l = 1; l < 4; ++l) p.dq[l] = 1.0f / (scales[l - 1] * scales[3 + l - 1]);
+  for (int l = 0; l < 3; ++l) p.qs[l] = scales[3 + l];
+  p.qs[3] = 1.0f;
   return true;
 }
 
@@ -638,6 +743,62 @@ int nsvf_prune_scores_bf16(int64_t n_voxels, int bits, int rule, float step, int
   p.ns = n_voxels * (int64_t)bits * bits * bits;
   p.err = err;
   return launch_mlp<kPrune>(p, (cudaStream_t)stream);
+}
+
+int nsvf_field_samples_fp8_dev(int64_t capacity, const int64_t *n_samples_dev,
+                               const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
+                               int64_t n_keys, float voxel_size, const float *centers,
+                               const int32_t *feats, const float *values,
+                               const void *const weights[5], const float *const biases[5],
+                               const float scales[6], float *out, int32_t *err, void *stream) {
+  if (capacity < 0 || !n_samples_dev || n_voxels < 1 || n_keys < 1) return NSVF_ERR_INVALID;
+  if (capacity == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!voxel || !xyz_dist || !centers || !feats || !values || !out ||
+      !set_weights_fp8(p, weights, biases, scales))
+    return NSVF_ERR_INVALID;
+  if ((((uintptr_t)xyz_dist) | ((uintptr_t)values) | ((uintptr_t)out) | ((uintptr_t)feats)) & 15)
+    return NSVF_ERR_INVALID;
+  p.vox = voxel;
+  p.xyzd = (const float4 *)xyz_dist;
+  p.centers = centers;
+  p.feats = feats;
+  p.values = (const float4 *)values;
+  p.n_vox = n_voxels;
+  p.n_keys = n_keys;
+  p.voxel_size = voxel_size;
+  p.out = out;
+  p.ns = capacity;
+  p.ns_dev = n_samples_dev;
+  p.err = err;
+  return launch_mlp_grid<kSamplesIn, true>(p, (cudaStream_t)stream, -1);
+}
+
+int nsvf_field_samples_fp8(int64_t n_samples, const int32_t *voxel, const float *xyz_dist,
+                           int64_t n_voxels, int64_t n_keys, float voxel_size,
+                           const float *centers, const int32_t *feats, const float *values,
+                           const void *const weights[5], const float *const biases[5],
+                           const float scales[6], float *out, int32_t *err, void *stream) {
+  if (n_samples < 0 || n_voxels < 1 || n_keys < 1) return NSVF_ERR_INVALID;
+  if (n_samples == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!voxel || !xyz_dist || !centers || !feats || !values || !out ||
+      !set_weights_fp8(p, weights, biases, scales))
+    return NSVF_ERR_INVALID;
+  if ((((uintptr_t)xyz_dist) | ((uintptr_t)values) | ((uintptr_t)out) | ((uintptr_t)feats)) & 15)
+    return NSVF_ERR_INVALID;
+  p.vox = voxel;
+  p.xyzd = (const float4 *)xyz_dist;
+  p.centers = centers;
+  p.feats = feats;
+  p.values = (const float4 *)values;
+  p.n_vox = n_voxels;
+  p.n_keys = n_keys;
+  p.voxel_size = voxel_size;
+  p.out = out;
+  p.ns = n_samples;
+  p.err = err;
+  return launch_mlp<kSamplesIn, true>(p, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -40,6 +40,36 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
          | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
+// Instruction descriptor of tcgen05.mma.kind::f8f6f4: D f32, A and B both
+// E4M3 (format code 0), both K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_e4m3_f32(int M, int N) {
+  return (1u << 4)                       // D format: f32
+         | (0u << 7)                     // A format: e4m3
+         | (0u << 10)                    // B format: e4m3
+         | ((uint32_t)(N >> 3) << 17)    // N / 8
+         | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// One MMA of K = 32 E4M3 elements (32 bytes: two core matrices along K).
+__device__ __forceinline__ void mma_e4m3(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n"
+      :
+      : "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Two floats to two E4M3 bytes (round to nearest even, saturating to
+// +-448): `lo` in the low byte.
+__device__ __forceinline__ uint32_t pack_e4m3x2(float lo, float hi) {
+  uint16_t d;
+  asm("cvt.rn.satfinite.e4m3x2.f32 %0, %2, %1;\n" : "=h"(d) : "f"(lo), "f"(hi));
+  return (uint32_t)d;
+}
+
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(
@@ -194,6 +224,12 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 // K-major layout of a K-wide operand.
 __device__ __forceinline__ uint32_t kmajor_off(int row, int k, int K) {
   return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16);
+}
+
+// The same layout for 8-bit elements: a core matrix is 8 rows x 16 elements.
+// Byte offset of the 16-byte chunk holding (row, k..k+15) of a K-wide operand.
+__device__ __forceinline__ uint32_t kmajor_off8(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K / 16) * 128 + (k >> 4) * 128 + (row & 7) * 16);
 }
 
 }  // namespace nsvf_tc

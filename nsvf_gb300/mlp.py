@@ -3,6 +3,10 @@
 TensorCoreMLP(field) snapshots the field's weights as bf16 (row-major
 [out, in]) and biases as FP32 on the field's device; calling it on an FP32
 embedding [N, 32] returns [N, 4] = (sigma, r, g, b) in FP32.
+
+enable_fp8(calibration_emb) adds the FP8 option of the fused sample kernel
+(nsvf_field_samples_fp8): the three 128x128 hidden layers in E4M3 with
+per-layer scales, the input layer and the (sigma, rgb) head in BF16.
 """
 import ctypes
 
@@ -22,6 +26,31 @@ class TensorCoreMLP:
         self.device = self.w[0].device
         self._wp = (ctypes.c_void_p * 5)(*[t.data_ptr() for t in self.w])
         self._bp = (ctypes.c_void_p * 5)(*[t.data_ptr() for t in self.b])
+        self.w32 = [lin.weight.detach().float().contiguous() for lin in field.layers]
+        self.fp8 = None
+
+    E4M3_MAX = 448.0
+
+    def enable_fp8(self, calibration_emb):
+        """Per-layer scales for E4M3 hidden layers. Weights: w_scale[l] =
+        448 / max|W_l|. Activations: a_scale[l] = 448 / (max of the FP32
+        activation entering layer l on `calibration_emb` [N, 32]); larger
+        values saturate to 448 at run time."""
+        x = calibration_emb.float()
+        amax = []
+        with torch.no_grad():
+            for i in range(3):
+                x = torch.relu(x @ self.w32[i].t() + self.b[i])
+                amax.append(float(x.abs().max()))
+        w_scale = [self.E4M3_MAX / max(float(self.w32[l].abs().max()), 1e-30) for l in (1, 2, 3)]
+        a_scale = [self.E4M3_MAX / max(a, 1e-30) for a in amax]
+        w8 = [(self.w32[l] * s).clamp(-self.E4M3_MAX, self.E4M3_MAX).to(torch.float8_e4m3fn)
+              .contiguous() for l, s in zip((1, 2, 3), w_scale)]
+        ptrs = [self.w[0].data_ptr()] + [t.data_ptr() for t in w8] + [self.w[4].data_ptr()]
+        self.fp8 = {"w8": w8, "w_scale": w_scale, "a_scale": a_scale,
+                    "wp": (ctypes.c_void_p * 5)(*ptrs),
+                    "scales": (ctypes.c_float * 6)(*(w_scale + a_scale))}
+        return self
 
     def __call__(self, emb, out=None):
         emb = emb.float().contiguous()
@@ -50,6 +79,22 @@ class TensorCoreMLP:
                 ext.ctypes_stream(dev)), "field_samples_bf16")
         return out
 
+    def field_samples_fp8(self, voxel, xyz_dist, centers, feats, values, voxel_size, out=None):
+        """field_samples with E4M3 hidden layers (enable_fp8 first)."""
+        if self.fp8 is None:
+            raise RuntimeError("TensorCoreMLP.enable_fp8 has not been called")
+        n = voxel.numel()
+        dev = voxel.device
+        if out is None:
+            out = torch.empty(n, 4, dtype=torch.float32, device=dev)
+        with ext._timed("field_samples_fp8", dev):
+            check(LIB.nsvf_field_samples_fp8(
+                n, voxel.data_ptr(), xyz_dist.data_ptr(), centers.size(0), values.size(0),
+                float(voxel_size), centers.data_ptr(), feats.data_ptr(), values.data_ptr(),
+                self.fp8["wp"], self._bp, self.fp8["scales"], out.data_ptr(),
+                ext.error_word(dev).data_ptr(), ext.ctypes_stream(dev)), "field_samples_fp8")
+        return out
+
     def prune_scores(self, centers, feats, values, voxel_size, bits=8, rule=1, step=0.0):
         """Per-voxel pruning score over bits^3 points (see nsvf_prune_scores_bf16):
         rule 0 -> min exp(-relu sigma), rule 1 -> max 1 - exp(-relu(sigma) step)."""
@@ -73,3 +118,20 @@ class TensorCoreMLP:
             if i < 4:
                 x = torch.relu(x).to(torch.bfloat16).float()
         return x
+
+    def reference_fp8(self, emb):
+        """torch emulation of the FP8 kernel: bf16 input layer, E4M3 (saturating)
+        activations and weights with the per-layer scales for layers 1-3,
+        dequantise + bias + ReLU in FP32, bf16 head."""
+        f = self.fp8
+        e4 = torch.float8_e4m3fn
+        x = emb.float().to(torch.bfloat16).float()
+        x = x @ self.w[0].float().t()
+        for l in range(1, 4):
+            dq = 1.0 if l == 1 else 1.0 / (f["a_scale"][l - 2] * f["w_scale"][l - 2])
+            x = torch.relu(x * dq + self.b[l - 1]) * f["a_scale"][l - 1]
+            x = x.clamp(-self.E4M3_MAX, self.E4M3_MAX).to(e4).float()
+            x = x @ f["w8"][l - 1].float().t()
+        dq = 1.0 / (f["a_scale"][2] * f["w_scale"][2])
+        x = torch.relu(x * dq + self.b[3]).to(torch.bfloat16).float()
+        return x @ self.w[4].float().t() + self.b[4]

@@ -12,7 +12,18 @@ and compositing in float64 with torch:
   p_i = (1 - exp(-fe_i)) exp(-sum_{j<i} fe_j), colour = sum p c + missed * bg.
 
 `report()` gives the max and RMS RGB error and the max depth error (hit
-pixels) of each path against it.
+pixels) of each path against it: the served BF16 frame, the served frame with
+E4M3 hidden layers, and the drop-in FP32 frame.
+
+Samples far outside their voxel. The reference's inverse-CDF kernel can give
+a sample the voxel id of the next row (its tail loop, which this library
+reproduces bit for bit: fairnr/clib/src/sample_gpu.cu:188-201). Such a
+sample's position lies voxels away from that voxel, and the trilinear weights
+extrapolate (by 1e5x at the c2 frame), so field outputs there are orders of
+magnitude larger than elsewhere. A relative MLP error then becomes a large
+absolute colour error on those pixels. The report counts these samples (a
+coordinate more than half a voxel outside the voxel) and gives the errors
+over all pixels and over the pixels that have none.
 """
 import torch
 
@@ -45,6 +56,8 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
     W = [(l.weight.double(), l.bias.double()) for l in field.layers]
     bg = field.bg_color.bg_color.double()
     colors = bg.expand(R, 3).clone()
+    foreign = torch.zeros(R, dtype=torch.bool, device=dev)
+    n_foreign = 0
     depths = torch.full((R,), float(field.bg_color.depth), dtype=torch.float64, device=dev)
     vs = float(encoder.voxel_size)
     cc = torch.tensor([-1.0, 1.0], dtype=torch.float64, device=dev)
@@ -61,6 +74,11 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
         xyz = o64 + rd[:, None, :] * t[..., None]
         v = vid[mask]
         p = ((xyz[mask] - centers[v]) / vs + .5)[:, None, :]
+        far = ((p[:, 0] < -0.5) | (p[:, 0] > 1.5)).any(-1)
+        n_foreign += int(far.sum())
+        fr = torch.zeros(mask.shape, dtype=torch.bool, device=dev)
+        fr[mask] = far
+        foreign[pix[a:b]] = fr.any(-1)
         w = (p * q + (1 - p) * (1 - q)).prod(-1)
         emb = (w[..., None] * values[feats[v]]).sum(1)
         x = emb
@@ -78,23 +96,30 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
         missed = 1 - pr.sum(-1)
         colors[pix[a:b]] = (rgb * pr[..., None]).sum(1) + missed[:, None] * bg
         depths[pix[a:b]] = (t.masked_fill(~mask, 0) * pr).sum(-1) + missed * float(field.bg_color.depth)
-    return colors, depths, hits
+    return colors, depths, hits, foreign, n_foreign
 
 
 def report(encoder, field, renderer, ray_start, ray_dir):
     """Errors of the served BF16 and the drop-in FP32 frame against float64."""
-    ref_c, ref_d, hits = fp64_render(encoder, field, ray_start, ray_dir)
+    ref_c, ref_d, hits, foreign, n_foreign = fp64_render(encoder, field, ray_start, ray_dir)
     scene = SceneState(encoder, field)
     served = render_frame(scene, ray_start, ray_dir)
+    served8 = render_frame(scene, ray_start, ray_dir, mlp="tc_fp8")
     with torch.no_grad():
         plain = render_rays(encoder, field, renderer, ray_start.reshape(1, 1, 1, 3),
                             ray_dir.reshape(1, 1, -1, 3))
     out = {}
     for name, c, d in [("served_bf16", served["colors"], served["depths"]),
+                       ("served_fp8", served8["colors"], served8["depths"]),
                        ("plain_fp32", plain["colors"].reshape(-1, 3), plain["depths"].reshape(-1))]:
         e = (c.double() - ref_c).abs()
         de = (d.double() - ref_d).abs()[hits]
+        clean = e[~foreign]
         out[name] = {"max_rgb_err": float(e.max()), "rms_rgb_err": float(e.pow(2).mean().sqrt()),
-                     "max_depth_err_hit_pixels": float(de.max()) if de.numel() else 0.0}
+                     "max_depth_err_hit_pixels": float(de.max()) if de.numel() else 0.0,
+                     "max_rgb_err_clean_pixels": float(clean.max()) if clean.numel() else 0.0,
+                     "rms_rgb_err_clean_pixels": float(clean.pow(2).mean().sqrt()) if clean.numel() else 0.0}
     out["hit_pixels"] = int(hits.sum())
+    out["samples_outside_their_voxel"] = n_foreign
+    out["pixels_with_such_samples"] = int(foreign.sum())
     return out

@@ -53,6 +53,21 @@ class SceneState:
         self.bg_depth = float(field.bg_color.depth)
         self.device = self.centers.device
 
+    def mlp_fp8(self, n_calibration=65536, seed=0):
+        """The tensor-core MLP with E4M3 hidden layers, its activation scales
+        calibrated once on `n_calibration` points drawn uniformly inside
+        random voxels of this scene (FP32 interpolation + FP32 MLP)."""
+        if self.mlp.fp8 is None:
+            g = torch.Generator(device="cpu").manual_seed(seed)
+            V = self.centers.size(0)
+            vox = torch.randint(0, V, (n_calibration,), generator=g).to(self.device)
+            off = (torch.rand(n_calibration, 3, generator=g) - 0.5).to(self.device) * self.voxel_size
+            xyz = self.centers[vox] + off
+            emb = trilinear_embed(vox.int(), xyz, self.centers, self.feats, self.values,
+                                  self.voxel_size)
+            self.mlp.enable_fp8(emb)
+        return self.mlp
+
     def bytes(self):
         ts = [self.octree_centers, self.octree_children, self.centers, self.feats, self.values]
         ts += self.mlp.w + self.mlp.b
@@ -62,10 +77,10 @@ class SceneState:
 def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     """ray_start [3] (shared origin) or [R, 3], ray_dir [R, 3] (FP32, on the
     scene's device) -> dict(colors [R, 3], depths [R], missed [R]).
-    mlp: "tc" (interpolation fused into the tcgen05 BF16 MLP), "tc_unfused"
-    (interpolation kernel, then the MLP kernel), "bf16_emulated" (torch
-    emulation of the kernel's rounding) or "fp32" (the field's FP32 torch
-    forward)."""
+    mlp: "tc" (interpolation fused into the tcgen05 BF16 MLP), "tc_fp8" (the
+    same with E4M3 hidden layers), "tc_unfused" (interpolation kernel, then
+    the MLP kernel), "bf16_emulated" / "fp8_emulated" (torch emulations of
+    the kernels' rounding) or "fp32" (the field's FP32 torch forward)."""
     dev = scene.device
     R = ray_dir.shape[0]
     rd = ray_dir.float().contiguous()
@@ -115,6 +130,9 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     if mlp == "tc":
         field = scene.mlp.field_samples(vox, xyzd, scene.centers, scene.feats, scene.values,
                                         scene.voxel_size)
+    elif mlp == "tc_fp8":
+        field = scene.mlp_fp8().field_samples_fp8(vox, xyzd, scene.centers, scene.feats,
+                                                  scene.values, scene.voxel_size)
     else:
         emb = trilinear_embed(vox, xyzd[:, :3], scene.centers, scene.feats, scene.values,
                               scene.voxel_size)
@@ -122,6 +140,8 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
             field = scene.mlp(emb)
         elif mlp == "bf16_emulated":
             field = scene.mlp.reference_bf16(emb).contiguous()
+        elif mlp == "fp8_emulated":
+            field = scene.mlp_fp8().reference_fp8(emb).contiguous()
         else:
             field = scene.field.mlp(emb).float().contiguous()
     with ext._timed("composite_segments", dev):

@@ -107,3 +107,51 @@ def test_prune_scores_against_reference(golden, golden_prune, cuda, rule, bits):
     far = margin > 0.02
     assert np.array_equal(keep[far], ref_keep[far])
     assert far.sum() > 0.8 * far.size
+
+
+def test_fp8_hidden_layers_match_emulation(golden, cuda):
+    """E4M3 hidden layers (nsvf_field_samples_fp8) against a torch emulation
+    of the same quantisation (per-layer scales, saturating E4M3 rounding,
+    FP32 sums). Summation order and one fused multiply-add in the dequantise
+    step can flip single E4M3 roundings, so the bar is statistical; the
+    error against the FP32 field is reported as the FP8 option's cost."""
+    from nsvf_gb300 import scenes
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.functional import trilinear_embed
+    from nsvf_gb300.mlp import TensorCoreMLP
+    g = golden
+    hit = g["svo_hits"][0]
+    d = g["svo_det_sampled_point_depth"]
+    mask = g["svo_det_sampled_point_voxel_idx"] != -1
+    xyz = (g["ray_start"][None, None] + g["ray_dir"][hit][:, None] * d[..., None]).astype(np.float32)[mask]
+    n = xyz.shape[0]
+    xyzd = torch.zeros(n, 4, device=cuda)
+    xyzd[:, :3] = torch.from_numpy(xyz).to(cuda)
+    vox = torch.from_numpy(g["svo_det_sampled_point_voxel_idx"][mask]).to(cuda).int()
+    centers = torch.from_numpy(g["svo_centers_shifted"]).to(cuda)
+    feats = torch.from_numpy(g["feats"]).to(cuda).int()
+    values = (torch.from_numpy(g["embed"]) * 50.0).to(cuda)      # activations well inside E4M3
+    vs = float(g["voxel_size"])
+    field = StandInField(weights=scenes.stand_in_mlp_weights(seed=5)).to(cuda)
+    with torch.no_grad():
+        for lin in field.layers:
+            lin.bias.uniform_(-0.05, 0.05)
+    mlp = TensorCoreMLP(field)
+    emb = trilinear_embed(vox, xyzd[:, :3], centers, feats, values, vs)
+    mlp.enable_fp8(emb)
+    out = mlp.field_samples_fp8(vox, xyzd, centers, feats, values, vs)
+    from nsvf_gb300 import ext
+    ext.check_errors(cuda)
+    emu = mlp.reference_fp8(emb)
+    with torch.no_grad():
+        f32 = field.mlp(emb)
+    scale = f32.abs().max().item()
+    diff = (out - emu).abs() / scale
+    err32 = (out - f32).abs() / scale
+    stats = dict(n=n, median_vs_emulation=diff.median().item(), max_vs_emulation=diff.max().item(),
+                 max_vs_fp32=err32.max().item(), rms_vs_fp32=err32.pow(2).mean().sqrt().item())
+    print("fp8 hidden layers:", stats)
+    assert n > 5000
+    assert stats["median_vs_emulation"] <= 2e-3, stats
+    assert stats["max_vs_emulation"] <= 5e-2, stats
+    assert stats["max_vs_fp32"] <= 0.15, stats
