@@ -32,28 +32,60 @@ constexpr int HID = 128;    // hidden width
 constexpr int NOUT = 16;    // N of the last MMA (4 outputs used)
 constexpr int TILE = 128;   // samples per MMA tile (M)
 constexpr int NB = 4;       // input tile ring depth
-constexpr int kMmaWarp = 8;
-constexpr int kLoaderWarp0 = 9;                 // warps 9..16: two loader warpgroups
-constexpr int kThreads = 17 * 32;
 constexpr uint32_t kTmemCols = 512;
 
+// Warp roles and tile slots of the two variants.
+//   BF16: 17 warps; two tile slots of 256 TMEM columns (head output at
+//         +128); epilogue warps 0-7, MMA warp 8, loader warps 9-16.
+//   FP8:  the hidden weights and activations take half the shared memory,
+//         which makes room for a third tile slot: 24 warps; three slots of
+//         128 TMEM columns (the head output reuses the slot's first 16);
+//         epilogue warps 0-11, loader warps 12-19, MMA warp 20 (21-23 only
+//         complete its warpgroup). The warpgroups rebalance registers with
+//         setmaxnreg (below).
+template <bool F8>
+struct Cfg {
+  static constexpr int kSlots = F8 ? 3 : 2;
+  static constexpr int kEpiWarps = 4 * kSlots;
+  static constexpr int kLoaderWarp0 = F8 ? kEpiWarps : kEpiWarps + 1;
+  static constexpr int kMmaWarp = F8 ? kLoaderWarp0 + 8 : kEpiWarps;
+  static constexpr int kThreads = F8 ? 24 * 32 : 17 * 32;
+  static constexpr uint32_t kSlotCols = F8 ? 128u : 256u;
+  static constexpr uint32_t kHeadCol = F8 ? 0u : 128u;
+  static constexpr int kHidBytes = F8 ? HID * HID : HID * HID * 2;  // one hidden weight matrix
+};
+
+// FP8 variant: registers per thread after the warpgroups rebalance. The MMA
+// warpgroup gives registers up and the loaders take them (two rows of
+// gathers in flight); the epilogues keep the launch count. The kernel is launched with
+// kLaunchRegs8 per thread; the split must fit in 768 * kLaunchRegs8, or the
+// loaders' setmaxnreg.inc would wait forever -- the host checks the compiled
+// register count before the first launch.
+constexpr int kLaunchRegs8 = 80, kEpiRegs8 = 80, kLoaderRegs8 = 88, kMmaRegs8 = 64;
+static_assert(Cfg<true>::kThreads * kLaunchRegs8 <= 65536, "launch registers");
+static_assert(3 * 128 * kEpiRegs8 + 2 * 128 * kLoaderRegs8 + 128 * kMmaRegs8 <=
+                  Cfg<true>::kThreads * kLaunchRegs8,
+              "register split exceeds the launch allocation");
+
+template <bool F8>
 struct __align__(128) MlpSmem {
   __nv_bfloat16 w0[HID * E];
-  __nv_bfloat16 wh[3][HID * HID];
+  uint8_t wh[3][Cfg<F8>::kHidBytes];       // bf16 or E4M3 hidden weights
   __nv_bfloat16 w4[NOUT * HID];
   __nv_bfloat16 ain[NB][TILE * E];
-  __nv_bfloat16 ah[2][TILE * HID];
+  __nv_bfloat16 ah[Cfg<F8>::kSlots][TILE * HID];  // E4M3 uses the first half
   // per loader warp: its 32 rows' corner keys (kSkipKey = skip) and
   // trilinear weights, written by the row's lane and read by the 8 lanes
   // that gather the row
   int meta_key[8][32 * 8];
   float meta_w[8][32 * 8];
   float bias[4][HID];
+  float bias_q[F8 ? 3 : 1][HID];          // FP8: bias[l] * qs[l] for layers 0-2
   float bias4[NOUT];
-  uint64_t mma_done[2][5];   // per slot and layer: one phase per tile
-  uint64_t act_ready[2];     // epilogue -> MMA: hidden activations written
-  uint64_t in_full[NB];      // loaders -> MMA: input tile written
-  uint64_t in_empty[NB];     // MMA -> loaders: first layer done reading
+  uint64_t mma_done[Cfg<F8>::kSlots][5];  // per slot and layer: one phase per tile
+  uint64_t act_ready[Cfg<F8>::kSlots];    // epilogue -> MMA: hidden activations written
+  uint64_t in_full[NB];                   // loaders -> MMA: input tile written
+  uint64_t in_empty[NB];                  // MMA -> loaders: first layer done reading
   uint32_t tmem_base;
   int abort;
 };
@@ -90,6 +122,7 @@ struct MlpParams {
   const uint8_t *w8[3];
   float dq[4];
   float qs[4];
+  float dqs[3];                      // dq[l] * qs[l]: FP8 outputs are relu(fmaf(acc, dqs, bias * qs))
   float *out;                        // [ns, 4]: sigma, r, g, b
   int64_t ns;                        // rows (the capacity when ns_dev is set)
   const int64_t *ns_dev;             // optional: row count read on the device
@@ -286,18 +319,18 @@ __device__ __forceinline__ void store_in4(uint8_t *ain, int row, int cb, float4 
       make_uint2(pack_bf16x2(e.x, e.y), pack_bf16x2(e.z, e.w));
 }
 
-// FP8 variant: dequantise (dq), bias, ReLU, scale for the next layer (qs),
-// round to E4M3 (saturating), store into the 8-bit K-major activation tile.
-__device__ __forceinline__ void epi_chunk8(const float (&v)[32], const float *__restrict__ bias,
-                                           float dq, float qs, uint8_t *ah, int row, int c) {
+// FP8 variant: dequantise and scale for the next layer in one fmaf
+// (dqs = dq * qs, bias_q = bias * qs; ReLU commutes with the positive
+// scale), ReLU + round to E4M3 (saturating) in one cvt, store into the
+// 8-bit K-major activation tile.
+__device__ __forceinline__ void epi_chunk8(const float (&v)[32], const float *__restrict__ bias_q,
+                                           float dqs, uint8_t *ah, int row, int c) {
   uint32_t pk[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    float x0 = fmaxf(fmaf(v[4 * j + 0], dq, bias[c + 4 * j + 0]), 0.0f) * qs;
-    float x1 = fmaxf(fmaf(v[4 * j + 1], dq, bias[c + 4 * j + 1]), 0.0f) * qs;
-    float x2 = fmaxf(fmaf(v[4 * j + 2], dq, bias[c + 4 * j + 2]), 0.0f) * qs;
-    float x3 = fmaxf(fmaf(v[4 * j + 3], dq, bias[c + 4 * j + 3]), 0.0f) * qs;
-    pk[j] = pack_e4m3x2(x0, x1) | (pack_e4m3x2(x2, x3) << 16);
+    const float4 bq = *reinterpret_cast<const float4 *>(bias_q + c + 4 * j);
+    pk[j] = pack_relu_e4m3x2(fmaf(v[4 * j + 0], dqs, bq.x), fmaf(v[4 * j + 1], dqs, bq.y)) |
+            (pack_relu_e4m3x2(fmaf(v[4 * j + 2], dqs, bq.z), fmaf(v[4 * j + 3], dqs, bq.w)) << 16);
   }
   *reinterpret_cast<uint4 *>(ah + kmajor_off8(row, c, HID)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
   *reinterpret_cast<uint4 *>(ah + kmajor_off8(row, c + 16, HID)) =
@@ -332,34 +365,37 @@ __device__ __forceinline__ void epi_chunk(const float (&v)[32], const float *__r
         make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
 }
 
-// Persistent CTA (one per SM), 17 warps:
-//   warps 0-3, 4-7  epilogue warpgroups of tile slots 0 and 1 (TMEM columns
-//                   [256 g, 256 g + 144)): bias + ReLU + bf16 of each hidden
-//                   layer back to shared memory, and the output stage;
-//   warp 8          TMEM allocation; lane 0 issues all tcgen05.mma;
-//   warps 9-16      two loader warpgroups that build the input tiles (the
-//                   embedding gathers and interpolation) into a ring of NB
-//                   buffers ahead of the MMAs.
-// The CTA's tiles are b, b + G, b + 2G, ...: local tile i uses slot i % 2,
-// ring buffer i % NB and loader group i % 2. Each mbarrier completes exactly
-// one phase per use and every waiter consumes it before the next phase can
-// complete, so parity waits are unambiguous.
+// Persistent CTA (one per SM), roles as in Cfg:
+//   epilogue warpgroups, one per tile slot g: bias + ReLU + rounding of each
+//                   hidden layer back to shared memory, and the output stage;
+//   MMA warp        TMEM allocation; lane 0 issues all tcgen05.mma;
+//   loader warps    two warpgroups that build the input tiles (the embedding
+//                   gathers and interpolation) into a ring of NB buffers
+//                   ahead of the MMAs.
+// The CTA's tiles are b, b + G, b + 2G, ...: local tile i uses slot
+// i % kSlots, ring buffer i % NB and loader group i % 2. Each mbarrier
+// completes exactly one phase per use and every waiter consumes it before
+// the next phase can complete, so parity waits are unambiguous.
 template <int MODE, bool F8>
-__global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) {
+__global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpParams p) {
+  using C = Cfg<F8>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  MlpSmem &S = *reinterpret_cast<MlpSmem *>(smem_raw);
+  MlpSmem<F8> &S = *reinterpret_cast<MlpSmem<F8> *>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   stage_weights(S.w0, p.w[0], HID, HID, E);
   for (int l = 0; l < 3; ++l) {
-    if (F8) stage_weights8(reinterpret_cast<uint8_t *>(S.wh[l]), p.w8[l], HID, HID);
-    else stage_weights(S.wh[l], p.w[l + 1], HID, HID, HID);
+    if (F8) stage_weights8(S.wh[l], p.w8[l], HID, HID);
+    else stage_weights(reinterpret_cast<__nv_bfloat16 *>(S.wh[l]), p.w[l + 1], HID, HID, HID);
   }
   stage_weights(S.w4, p.w[4], NOUT, 4, HID);
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
+  if (F8)
+    for (int i = tid; i < 3 * HID; i += blockDim.x)
+      S.bias_q[i / HID][i % HID] = p.b[i / HID][i % HID] * p.qs[i / HID];
   if (tid < NOUT) S.bias4[tid] = tid < 4 ? p.b[4][tid] : 0.0f;
   if (tid == 0) {
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < C::kSlots; ++g) {
       for (int l = 0; l < 5; ++l) mbar_init(&S.mma_done[g][l], 1);
       mbar_init(&S.act_ready[g], 128);
     }
@@ -370,7 +406,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
     S.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == kMmaWarp) tmem_alloc(&S.tmem_base, kTmemCols);
+  if (warp == C::kMmaWarp) tmem_alloc(&S.tmem_base, kTmemCols);
   fence_async_smem();
   fence_before_sync();
   __syncthreads();
@@ -389,18 +425,23 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
   const int64_t G = gridDim.x, b = blockIdx.x;
   auto tile_of = [&](int64_t i) { return b + i * G; };
 
-  if (warp == kMmaWarp) {
-    if (lane == 0) {
-      uint32_t ph_act[2] = {0u, 0u};
+  const bool mma_role = F8 ? warp >= C::kMmaWarp : warp == C::kMmaWarp;
+  const bool loader_role = warp >= C::kLoaderWarp0 && warp < C::kLoaderWarp0 + 8;
+  if (mma_role) {
+    if constexpr (F8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kMmaRegs8));
+    if (warp == C::kMmaWarp && lane == 0) {
+      uint32_t ph_act[C::kSlots] = {};
       bool ok = true;
-      for (int64_t i = 0; ok; i += 2) {
-        bool has[2] = {tile_of(i) < n_tiles, tile_of(i + 1) < n_tiles};
-        if (!has[0]) break;
+#pragma unroll 1
+      for (int64_t i = 0; ok; i += C::kSlots) {
+        if (tile_of(i) >= n_tiles) break;
+#pragma unroll 1
         for (int layer = 0; layer < 5 && ok; ++layer) {
-          for (int g = 0; g < 2 && ok; ++g) {
-            if (!has[g]) continue;
-            int64_t ii = i + g;
-            uint32_t d = tmem + 256u * g;
+#pragma unroll 1
+          for (int g = 0; g < C::kSlots && ok; ++g) {
+            const int64_t ii = i + g;
+            if (tile_of(ii) >= n_tiles) break;
+            const uint32_t d = tmem + C::kSlotCols * g;
             if (layer == 0) {
               int q = (int)(ii % NB);
               if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
@@ -414,12 +455,13 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
               fence_after_sync();
               if (layer < 4) {
                 if (F8)
-                  issue_layer8(d, reinterpret_cast<const uint8_t *>(S.ah[g]),
-                               reinterpret_cast<const uint8_t *>(S.wh[layer - 1]), HID, HID);
+                  issue_layer8(d, reinterpret_cast<const uint8_t *>(S.ah[g]), S.wh[layer - 1],
+                               HID, HID);
                 else
-                  issue_layer(d, S.ah[g], S.wh[layer - 1], HID, HID);
+                  issue_layer(d, S.ah[g], reinterpret_cast<const __nv_bfloat16 *>(S.wh[layer - 1]),
+                              HID, HID);
               } else {
-                issue_layer(d + 128u, S.ah[g], S.w4, HID, NOUT);
+                issue_layer(d + C::kHeadCol, S.ah[g], S.w4, HID, NOUT);
               }
               mma_commit(&S.mma_done[g][layer]);
             }
@@ -428,14 +470,15 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       }
     }
     __syncwarp();
-  } else if (warp >= kLoaderWarp0) {
+  } else if (loader_role) {
+    if constexpr (F8) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(kLoaderRegs8));
     // loaders: every wait result is taken warp-uniformly. Warp wq of group
     // L builds rows [32 wq, 32 wq + 32) of the group's tiles: pass 1 with
     // lane = row, pass 2 with 8 lanes per row (4 rows at a time).
-    const int L = (warp - kLoaderWarp0) >> 2, wq = (warp - kLoaderWarp0) & 3;
+    const int L = (warp - C::kLoaderWarp0) >> 2, wq = (warp - C::kLoaderWarp0) & 3;
     const int rsub = lane >> 3, cb = lane & 7;
-    int *mkey = S.meta_key[warp - kLoaderWarp0];
-    float *mw = S.meta_w[warp - kLoaderWarp0];
+    int *mkey = S.meta_key[warp - C::kLoaderWarp0];
+    float *mw = S.meta_w[warp - C::kLoaderWarp0];
     // this lane's sample row of the group's next tile, loaded a tile ahead
     SampleRow next = load_sample<MODE>(p, tile_of(L) * TILE + wq * 32 + lane, ns);
     for (int64_t i = L;; i += 2) {
@@ -484,19 +527,21 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       __syncwarp();                     // pass 2's reads of the row table before the next pass 1
     }
   } else {
+    if constexpr (F8 && kEpiRegs8 < kLaunchRegs8)
+      asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kEpiRegs8));
     // Epilogue warpgroups. Every wait result is taken warp-uniformly
     // (__all_sync), so the .sync.aligned tcgen05.ld and the warp shuffles
     // below always run with all 32 lanes, also when a timeout makes the CTA
     // unwind.
     const int g = warp >> 2, q4 = warp & 3;
     const int row = q4 * 32 + lane;
-    const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + 256u * g;
+    const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + C::kSlotCols * g;
     uint8_t *ah = reinterpret_cast<uint8_t *>(S.ah[g]);
     bool ok = true;
-    for (int64_t i = g; ok; i += 2) {
+    for (int64_t i = g; ok; i += C::kSlots) {
       int64_t tile = tile_of(i);
       if (tile >= n_tiles) break;
-      const uint32_t par = (uint32_t)((i >> 1) & 1);
+      const uint32_t par = (uint32_t)((i / C::kSlots) & 1);
       int64_t r = tile * TILE + row;
       for (int layer = 0; layer < 4; ++layer) {
         if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) { ok = false; break; }
@@ -506,18 +551,31 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
         // one is converted and stored
         float va[32], vb[32];
         if (F8) {
-          // layers 0-2 feed E4M3 layers; layer 3 feeds the BF16 head
-          const float dq = p.dq[layer], qs = p.qs[layer];
+          // layers 0-2 feed E4M3 layers; layer 3 feeds the BF16 head. The
+          // next chunk's TMEM load is in flight while this one is stored.
+          if (layer < 3) {
+            const float dqs = p.dqs[layer];
+            const float *bq = S.bias_q[layer];
 #pragma unroll 1
-          for (int c = 0; c < HID; c += 64) {
-            tmem_ld32(tl + c, va);
-            tmem_wait_ld_bind(va);
-            tmem_ld32(tl + c + 32, vb);
-            if (layer < 3) epi_chunk8(va, bias, dq, qs, ah, row, c);
-            else epi_chunk_dq(va, bias, dq, ah, row, c);
-            tmem_wait_ld_bind(vb);
-            if (layer < 3) epi_chunk8(vb, bias, dq, qs, ah, row, c + 32);
-            else epi_chunk_dq(vb, bias, dq, ah, row, c + 32);
+            for (int c = 0; c < HID; c += 64) {
+              tmem_ld32(tl + c, va);
+              tmem_wait_ld_bind(va);
+              tmem_ld32(tl + c + 32, vb);
+              epi_chunk8(va, bq, dqs, ah, row, c);
+              tmem_wait_ld_bind(vb);
+              epi_chunk8(vb, bq, dqs, ah, row, c + 32);
+            }
+          } else {
+            const float dq = p.dq[layer];
+#pragma unroll 1
+            for (int c = 0; c < HID; c += 64) {
+              tmem_ld32(tl + c, va);
+              tmem_wait_ld_bind(va);
+              tmem_ld32(tl + c + 32, vb);
+              epi_chunk_dq(va, bias, dq, ah, row, c);
+              tmem_wait_ld_bind(vb);
+              epi_chunk_dq(vb, bias, dq, ah, row, c + 32);
+            }
           }
         } else {
           tmem_ld32(tl, va);
@@ -541,7 +599,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
       if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) { ok = false; break; }
       fence_after_sync();
       float v[16];
-      tmem_ld16(tl + 128u, v);
+      tmem_ld16(tl + C::kHeadCol, v);
       tmem_wait_ld();
       fence_before_sync();
       float sigma = v[0] + S.bias4[0];
@@ -580,7 +638,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_tc_kernel(const MlpParams p) 
   fence_before_sync();
   __syncthreads();
   if (tid == 0 && S.abort && p.err) atomicOr(p.err, 8);
-  if (warp == kMmaWarp) {
+  if (warp == C::kMmaWarp) {
     fence_after_sync();
     tmem_dealloc(tmem, kTmemCols);
   }
@@ -601,8 +659,17 @@ int launch_mlp(const MlpParams &p, cudaStream_t stream) {
 template <int MODE, bool F8>
 int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_override) {
   static bool attr_set = false;
-  size_t smem = sizeof(MlpSmem) + 1024;
+  size_t smem = sizeof(MlpSmem<F8>) + 1024;
   if (!attr_set) {
+    if (F8) {
+      // the setmaxnreg split is sized for kLaunchRegs8 registers per thread;
+      // with any other compiled count it might not fit, and the loaders'
+      // setmaxnreg.inc would never return: refuse to launch
+      cudaFuncAttributes fa;
+      if (cudaFuncGetAttributes(&fa, mlp_tc_kernel<MODE, F8>) != cudaSuccess ||
+          fa.numRegs != kLaunchRegs8)
+        return NSVF_ERR_CUDA;
+    }
     if (cudaFuncSetAttribute(mlp_tc_kernel<MODE, F8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return NSVF_ERR_CUDA;
@@ -615,7 +682,7 @@ int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_overri
   int64_t grid = grid_override < 0 ? g_num_sms : (n_tiles + 1) / 2;
   if (grid > g_num_sms) grid = g_num_sms;
   if (grid < 1) grid = 1;
-  mlp_tc_kernel<MODE, F8><<<(int)grid, kThreads, smem, stream>>>(p);
+  mlp_tc_kernel<MODE, F8><<<(int)grid, Cfg<F8>::kThreads, smem, stream>>>(p);
   return nsvf_launch_status();
 }
 
@@ -641,6 +708,7 @@ bool set_weights_fp8(MlpParams &p, const void *const weights[5], const float *co
   for (int l = 1; l < 4; ++l) p.dq[l] = 1.0f / (scales[l - 1] * scales[3 + l - 1]);
   for (int l = 0; l < 3; ++l) p.qs[l] = scales[3 + l];
   p.qs[3] = 1.0f;
+  for (int l = 0; l < 3; ++l) p.dqs[l] = p.dq[l] * p.qs[l];
   return true;
 }
 

@@ -70,6 +70,13 @@ __device__ __forceinline__ uint32_t pack_e4m3x2(float lo, float hi) {
   return (uint32_t)d;
 }
 
+// The same with ReLU applied first (negative inputs become +0).
+__device__ __forceinline__ uint32_t pack_relu_e4m3x2(float lo, float hi) {
+  uint16_t d;
+  asm("cvt.rn.satfinite.relu.e4m3x2.f32 %0, %2, %1;\n" : "=h"(d) : "f"(lo), "f"(hi));
+  return (uint32_t)d;
+}
+
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(

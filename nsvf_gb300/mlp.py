@@ -120,18 +120,29 @@ class TensorCoreMLP:
         return x
 
     def reference_fp8(self, emb):
-        """torch emulation of the FP8 kernel: bf16 input layer, E4M3 (saturating)
-        activations and weights with the per-layer scales for layers 1-3,
-        dequantise + bias + ReLU in FP32, bf16 head."""
+        """torch emulation of the FP8 kernel: bf16 input layer; for layers 0-2
+        the output relu(fmaf(acc, dq*qs, bias*qs)) rounded to saturating E4M3
+        (dq = 1 / (a_scale * w_scale) of the layer, qs = a_scale of the next,
+        all scalars in float32 as the library computes them; fmaf emulated in
+        float64); E4M3 weights; layer 3 relu(fmaf(acc, dq, bias)) in bf16;
+        bf16 head."""
+        import numpy as np
         f = self.fp8
+        f32 = np.float32
         e4 = torch.float8_e4m3fn
-        x = emb.float().to(torch.bfloat16).float()
-        x = x @ self.w[0].float().t()
-        for l in range(1, 4):
-            dq = 1.0 if l == 1 else 1.0 / (f["a_scale"][l - 2] * f["w_scale"][l - 2])
-            x = torch.relu(x * dq + self.b[l - 1]) * f["a_scale"][l - 1]
-            x = x.clamp(-self.E4M3_MAX, self.E4M3_MAX).to(e4).float()
-            x = x @ f["w8"][l - 1].float().t()
-        dq = 1.0 / (f["a_scale"][2] * f["w_scale"][2])
-        x = torch.relu(x * dq + self.b[3]).to(torch.bfloat16).float()
+        ws = [f32(x) for x in f["w_scale"]]
+        as_ = [f32(x) for x in f["a_scale"]]
+        dq = [f32(1.0)] + [f32(f32(1.0) / f32(ws[l - 1] * as_[l - 1])) for l in (1, 2, 3)]
+        qs = as_ + [f32(1.0)]
+        x = emb.float().to(torch.bfloat16).float() @ self.w[0].float().t()
+        for l in range(4):
+            if l < 3:
+                dqs = float(f32(dq[l] * qs[l]))
+                bq = self.b[l] * float(qs[l])
+                y = (x.double() * dqs + bq.double()).float()
+                x = torch.relu(y).clamp(max=self.E4M3_MAX).to(e4).float()
+                x = x @ f["w8"][l].float().t()
+            else:
+                y = (x.double() * float(dq[3]) + self.b[3].double()).float()
+                x = torch.relu(y).to(torch.bfloat16).float()
         return x @ self.w[4].float().t() + self.b[4]
