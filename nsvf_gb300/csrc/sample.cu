@@ -228,6 +228,279 @@ __global__ void __launch_bounds__(kBlock) icdf_compact_kernel(
   if ((overflow || em.pos != em.end) && err) atomicOr(err, 2);
 }
 
+// ------------------------------------------------------------------------
+// Served path, warp per ray. The walk above emits, for a ray with B valid
+// bins (ids before the first -1) and T = ceil(steps) jittered steps at
+// cdf_t = (t + 0.5) * step, this sequence: for each bin b, the steps that
+// land in it, then (when a later step passes the bin's upper CDF bound) the
+// bin's closing segment; after the last valid bin is closed the walk is
+// done; then the tail loop. With sf[b + 1] = #{t : cdf_t <= cdf_hi[b]} (a
+// binary search, cdf_t is increasing) every position is closed-form:
+//   step t in bin b          at t + b,
+//   closing segment of bin b at sf[b + 1] + b,   emitted iff sf[b + 1] < T,
+// and a step's z_low is the previous step's z when that step is in the same
+// bin, else the bin's min depth. So 32 lanes place 32 consecutive samples
+// at once, with the walk's exact FP32 operations, and write them coalesced.
+// The CDF bounds are the walk's sequential FP32 prefix (one lane); the tail
+// loop runs on one lane. Rows with max_hits > kMaxH use the per-thread walk.
+constexpr int kMaxH = 128;
+constexpr int kWarpRays = 8;                 // warps (rays in flight) per block
+
+struct RayTab {
+  float lo[kMaxH], hi[kMaxH], cdf_hi[kMaxH];
+  int32_t id[kMaxH];
+  int sf[kMaxH + 1];
+  int end[kMaxH];
+};
+
+__device__ __forceinline__ float tab_cdf(int t, float step) {
+  return __fmul_rn(__fadd_rn((float)t, 0.5f), step);
+}
+
+// z of step t in bin b (the walk's in-bin placement)
+__device__ __forceinline__ float tab_z(const RayTab &T, int t, int b, float step) {
+  float cl = b > 0 ? T.cdf_hi[b - 1] : 0.0f;
+  float u = __fdiv_rn(__fsub_rn(tab_cdf(t, step), cl), __fsub_rn(T.cdf_hi[b], cl));
+  return __fmaf_rn(u, __fsub_rn(T.hi[b], T.lo[b]), T.lo[b]);
+}
+
+// z_low of bin b's closing segment: its last step's z, or its min depth
+__device__ __forceinline__ float tab_zlow_close(const RayTab &T, int b, float step) {
+  return T.sf[b + 1] > T.sf[b] ? tab_z(T, T.sf[b + 1] - 1, b, step) : T.lo[b];
+}
+
+struct WarpRay {
+  int B, nb, M, total;
+  float step;
+  bool done;
+};
+
+// Builds the ray's table (all 32 lanes; returns the same WarpRay on every
+// lane). B == 0 (an empty first slot) is left to the caller.
+__device__ __forceinline__ WarpRay build_tab(RayTab &T, int H, const int32_t *__restrict__ I,
+                                             const float *__restrict__ lo,
+                                             const float *__restrict__ hi,
+                                             const float *__restrict__ pr, float steps, int lane) {
+  for (int b = lane; b < H; b += 32) { T.id[b] = I[b]; T.lo[b] = lo[b]; T.hi[b] = hi[b]; }
+  __syncwarp();
+  WarpRay w;
+  w.step = __double2float_rn(__ddiv_rn(1.0, (double)steps));
+  w.total = (int)ceilf(steps);
+  int B = H;
+  for (int b0 = 0; b0 < H; b0 += 32) {
+    uint32_t m = __ballot_sync(0xffffffffu, b0 + lane < H && T.id[b0 + lane] == -1);
+    if (m) { B = b0 + __ffs(m) - 1; break; }
+  }
+  w.B = B;
+  if (lane == 0) {
+    float c = pr[0];
+    if (B > 0) T.cdf_hi[0] = c;
+    for (int b = 1; b < B; ++b) { c = __fadd_rn(c, pr[b]); T.cdf_hi[b] = c; }
+    T.sf[0] = 0;
+  }
+  __syncwarp();
+  for (int b = lane; b < B; b += 32) {
+    const float bound = T.cdf_hi[b];
+    int a = 0, e = w.total;
+    while (a < e) {
+      int mid = (a + e) >> 1;
+      if (tab_cdf(mid, w.step) <= bound) a = mid + 1;
+      else e = mid;
+    }
+    T.sf[b + 1] = a;
+  }
+  __syncwarp();
+  int nb = 0;
+  for (int b0 = 0; b0 < B; b0 += 32)
+    nb += __popc(__ballot_sync(0xffffffffu, b0 + lane < B && T.sf[b0 + lane + 1] < w.total));
+  for (int b = lane; b < nb; b += 32) T.end[b] = T.sf[b + 1] + b + 1;
+  __syncwarp();
+  w.nb = nb;
+  w.done = B > 0 && T.sf[B] < w.total;
+  w.M = B > 0 ? T.sf[B] + nb : 0;
+  return w;
+}
+
+// Main-sequence sample j (0 <= j < M): voxel id, depth, distance.
+__device__ __forceinline__ void tab_sample(const RayTab &T, const WarpRay &w, int j, int32_t &id,
+                                           float &t, float &dist) {
+  int a = 0, e = w.nb;                     // b = #{b' < nb : end[b'] <= j}
+  while (a < e) {
+    int mid = (a + e) >> 1;
+    if (T.end[mid] <= j) a = mid + 1;
+    else e = mid;
+  }
+  const int b = a;
+  id = T.id[b];
+  if (b < w.nb && j == T.end[b] - 1) {
+    float zl = tab_zlow_close(T, b, w.step);
+    t = __fmul_rn(__fadd_rn(T.hi[b], zl), 0.5f);
+    dist = __fsub_rn(T.hi[b], zl);
+  } else {
+    const int st = j - b;
+    float z = tab_z(T, st, b, w.step);
+    float zl = st > T.sf[b] ? tab_z(T, st - 1, b, w.step) : T.lo[b];
+    t = __fmul_rn(__fadd_rn(z, zl), 0.5f);
+    dist = __fsub_rn(z, zl);
+  }
+}
+
+// The tail loop of the walk from its end state, calling emit(id, t, dist).
+template <typename Emit>
+__device__ __forceinline__ void tab_tail(const RayTab &T, const WarpRay &w, int H,
+                                         const int32_t *__restrict__ I0,
+                                         const int32_t *__restrict__ pts_all, int64_t nxt,
+                                         Emit &emit) {
+  int bin;
+  float cmax, z_low;
+  if (w.done) {
+    bin = w.B; cmax = T.hi[w.B - 1]; z_low = tab_zlow_close(T, w.B - 1, w.step);
+  } else if (w.total > 0) {
+    bin = w.nb; cmax = T.hi[w.nb]; z_low = tab_z(T, w.total - 1, w.nb, w.step);
+  } else {
+    bin = 0; cmax = T.hi[0]; z_low = T.lo[0];
+  }
+  while (z_low < cmax) {
+    int32_t id;
+    if (bin < H) id = T.id[bin];
+    else id = (nxt >= 0) ? pts_all[nxt * H] : -1;
+    emit(id, __fmul_rn(__fadd_rn(cmax, z_low), 0.5f), __fsub_rn(cmax, z_low));
+    bin++;
+    if (bin >= H || I0[bin] == -1) break;
+    cmax = T.hi[bin];
+    z_low = T.lo[bin];
+  }
+}
+
+struct TailCount {
+  int n;
+  __device__ void operator()(int32_t id, float, float) { n += (id != -1); }
+};
+
+struct TailWrite {
+  int32_t *vox;
+  float4 *xyzd;
+  float *depth;
+  float ox, oy, oz, dx, dy, dz;
+  int64_t pos, end;
+  bool over;
+  __device__ void operator()(int32_t id, float t, float dist) {
+    if (id == -1) return;
+    if (pos >= end) { over = true; return; }
+    vox[pos] = id;
+    xyzd[pos] = make_float4(__fadd_rn(ox, __fmul_rn(dx, t)), __fadd_rn(oy, __fmul_rn(dy, t)),
+                            __fadd_rn(oz, __fmul_rn(dz, t)), fmaxf(dist, 0.0f));
+    depth[pos] = t;
+    ++pos;
+  }
+};
+
+// WRITE = false: count[r] = number of valid samples of row r (rows past the
+// device-side row count get 0). WRITE = true: the samples, compacted at
+// offset[r].
+template <bool WRITE>
+__global__ void __launch_bounds__(32 * kWarpRays) icdf_warp_kernel(
+    int64_t rows, int H, const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
+    const float *__restrict__ max_depth, const float *__restrict__ probs,
+    const float *__restrict__ steps, int64_t K, int64_t C, int64_t N, int64_t G,
+    const int64_t *__restrict__ n_dev, int32_t *__restrict__ count,
+    const float *__restrict__ ray_start, int64_t ray_start_stride,
+    const float *__restrict__ ray_dir, const int64_t *__restrict__ ray_index,
+    const int64_t *__restrict__ offset, int64_t sample_cap, int32_t *__restrict__ vox,
+    float4 *__restrict__ xyzd, float *__restrict__ depth, int32_t *__restrict__ err) {
+  __shared__ RayTab tabs[kWarpRays];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  RayTab &T = tabs[wib];
+  const int64_t cap = rows;
+  dyn_rows(n_dev, cap, rows, K, C, N, G);
+  const int64_t stride = (int64_t)gridDim.x * kWarpRays;
+  for (int64_t r = (int64_t)blockIdx.x * kWarpRays + wib; r < cap; r += stride) {
+    if (r >= rows) {
+      if (!WRITE && lane == 0) count[r] = 0;
+      continue;
+    }
+    int64_t tail, nxt;
+    icdf_rows(r, K, C, N, G, tail, nxt);
+    const int32_t *I = pts_idx + r * H;
+    WarpRay w = build_tab(T, H, I, min_depth + r * H, max_depth + r * H, probs + r * H,
+                          steps[r], lane);
+    if (w.B == 0) {
+      // an empty first slot: the per-thread walk on lane 0
+      if (lane == 0) {
+        if (!WRITE) {
+          CountEmit em{0};
+          icdf_walk(H, I, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H, max_depth + r * H,
+                    probs + r * H, steps[r], nullptr, 0, -1.0f, em);
+          count[r] = em.n;
+        } else {
+          int64_t rr = ray_index ? ray_index[r] : r;
+          const float *o = ray_start + rr * ray_start_stride;
+          int64_t e = offset[r + 1] < sample_cap ? offset[r + 1] : sample_cap;
+          CompactEmit em{vox, xyzd, depth, o[0], o[1], o[2], ray_dir[rr * 3], ray_dir[rr * 3 + 1],
+                         ray_dir[rr * 3 + 2], offset[r] < e ? offset[r] : e, e};
+          bool over = icdf_walk(H, I, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H,
+                                max_depth + r * H, probs + r * H, steps[r], nullptr, 0, -1.0f,
+                                em);
+          if ((over || em.pos != offset[r + 1]) && err) atomicOr(err, 2);
+        }
+      }
+      __syncwarp();
+      continue;
+    }
+    if (!WRITE) {
+      if (lane == 0) {
+        TailCount tc{0};
+        tab_tail(T, w, H, pts_idx + tail * H, pts_idx, nxt, tc);
+        count[r] = w.M + tc.n;
+      }
+    } else {
+      const int64_t rr = ray_index ? ray_index[r] : r;
+      const float *o = ray_start + rr * ray_start_stride;
+      const float ox = o[0], oy = o[1], oz = o[2];
+      const float dx = ray_dir[rr * 3], dy = ray_dir[rr * 3 + 1], dz = ray_dir[rr * 3 + 2];
+      const int64_t base = offset[r], lim = offset[r + 1] < sample_cap ? offset[r + 1] : sample_cap;
+      for (int j0 = 0; j0 < w.M; j0 += 32) {
+        const int j = j0 + lane;
+        if (j < w.M) {
+          int32_t id;
+          float t, dist;
+          tab_sample(T, w, j, id, t, dist);
+          const int64_t pos = base + j;
+          if (pos < lim) {
+            vox[pos] = id;
+            xyzd[pos] = make_float4(__fadd_rn(ox, __fmul_rn(dx, t)), __fadd_rn(oy, __fmul_rn(dy, t)),
+                                    __fadd_rn(oz, __fmul_rn(dz, t)), fmaxf(dist, 0.0f));
+            depth[pos] = t;
+          }
+        }
+      }
+      if (lane == 0) {
+        TailWrite tw{vox, xyzd, depth, ox, oy, oz, dx, dy, dz, base + w.M, lim, false};
+        if (base + w.M > lim) tw.over = true;
+        tab_tail(T, w, H, pts_idx + tail * H, pts_idx, nxt, tw);
+        if ((tw.over || tw.pos != offset[r + 1] || offset[r + 1] > sample_cap) && err)
+          atomicOr(err, 2);
+      }
+    }
+    __syncwarp();                          // the table is rebuilt for the next ray
+  }
+}
+
+// Blocks for the warp-per-ray kernels: enough warps to cover the rows (or
+// the capacity), at most 16 blocks of 8 warps per SM (grid-stride beyond).
+int warp_grid(int64_t rows) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  int64_t want = (rows + kWarpRays - 1) / kWarpRays;
+  int64_t lim = (int64_t)sms * 16;
+  return (int)(want < 1 ? 1 : (want < lim ? want : lim));
+}
+
 // Uniform sampler (fairnr/clib/src/sample_gpu.cu:15-106): merge interval
 // starts, interval ends and jittered steps into one sorted depth list in the
 // output row, then turn it into midpoints/lengths and keep those inside a
@@ -319,8 +592,13 @@ int nsvf_sample_count(int64_t rows, int max_hits, const int32_t *pts_idx, const 
   if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !count) return NSVF_ERR_INVALID;
   int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
   if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
-  icdf_count_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count);
+  if (max_hits <= kMaxH)
+    icdf_warp_kernel<false><<<warp_grid(rows), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+        rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count,
+        nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr);
+  else
+    icdf_count_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+        rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count);
   return nsvf_launch_status();
 }
 
@@ -338,10 +616,16 @@ int nsvf_sample_compact(int64_t rows, int max_hits, const int32_t *pts_idx,
     return NSVF_ERR_INVALID;
   int64_t K = layout[0], C = layout[1], N = layout[2], G = layout[3];
   if (K < 1 || C < 1 || N < rows || G < 1 || G * K < N) return NSVF_ERR_INVALID;
-  icdf_compact_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, ray_start,
-      ray_start_stride, ray_dir, nullptr, offset, INT64_MAX, voxel, (float4 *)xyz_dist, depth,
-      err);
+  if (max_hits <= kMaxH)
+    icdf_warp_kernel<true><<<warp_grid(rows), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+        rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, nullptr,
+        ray_start, ray_start_stride, ray_dir, nullptr, offset, INT64_MAX, voxel,
+        (float4 *)xyz_dist, depth, err);
+  else
+    icdf_compact_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+        rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, ray_start,
+        ray_start_stride, ray_dir, nullptr, offset, INT64_MAX, voxel, (float4 *)xyz_dist, depth,
+        err);
   return nsvf_launch_status();
 }
 
@@ -351,9 +635,14 @@ int nsvf_sample_count_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_h
   if (rows_cap < 0 || max_hits < 1 || !n_rows_dev) return NSVF_ERR_INVALID;
   if (rows_cap == 0) return NSVF_OK;
   if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !count) return NSVF_ERR_INVALID;
-  icdf_count_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
-      count);
+  if (max_hits <= kMaxH)
+    icdf_warp_kernel<false><<<warp_grid(rows_cap), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+        count, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr);
+  else
+    icdf_count_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+        count);
   return nsvf_launch_status();
 }
 
@@ -371,10 +660,16 @@ int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max
   if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !ray_start || !ray_dir ||
       !offset || !voxel || !xyz_dist || !depth || (((uintptr_t)xyz_dist) & 15))
     return NSVF_ERR_INVALID;
-  icdf_compact_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
-      ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
-      (float4 *)xyz_dist, depth, err);
+  if (max_hits <= kMaxH)
+    icdf_warp_kernel<true><<<warp_grid(rows_cap), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+        nullptr, ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
+        (float4 *)xyz_dist, depth, err);
+  else
+    icdf_compact_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+        ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
+        (float4 *)xyz_dist, depth, err);
   return nsvf_launch_status();
 }
 

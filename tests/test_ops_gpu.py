@@ -327,3 +327,86 @@ def test_full_frame_properties(cuda):
     ref = cpu.sort_hits(*ref)
     assert np.array_equal(_np(idx)[0][sel], ref[0][0])
     assert np.array_equal(lo_np[sel], ref[1][0])
+
+
+def _icdf_rows(case, cuda):
+    """(pts_idx, min_depth, max_depth) rows for the sampling parity test:
+    sorted SVO hit rows of a scene, or synthetic sorted rows (1,000 rows,
+    several of the reference wrapper's 200-row blocks; H = 160 exercises the
+    per-thread walk used beyond 128 slots)."""
+    from nsvf_gb300 import ext, geometry, scenes
+    if case == "scene":
+        p, vs = scenes.scene_shell(1.0 / 32)
+        cen, chi = geometry.build_easy_octree(torch.from_numpy(p), vs / 2)
+        o, d = _random_rays(6000, seed=21)
+        idx, lo, hi, hits = ext.svo_intersect_sorted(_t(o[None], cuda), _t(d[None], cuda),
+                                                     cen[None].to(cuda), chi[None].to(cuda), vs, 64)
+        h = hits[0].bool()
+        return idx[0][h].contiguous(), lo[0][h].contiguous(), hi[0][h].contiguous(), vs / 8, \
+            _t(o, cuda)[h].contiguous(), _t(d, cuda)[h].contiguous()
+    H = 20 if case == "synthetic" else 160
+    rng = np.random.RandomState(7 if case == "synthetic" else 8)
+    n = 1000
+    I = np.full((n, H), -1, np.int32)
+    lo = np.full((n, H), 10000.0, np.float32)
+    hi = np.full((n, H), 10000.0, np.float32)
+    for r in range(n):
+        k = rng.randint(1, H + 1)
+        t = np.sort(rng.uniform(0.5, 4.0, size=2 * k)).astype(np.float32)
+        I[r, :k] = rng.randint(0, 5000, size=k)
+        lo[r, :k], hi[r, :k] = t[0::2], t[1::2]
+        if rng.rand() < 0.1:
+            hi[r, :k] = lo[r, :k]                 # rays of zero length inside voxels
+    o = rng.normal(size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    return _t(I, cuda), _t(lo, cuda), _t(hi, cuda), 0.02, _t(o, cuda), _t(d, cuda)
+
+
+@pytest.mark.parametrize("case", ["scene", "synthetic", "synthetic_h160"])
+def test_sample_compact_matches_inverse_cdf_op(cuda, case):
+    """The served path's sample pass (nsvf_sample_count + nsvf_sample_compact,
+    warp per ray; per-thread walk beyond 128 slots) gives exactly the valid
+    samples of the reference op's padded rows (deterministic jitter, the
+    wrapper's 200-block layout), in row order: ids, depths, clamped
+    distances and positions o + d t, bit for bit."""
+    import ctypes
+    from nsvf_gb300 import clib, ext
+    from nsvf_gb300._lib import LIB, check
+    I, L, Hh, step, ro, rd = _icdf_rows(case, cuda)
+    n, H = I.shape
+    d = (Hh - L).masked_fill(I.eq(-1), 0)
+    tot = d.sum(-1, keepdim=True)
+    keep = tot[:, 0] > 0
+    I, L, Hh, ro, rd, d, tot = I[keep], L[keep], Hh[keep], ro[keep], rd[keep], d[keep], tot[keep]
+    n = I.shape[0]
+    probs = (d / tot).contiguous()
+    steps = (tot[:, 0] / step).contiguous()
+    si, sd, ss = clib.inverse_cdf_sampling(I, L, Hh, probs, steps, -1, True)
+    valid = si.ne(-1)
+    layout = torch.tensor(clib.inverse_cdf_layout(n), dtype=torch.int64)
+    stream = ext.ctypes_stream(cuda)
+    count = torch.empty(n, dtype=torch.int32, device=cuda)
+    check(LIB.nsvf_sample_count(n, H, I.data_ptr(), L.data_ptr(), Hh.data_ptr(), probs.data_ptr(),
+                                steps.data_ptr(), layout.data_ptr(), count.data_ptr(), stream),
+          "sample_count")
+    assert torch.equal(count.long(), valid.sum(1))
+    offset = torch.zeros(n + 1, dtype=torch.int64, device=cuda)
+    torch.cumsum(count, 0, out=offset[1:])
+    ns = int(offset[-1].item())
+    vox = torch.empty(ns, dtype=torch.int32, device=cuda)
+    xyzd = torch.empty(ns, 4, device=cuda)
+    depth = torch.empty(ns, device=cuda)
+    err = ext.error_word(cuda)
+    check(LIB.nsvf_sample_compact(n, H, I.data_ptr(), L.data_ptr(), Hh.data_ptr(),
+                                  probs.data_ptr(), steps.data_ptr(), layout.data_ptr(),
+                                  ro.data_ptr(), 3, rd.data_ptr(), offset.data_ptr(),
+                                  vox.data_ptr(), xyzd.data_ptr(), depth.data_ptr(),
+                                  err.data_ptr(), stream), "sample_compact")
+    ext.check_errors(cuda)
+    assert ns == int(valid.sum()) > 1000
+    assert torch.equal(vox, si[valid].int())
+    assert torch.equal(depth, sd[valid])
+    assert torch.equal(xyzd[:, 3], ss[valid].clamp(min=0))
+    row = torch.arange(n, device=cuda)[:, None].expand_as(si)[valid]
+    xyz = ro[row] + rd[row] * sd[valid][:, None]
+    assert torch.equal(xyzd[:, :3], xyz)
