@@ -418,6 +418,9 @@ def run_ours(a):
         dist.barrier()
     e2e_times = []
     h2d = d2h = 0
+    # results land in pinned host buffers (as a serving front end would keep)
+    col_h = torch.empty(a.size * a.size, 3, dtype=torch.float32).pin_memory()
+    dep_h = torch.empty(a.size * a.size, dtype=torch.float32).pin_memory()
     for i in range(a.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -426,8 +429,8 @@ def run_ours(a):
         rs_d = rst.to(dev, non_blocking=True)
         rd_d = rdt.to(dev, non_blocking=True)
         out = step(rs_d, rd_d)
-        col = out["colors"].reshape(-1, 3).to("cpu")
-        dep = out["depths"].reshape(-1).to("cpu")
+        col = col_h.copy_(out["colors"].reshape(-1, 3), non_blocking=True)
+        dep = dep_h.copy_(out["depths"].reshape(-1), non_blocking=True)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
         h2d = rst.numel() * 4 + rdt.numel() * 4

@@ -51,7 +51,14 @@ struct Cfg {
   static constexpr int kMmaWarp = F8 ? kLoaderWarp0 + 8 : kEpiWarps;
   static constexpr int kThreads = F8 ? 24 * 32 : 17 * 32;
   static constexpr uint32_t kSlotCols = F8 ? 128u : 256u;
-  static constexpr uint32_t kHeadCol = F8 ? 0u : 128u;
+  // TMEM column of slot g's (sigma, rgb) head output. The MMA lane issues
+  // the slot's next tile's first layer without waiting for the epilogue to
+  // read the head, so the head must not share columns with it: BF16 uses the
+  // slot's spare columns [256 g + 128, + 16); FP8 has none and uses columns
+  // 384 + 16 g (after the three 128-column slots).
+  __device__ static constexpr uint32_t head_col(int g) {
+    return F8 ? 384u + 16u * (uint32_t)g : 256u * (uint32_t)g + 128u;
+  }
   static constexpr int kHidBytes = F8 ? HID * HID : HID * HID * 2;  // one hidden weight matrix
 };
 
@@ -461,7 +468,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
                   issue_layer(d, S.ah[g], reinterpret_cast<const __nv_bfloat16 *>(S.wh[layer - 1]),
                               HID, HID);
               } else {
-                issue_layer(d + C::kHeadCol, S.ah[g], S.w4, HID, NOUT);
+                issue_layer(tmem + C::head_col(g), S.ah[g], S.w4, HID, NOUT);
               }
               mma_commit(&S.mma_done[g][layer]);
             }
@@ -599,7 +606,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) { ok = false; break; }
       fence_after_sync();
       float v[16];
-      tmem_ld16(tl + C::kHeadCol, v);
+      tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + C::head_col(g), v);
       tmem_wait_ld();
       fence_before_sync();
       float sigma = v[0] + S.bias4[0];
