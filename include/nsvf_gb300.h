@@ -268,6 +268,19 @@ int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *fi
 int nsvf_pinhole_rays(int64_t n, const float *cam, float *ray_start, float *ray_dir,
                       void *stream);
 
+/* camera_rays: n rays in the reference's camera convention, the eval path of
+ * ImageReader (fairnr/modules/reader.py:92-119) with get_uv
+ * (fairnr/data/data_utils.py:57-65) and get_ray_direction
+ * (fairnr/data/geometry.py:116-122). cam (device, 20 floats) = fx, fy, cx,
+ * cy, inv_RT (3 x 4 camera-to-world, row-major), W / w, H / h (an H x W
+ * image read at h x w), w, first pixel. Ray t is pixel first + t of the
+ * w-wide grid, row-major, at integer pixel coordinates scaled to the full
+ * image. ray_start[n, 3] = inv_RT's translation, ray_dir[n, 3] =
+ * (rt - ray_start) / (|rt - ray_start| + 1e-8) with rt the pixel's point at
+ * depth 1. */
+int nsvf_camera_rays(int64_t n, const float *cam, float *ray_start, float *ray_dir,
+                     void *stream);
+
 /* compact_hits: given hits[n] (uint8) and scan = their inclusive prefix sum
  * (int32), writes the hit rays' indices in order to pix and their number to
  * *n_hit (both on the device). */

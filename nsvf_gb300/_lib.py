@@ -50,6 +50,7 @@ def _load():
         "nsvf_sample_compact": ([i64, i32, P, P, P, P, P, P, P, i64, P, P, P, P, P, P, P], i32),
         "nsvf_composite_segments": ([i64, P, P, P, P, P, f32, P, f32, P, P, P, i32, P], i32),
         "nsvf_pinhole_rays": ([i64, P, P, P, P], i32),
+        "nsvf_camera_rays": ([i64, P, P, P, P], i32),
         "nsvf_compact_hits": ([i64, P, P, P, P, P], i32),
         "nsvf_gather_probs": ([i64, P, i32, f32, P, P, P, P, P, P, P, P, P, P], i32),
         "nsvf_sample_count_dev": ([i64, P, i32, P, P, P, P, P, P, P], i32),
@@ -87,7 +88,7 @@ def exported_symbols():
         "nsvf_trilinear_embed", "nsvf_trilinear_embed_backward", "nsvf_composite",
         "nsvf_composite_backward", "nsvf_mlp_forward_bf16", "nsvf_sample_count",
         "nsvf_sample_compact", "nsvf_composite_segments", "nsvf_field_samples_bf16",
-        "nsvf_prune_scores_bf16", "nsvf_pinhole_rays", "nsvf_compact_hits", "nsvf_gather_probs",
-        "nsvf_sample_count_dev", "nsvf_sample_compact_dev", "nsvf_composite_segments_dev",
+        "nsvf_prune_scores_bf16", "nsvf_pinhole_rays", "nsvf_camera_rays", "nsvf_compact_hits",
+        "nsvf_gather_probs", "nsvf_sample_count_dev", "nsvf_sample_compact_dev", "nsvf_composite_segments_dev",
         "nsvf_field_samples_bf16_dev", "nsvf_field_samples_fp8", "nsvf_field_samples_fp8_dev",
     ]

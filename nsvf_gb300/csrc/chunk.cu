@@ -36,6 +36,41 @@ __global__ void pinhole_kernel(int64_t n, const float *__restrict__ cam, float *
   rd[t * 3 + 0] = x * inv; rd[t * 3 + 1] = y * inv; rd[t * 3 + 2] = z * inv;
 }
 
+// Rays in the reference's camera convention: ImageReader's eval path
+// (fairnr/modules/reader.py:92-119) with get_uv (fairnr/data/data_utils.py:
+// 57-65) and get_ray_direction (fairnr/data/geometry.py:116-122).
+// cam[20] = fx, fy, cx, cy, inv_RT (3 x 4 camera-to-world, row-major),
+// su = W / w, sv = H / h (image read at w x h), w, first pixel. Ray t is
+// pixel p = first + t of the w-wide grid (row-major): u = (p % w) su,
+// v = (p / w) sv (integer pixel coordinates, no half-pixel offset); the
+// point at depth 1 is rt = inv_RT ((u - cx) / fx, (v - cy) / fy, 1, 1), the
+// origin is inv_RT's translation and the direction is
+// (rt - origin) / (|rt - origin| + 1e-8).
+__global__ void camera_rays_kernel(int64_t n, const float *__restrict__ cam,
+                                   float *__restrict__ ro, float *__restrict__ rd) {
+  int64_t t = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (t >= n) return;
+  const float fx = cam[0], fy = cam[1], cx = cam[2], cy = cam[3];
+  const float *M = cam + 4;
+  const float su = cam[16], sv = cam[17];
+  int64_t w = (int64_t)cam[18];
+  if (w < 1) w = 1;
+  const int64_t p = (int64_t)cam[19] + t;
+  const float u = (float)(p % w) * su, v = (float)(p / w) * sv;
+  const float x = (u - cx) / fx, y = (v - cy) / fy;
+  float d[3];
+  for (int k = 0; k < 3; ++k) {
+    const float *m = M + 4 * k;
+    float pk = m[0] * x + m[1] * y + m[2] + m[3];
+    d[k] = pk - m[3];
+  }
+  const float l = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) + 1e-8f;
+  for (int k = 0; k < 3; ++k) {
+    ro[t * 3 + k] = M[4 * k + 3];
+    rd[t * 3 + k] = d[k] / l;
+  }
+}
+
 // scan = inclusive prefix sum of hits: hit ray r goes to pix[scan[r] - 1].
 __global__ void compact_hits_kernel(int64_t n, const uint8_t *__restrict__ hits,
                                     const int32_t *__restrict__ scan, int64_t *__restrict__ pix,
@@ -92,6 +127,16 @@ int nsvf_compact_hits(int64_t n, const uint8_t *hits, const int32_t *scan, int64
   if (n < 1 || !hits || !scan || !pix || !n_hit) return NSVF_ERR_INVALID;
   compact_hits_kernel<<<nsvf_grid(n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(n, hits, scan, pix,
                                                                                n_hit);
+  return nsvf_launch_status();
+}
+
+int nsvf_camera_rays(int64_t n, const float *cam, float *ray_start, float *ray_dir,
+                     void *stream) {
+  if (n < 0 || !cam) return NSVF_ERR_INVALID;
+  if (n == 0) return NSVF_OK;
+  if (!ray_start || !ray_dir) return NSVF_ERR_INVALID;
+  camera_rays_kernel<<<nsvf_grid(n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(n, cam, ray_start,
+                                                                               ray_dir);
   return nsvf_launch_status();
 }
 

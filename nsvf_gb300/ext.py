@@ -289,3 +289,25 @@ def build_octree(center, points, depth):
         check(int(n2), "build_octree")
     dev = points.device
     return torch.from_numpy(cen).to(dev), torch.from_numpy(chi).to(dev)
+
+
+def camera_rays(intrinsics, inv_RT, H, W, h=None, w=None, first=0, n=None, device=None):
+    """Rays of an H x W image read at h x w, in the reference's camera
+    convention (ImageReader eval path: get_uv, get_ray_direction), on the
+    GPU: intrinsics (fx, fy, cx, cy), inv_RT camera-to-world [3 or 4, 4].
+    Returns ray_start [n, 3] and ray_dir [n, 3] for pixels first..first+n-1
+    of the w-wide grid (all by default). Same kernel as nsvf_camera_rays."""
+    h = H if h is None else h
+    w = W if w is None else w
+    n = h * w - first if n is None else n
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    M = torch.as_tensor(inv_RT, dtype=torch.float32).reshape(-1, 4)[:3].reshape(-1)
+    fx, fy, cx, cy = [float(x) for x in intrinsics]
+    cam = torch.cat([torch.tensor([fx, fy, cx, cy]), M.cpu(),
+                     torch.tensor([float(W / w), float(H / h), float(w), float(first)])]).to(dev)
+    ro = torch.empty(n, 3, dtype=torch.float32, device=dev)
+    rd = torch.empty(n, 3, dtype=torch.float32, device=dev)
+    with _timed("camera_rays", dev):
+        check(LIB.nsvf_camera_rays(n, cam.data_ptr(), ro.data_ptr(), rd.data_ptr(),
+                                   ctypes_stream(dev)), "camera_rays")
+    return ro, rd

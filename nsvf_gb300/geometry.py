@@ -119,3 +119,35 @@ def voxel_corner_table(points, voxel_size):
     keys0 = offset_points(coords, 1.0).reshape(-1, 3)
     keys, feats = torch.unique(keys0, dim=0, sorted=True, return_inverse=True)
     return keys, feats.reshape(-1, 8)
+
+
+def get_uv(H, W, h, w):
+    """Pixel coordinates of an H x W image read at h x w: uv [2, h, w]
+    float32 (u = column, v = row, integer positions scaled by W / w and
+    H / h) and the ratios (fairnr/data/data_utils.py:57-65)."""
+    v, u = np.mgrid[0:h, 0:w]
+    uv = np.stack([u, v]).astype(np.float32)
+    uv[0] = uv[0] * float(W / w)
+    uv[1] = uv[1] * float(H / h)
+    return uv, [float(H / h), float(W / w)]
+
+
+def get_ray_direction(ray_start, uv, intrinsics, inv_RT, depths=None):
+    """Unit ray directions [3, N] through pixels uv [2, N]: the point at
+    `depths` (default 1) in camera space, (u - cx) / fx, (v - cy) / fy,
+    mapped to the world by inv_RT [4, 4], minus ray_start [3], normalised
+    with the reference's + 1e-8 (fairnr/data/geometry.py:116-122). intrinsics
+    is a [4, 4] or [3, 3] matrix (fx, fy on the diagonal, cx, cy in the last
+    column) or (fx, fy, cx, cy)."""
+    z = 1 if depths is None else depths
+    K = torch.as_tensor(intrinsics)
+    if K.dim() == 2:
+        fx, fy, cx, cy = K[0, 0], K[1, 1], K[0, 2], K[1, 2]
+    else:
+        fx, fy, cx, cy = K[0], K[1], K[2], K[3]
+    x = (uv[0] - cx) / fx * z
+    y = (uv[1] - cy) / fy * z
+    cam = torch.stack([x, y, torch.ones_like(x) * z, torch.ones_like(x)])
+    world = torch.matmul(inv_RT, cam)[:3]
+    d = world - ray_start[:, None]
+    return d / (d.norm(p=2, dim=0, keepdim=True) + 1e-8)

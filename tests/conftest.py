@@ -36,6 +36,11 @@ def golden_prune():
 
 
 @pytest.fixture(scope="session")
+def golden_next():
+    return dict(np.load(os.path.join(GOLDEN, "golden_next.npz")))
+
+
+@pytest.fixture(scope="session")
 def cuda():
     import torch
     if not torch.cuda.is_available():

@@ -1,0 +1,106 @@
+"""The steps either side of the rendering path, against fixtures made by the
+reference's own code (tests/golden/make_golden_next.py):
+
+* ray generation in the reference's camera convention: get_uv and
+  get_ray_direction (torch, CPU) and the nsvf_camera_rays kernel (GPU);
+* voxel splitting with embedding re-interpolation (SparseVoxelEncoder.
+  splitting), on the CPU;
+* the renderer's early termination (raymarching_tolerance: the column-chunk
+  loop stops evaluating rays whose accumulated free energy passed -log tol),
+  on the GPU: the same field evaluations ('ae') and the same image.
+
+Tolerances: ray directions 2e-6 (unit vectors; the reference's 4x4 matmul
+and norm sum in a different order); splitting: centres and corner ids exact,
+embeddings 1e-6; early-terminated render 2e-4 (the FP32 compositing kernels
+against the reference's torch cumsum, as for the full render)."""
+import argparse
+import os
+import tempfile
+
+import numpy as np
+import pytest
+import torch
+
+
+def _encoder(golden, dev):
+    from nsvf_gb300.encoder import SparseVoxelEncoder
+    g = golden
+    path = tempfile.mktemp(suffix=".txt")
+    np.savetxt(path, np.array([[-1, -1, -1, 1, 1, 1, float(g["voxel_size"])]]))
+    args = argparse.Namespace(voxel_path=None, initial_boundingbox=path,
+                              voxel_size=float(g["voxel_size"]), max_hits=20,
+                              raymarching_stepsize_ratio=0.125, voxel_embed_dim=32,
+                              use_octree=True, deterministic_step=True)
+    enc = SparseVoxelEncoder(args)
+    os.unlink(path)
+    enc.keep.copy_(torch.from_numpy(g["keep"]))
+    enc.values.weight.data.copy_(torch.from_numpy(g["embed"][: enc.values.weight.shape[0]]))
+    return enc.to(dev).eval()
+
+
+def test_get_uv_and_ray_direction_match_reference(golden_next):
+    from nsvf_gb300 import geometry
+    g = golden_next
+    H, W, h, w = [int(x) for x in g["rays_hw"]]
+    uv, ratio = geometry.get_uv(H, W, h, w)
+    assert np.array_equal(uv.reshape(2, -1), g["rays_uv"])
+    assert ratio == [H / h, W / w]
+    inv_RT = torch.from_numpy(g["rays_inv_RT"])
+    fx, fy, cx, cy = [float(x) for x in g["rays_intrinsics"]]
+    K = torch.eye(4)
+    K[0, 0], K[1, 1], K[0, 2], K[1, 2] = fx, fy, cx, cy
+    d = geometry.get_ray_direction(inv_RT[:3, 3], torch.from_numpy(uv.reshape(2, -1)), K, inv_RT)
+    np.testing.assert_allclose(d.t().numpy(), g["rays_dir"], atol=2e-6)
+
+
+def test_splitting_matches_reference(golden, golden_next):
+    g, n = golden, golden_next
+    enc = _encoder(g, "cpu")
+    enc.splitting()
+    assert np.array_equal(enc.points.numpy(), n["split_points"])
+    assert np.array_equal(enc.feats.numpy(), n["split_feats"])
+    assert int(enc.num_keys) == int(n["split_num_keys"])
+    assert np.array_equal(enc.keep.numpy(), n["split_keep"])
+    np.testing.assert_allclose(enc.values.weight.detach().numpy(), n["split_values"], atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_camera_rays_kernel_matches_reference(golden_next, cuda):
+    from nsvf_gb300 import ext
+    g = golden_next
+    H, W, h, w = [int(x) for x in g["rays_hw"]]
+    ro, rd = ext.camera_rays(g["rays_intrinsics"], g["rays_inv_RT"], H, W, h, w, device=cuda)
+    np.testing.assert_allclose(rd.cpu().numpy(), g["rays_dir"], atol=2e-6)
+    assert np.array_equal(ro.cpu().numpy(), np.broadcast_to(g["rays_start"], ro.shape))
+    # a chunk of the same frame: pixels 100..299
+    ro2, rd2 = ext.camera_rays(g["rays_intrinsics"], g["rays_inv_RT"], H, W, h, w, first=100, n=200,
+                               device=cuda)
+    assert torch.equal(rd2, rd[100:300])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tol", [0.01, 0.5])
+def test_early_termination_matches_reference(golden, golden_next, cuda, tol):
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.renderer import VolumeRenderer
+    g, n = golden, golden_next
+    enc = _encoder(g, cuda)
+    st = enc.precompute(id=None)
+    field = StandInField(weights=[(torch.from_numpy(g["W%d" % i]), torch.from_numpy(g["b%d" % i]))
+                                  for i in range(5)]).to(cuda).eval()
+    hit = g["svo_hits"][0]
+    N = int(hit.sum())
+    rs = torch.from_numpy(g["ray_start"]).to(cuda).reshape(1, 3).expand(N, 3)
+    rd = torch.from_numpy(g["ray_dir"][hit]).to(cuda)
+    samples = {k: torch.from_numpy(g["svo_det_%s" % k]).to(cuda)
+               for k in ["sampled_point_depth", "sampled_point_distance", "sampled_point_voxel_idx"]}
+    ren = VolumeRenderer(argparse.Namespace(chunk_size=1, raymarching_tolerance=tol)).eval()
+    with torch.no_grad():
+        out = ren(enc, field, rs, rd, samples, st)
+    tag = "es%g" % tol
+    assert int(out["ae"]) == int(n["%s_ae" % tag])
+    for k in ["colors", "depths", "missed"]:
+        np.testing.assert_allclose(out[k].cpu().numpy(), n["%s_%s" % (tag, k)], atol=2e-4)
+    np.testing.assert_allclose(out["probs"].cpu().numpy(), n["%s_probs" % tag], atol=2e-4)
+    # and it does stop early: fewer evaluations than valid samples
+    assert int(out["ae"]) < int((g["svo_det_sampled_point_voxel_idx"] != -1).sum())
