@@ -58,6 +58,43 @@ __device__ __forceinline__ bool nsvf_slab(float ox, float oy, float oz, float ix
   return !(lo > hi);
 }
 
+// nsvf_slab for a ray whose direction has no zero component (every
+// reciprocal finite and nonzero), with the same result bit for bit and about
+// half the compare/select work. s = +1 where the reciprocal is >= 0, else -1.
+//  * No NaN can occur, and for each axis rounding is monotone, so
+//    fl(fl(c - h) - o) * inv <= fl(fl(c + h) - o) * inv when inv > 0 (and >=
+//    when inv < 0): the reference's swap is decided by the sign alone. near =
+//    fl(c - s h) and far = fl(c + s h) are the reference's bounds, swapped
+//    when inv < 0 (s h is exact).
+//  * lo only grows from +0 and is never -0; max(lo, l + 0) equals
+//    (l > lo ? l : lo) for every non-NaN l (l + 0 turns -0 into +0).
+//  * hi keeps the compare/select: a -0 that becomes hi must stay -0.
+__device__ __forceinline__ bool nsvf_slab_fast(float ox, float oy, float oz, float ix, float iy,
+                                               float iz, float sx, float sy, float sz, float cx,
+                                               float cy, float cz, float h, float &t_lo,
+                                               float &t_hi) {
+  float lo = 0.0f, hi = 100000.0f;
+  float l, u, sh;
+  sh = __fmul_rn(sx, h);
+  l = __fmul_rn(__fsub_rn(__fsub_rn(cx, sh), ox), ix);
+  u = __fmul_rn(__fsub_rn(__fadd_rn(cx, sh), ox), ix);
+  lo = fmaxf(lo, __fadd_rn(l, 0.0f));
+  hi = (u < hi) ? u : hi;
+  sh = __fmul_rn(sy, h);
+  l = __fmul_rn(__fsub_rn(__fsub_rn(cy, sh), oy), iy);
+  u = __fmul_rn(__fsub_rn(__fadd_rn(cy, sh), oy), iy);
+  lo = fmaxf(lo, __fadd_rn(l, 0.0f));
+  hi = (u < hi) ? u : hi;
+  sh = __fmul_rn(sz, h);
+  l = __fmul_rn(__fsub_rn(__fsub_rn(cz, sh), oz), iz);
+  u = __fmul_rn(__fsub_rn(__fadd_rn(cz, sh), oz), iz);
+  lo = fmaxf(lo, __fadd_rn(l, 0.0f));
+  hi = (u < hi) ? u : hi;
+  t_lo = lo;
+  t_hi = hi;
+  return !(lo > hi);
+}
+
 // Correctly rounded reciprocal (the reference uses the approximate
 // __fdividef(1, d); see the note in include/nsvf_gb300.h).
 __device__ __forceinline__ float nsvf_rcp(float d) { return __frcp_rn(d); }

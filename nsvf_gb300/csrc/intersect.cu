@@ -41,6 +41,9 @@ __global__ void __launch_bounds__(kRayBlock) aabb_kernel(
     ix = nsvf_rcp(ray_dir[r * 3 + 0]); iy = nsvf_rcp(ray_dir[r * 3 + 1]);
     iz = nsvf_rcp(ray_dir[r * 3 + 2]);
   }
+  const bool fast = isfinite(ix) && isfinite(iy) && isfinite(iz);
+  const float sx = ix >= 0.0f ? 1.0f : -1.0f, sy = iy >= 0.0f ? 1.0f : -1.0f,
+              sz = iz >= 0.0f ? 1.0f : -1.0f;
   int cnt = 0;
   int32_t *I = idx + r * n_max;
   float *LO = min_depth + r * n_max, *HI = max_depth + r * n_max;
@@ -52,7 +55,12 @@ __global__ void __launch_bounds__(kRayBlock) aabb_kernel(
     if (live) {
       for (int k = 0; k < tile && cnt < n_max; ++k) {
         float lo, hi;
-        if (nsvf_slab(ox, oy, oz, ix, iy, iz, sc[k * 3], sc[k * 3 + 1], sc[k * 3 + 2], hv, lo, hi)) {
+        const bool hit =
+            fast ? nsvf_slab_fast(ox, oy, oz, ix, iy, iz, sx, sy, sz, sc[k * 3], sc[k * 3 + 1],
+                                  sc[k * 3 + 2], hv, lo, hi)
+                 : nsvf_slab(ox, oy, oz, ix, iy, iz, sc[k * 3], sc[k * 3 + 1], sc[k * 3 + 2], hv,
+                             lo, hi);
+        if (hit) {
           I[cnt] = base + k; LO[cnt] = lo; HI[cnt] = hi; ++cnt;
         }
       }
@@ -214,6 +222,15 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   const float ox = ray_start[rr * 3 + 0], oy = ray_start[rr * 3 + 1], oz = ray_start[rr * 3 + 2];
   const float ix = nsvf_rcp(ray_dir[rr * 3 + 0]), iy = nsvf_rcp(ray_dir[rr * 3 + 1]),
               iz = nsvf_rcp(ray_dir[rr * 3 + 2]);
+  // the compare/select-light slab test for rays without a zero direction
+  // component (the same on the group's 8 lanes)
+  const bool fast = isfinite(ix) && isfinite(iy) && isfinite(iz);
+  const float sx = ix >= 0.0f ? 1.0f : -1.0f, sy = iy >= 0.0f ? 1.0f : -1.0f,
+              sz = iz >= 0.0f ? 1.0f : -1.0f;
+  auto slab = [&](float cx, float cy, float cz, float h, float &lo, float &hi) {
+    return fast ? nsvf_slab_fast(ox, oy, oz, ix, iy, iz, sx, sy, sz, cx, cy, cz, h, lo, hi)
+                : nsvf_slab(ox, oy, oz, ix, iy, iz, cx, cy, cz, h, lo, hi);
+  };
   int32_t *I = idx + rr * n_max;
   float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
 
@@ -222,7 +239,7 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   {
     float4 rb = CB[(int64_t)n * 8];
     float lo, hi;
-    bool rh = live && nsvf_slab(ox, oy, oz, ix, iy, iz, rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi);
+    bool rh = live && slab(rb.x, rb.y, rb.z, fabsf(rb.w), lo, hi);
     if (rh && rb.w < 0.0f) {            // a single-leaf octree
       if (j == 0) { I[0] = n - 1; LO[0] = lo; HI[0] = hi; }
       cnt = 1;
@@ -253,7 +270,7 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
         } else {
           float4 b = CB[kb];
           bw = b.w;
-          hit = nsvf_slab(ox, oy, oz, ix, iy, iz, b.x, b.y, b.z, fabsf(b.w), lo, hi);
+          hit = slab(b.x, b.y, b.z, fabsf(b.w), lo, hi);
         }
       }
     }
@@ -315,7 +332,7 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
             if (j == 0) {
               float4 cb = CB[(int64_t)s_node[base] * 8 + u];
               float a, b2;
-              nsvf_slab(ox, oy, oz, ix, iy, iz, cb.x, cb.y, cb.z, -cb.w, a, b2);
+              slab(cb.x, cb.y, cb.z, -cb.w, a, b2);
               I[cnt] = ch; LO[cnt] = a; HI[cnt] = b2;
             }
             ++cnt;
