@@ -104,6 +104,22 @@ int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, i
                               float *max_depth, uint8_t *hits, int32_t *err, void *workspace,
                               void *stream);
 
+/* triangle_intersect: replaces triangle_intersect (fairnr/clib/src/
+ * intersect.cpp:120-145, kernel fairnr/clib/src/intersect_gpu.cu:238-345),
+ * the mesh encoder's ray-triangle op. face_points [b_faces, n, 9] (three
+ * vertices per face; b_faces 1 = shared by all b rows, where the reference
+ * copies it per row). Per ray: the first n_max faces with t > 0 in face
+ * order, sorted by depth (insertion; ties keep face order), idx [b, m,
+ * n_max] (-1 pad), depth [b, m, 3 n_max] = per hit (t, -min(cagesize, half
+ * the gap to the previous hit), +min(cagesize, half the gap to the next);
+ * -/+cagesize at the ends), uv [b, m, 2 n_max] barycentrics; unused slots 0.
+ * Moller-Trumbore with the reference's `blur` margin and its FP32 operation
+ * sequence; 1/det correctly rounded. */
+int nsvf_triangle_intersect(int b, int b_faces, int n, int m, float cagesize, float blur,
+                            int n_max, const float *ray_start, const float *ray_dir,
+                            const float *face_points, int32_t *idx, float *depth, float *uv,
+                            void *stream);
+
 /* ball_intersect: replaces `ball_intersect(ray_start, ray_dir, points,
  * radius, n_max)` (fairnr/clib/src/intersect.cpp:15-41). Rays vs spheres of
  * `radius` around each point; first n_max hits in point order. */

@@ -34,6 +34,7 @@ def _load():
         "nsvf_svo_intersect_sorted": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P, P, P,
                                        P, P], i32),
         "nsvf_ball_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P], i32),
+        "nsvf_triangle_intersect": ([i32, i32, i32, i32, f32, f32, i32, P, P, P, P, P, P, P], i32),
         "nsvf_uniform_ray_sampling": ([i32, i32, i32, i32, f32, P, P, P, P, P, P, P, P, P], i32),
         "nsvf_inverse_cdf_sampling": ([i64, i32, i32, i32, f32, P, P, P, P, P, P, P, P, P, P,
                                        P, P, P], i32),
@@ -84,6 +85,7 @@ def exported_symbols():
     return [
         "nsvf_status_string", "nsvf_launch_count", "nsvf_aabb_intersect", "nsvf_svo_workspace_bytes",
         "nsvf_svo_intersect", "nsvf_svo_intersect_sorted", "nsvf_ball_intersect",
+        "nsvf_triangle_intersect",
         "nsvf_uniform_ray_sampling", "nsvf_inverse_cdf_sampling", "nsvf_build_octree",
         "nsvf_trilinear_embed", "nsvf_trilinear_embed_backward", "nsvf_composite",
         "nsvf_composite_backward", "nsvf_mlp_forward_bf16", "nsvf_sample_count",

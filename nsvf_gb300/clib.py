@@ -81,6 +81,35 @@ class SparseVoxelOctreeRayIntersect(Function):
 svo_ray_intersect = SparseVoxelOctreeRayIntersect.apply
 
 
+class TriangleRayIntersect(Function):
+    """fairnr/clib/__init__.py:136-173: rays against the mesh `faces` [F, 3]
+    (vertex ids into `points`) -> inds [S, N, n_max], depth [S, N, n_max, 3]
+    (t, min offset, max offset per hit), uv [S, N, 2 n_max]. The reference
+    expands the face vertex table over up to 2048 ray groups; here one copy
+    serves every row."""
+
+    @staticmethod
+    def forward(ctx, cagesize, blur_ratio, n_max, points, faces, ray_start, ray_dir):
+        S, N = ray_start.shape[:2]
+        face_points = torch.nn.functional.embedding(faces.reshape(-1, 3), points.reshape(-1, 3))
+        face_points = face_points.reshape(1, -1, 9).float().contiguous()
+        inds, depth, uv = ext.triangle_intersect(
+            ray_start.float().contiguous(), ray_dir.float().contiguous(), face_points,
+            float(cagesize), float(blur_ratio), int(n_max))
+        depth = depth.type_as(ray_start).reshape(S, N, -1, 3)
+        uv = uv.type_as(ray_start).reshape(S, N, -1)
+        inds = inds.reshape(S, N, -1)
+        ctx.mark_non_differentiable(inds, depth, uv)
+        return inds, depth, uv
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None, None, None
+
+
+triangle_ray_intersect = TriangleRayIntersect.apply
+
+
 def _truncate(sampled_idx, sampled_depth, sampled_dists, max_len):
     return sampled_idx[:, :max_len], sampled_depth[:, :max_len], sampled_dists[:, :max_len]
 

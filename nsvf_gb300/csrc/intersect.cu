@@ -409,6 +409,111 @@ __global__ void __launch_bounds__(kRayBlock) ball_kernel(
   for (int l = cnt; l < n_max; ++l) { I[l] = -1; LO[l] = 0.0f; HI[l] = 0.0f; }
 }
 
+// ------------------------------------------------------------ triangle ----
+
+constexpr int kTriTile = 512;   // faces per shared-memory tile (18 KB)
+
+// The reference's float3 helpers as nvcc contracts them
+// (fairnr/clib/include/cutil_math.h:404-413, first product of a sum fused):
+// dot -> fma(z, z', fma(x, x', y*y')), cross a*b - c*d -> fma(a, b, -(c*d)).
+__device__ __forceinline__ float tri_dot(float ax, float ay, float az, float bx, float by,
+                                         float bz) {
+  return __fmaf_rn(az, bz, __fmaf_rn(ax, bx, __fmul_rn(ay, by)));
+}
+__device__ __forceinline__ float tri_cr(float a, float b, float c, float d) {
+  return __fmaf_rn(a, b, -__fmul_rn(c, d));
+}
+
+// RayTriangleIntersection (fairnr/clib/src/intersect_gpu.cu:238-270):
+// Moller-Trumbore with a `blur` margin on the barycentrics; t (> 0 on a hit)
+// and (u, v). 1/det is the correctly rounded reciprocal (the reference's
+// __fdividef is approximate).
+__device__ __forceinline__ float tri_test(float ox, float oy, float oz, float dx, float dy,
+                                          float dz, const float *__restrict__ f, float blur,
+                                          float &u_out, float &v_out) {
+  const float e1x = __fsub_rn(f[3], f[0]), e1y = __fsub_rn(f[4], f[1]), e1z = __fsub_rn(f[5], f[2]);
+  const float e2x = __fsub_rn(f[6], f[0]), e2y = __fsub_rn(f[7], f[1]), e2z = __fsub_rn(f[8], f[2]);
+  const float vx = __fsub_rn(ox, f[0]), vy = __fsub_rn(oy, f[1]), vz = __fsub_rn(oz, f[2]);
+  const float px = tri_cr(dy, e2z, dz, e2y), py = tri_cr(dz, e2x, dx, e2z),
+              pz = tri_cr(dx, e2y, dy, e2x);
+  const float det = nsvf_rcp(tri_dot(e1x, e1y, e1z, px, py, pz));
+  const float u = __fmul_rn(tri_dot(vx, vy, vz, px, py, pz), det);
+  const float lo = __fsub_rn(0.0f, blur), hi = __fadd_rn(1.0f, blur);
+  if ((u < lo) || (u > hi)) return -1.0f;
+  const float qx = tri_cr(vy, e1z, vz, e1y), qy = tri_cr(vz, e1x, vx, e1z),
+              qz = tri_cr(vx, e1y, vy, e1x);
+  const float v = __fmul_rn(tri_dot(dx, dy, dz, qx, qy, qz), det);
+  if ((v < lo) || (v > hi)) return -1.0f;
+  const float uv = __fadd_rn(u, v);
+  if ((uv < lo) || (uv > hi)) return -1.0f;
+  u_out = u;
+  v_out = v;
+  return __fmul_rn(tri_dot(e2x, e2y, e2z, qx, qy, qz), det);
+}
+
+// One thread per ray, faces staged through shared memory in tiles; the
+// first n_max hits in face order kept depth-sorted by insertion, then the
+// per-hit depth offsets (fairnr/clib/src/intersect_gpu.cu:273-345).
+__global__ void __launch_bounds__(kRayBlock) triangle_kernel(
+    int b, int b_faces, int n, int m, float cagesize, float blur, int n_max,
+    const float *__restrict__ ray_start, const float *__restrict__ ray_dir,
+    const float *__restrict__ faces, int32_t *__restrict__ idx, float *__restrict__ depth,
+    float *__restrict__ uv) {
+  __shared__ float sf[kTriTile * 9];
+  const int blocks_per_row = (m + kRayBlock - 1) / kRayBlock;
+  const int g = blockIdx.x / blocks_per_row;
+  const int j = (blockIdx.x % blocks_per_row) * kRayBlock + threadIdx.x;
+  const bool live = j < m;
+  const int64_t r = (int64_t)g * m + (live ? j : 0);
+  const float *F = faces + (b_faces == 1 ? 0 : (int64_t)g * n * 9);
+  float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0;
+  if (live) {
+    ox = ray_start[r * 3 + 0]; oy = ray_start[r * 3 + 1]; oz = ray_start[r * 3 + 2];
+    dx = ray_dir[r * 3 + 0]; dy = ray_dir[r * 3 + 1]; dz = ray_dir[r * 3 + 2];
+  }
+  int32_t *I = idx + r * n_max;
+  float *D = depth + r * n_max * 3, *UV = uv + r * n_max * 2;
+  int cnt = 0;
+  for (int base = 0; base < n; base += kTriTile) {
+    const int tile = min(kTriTile, n - base);
+    if (__syncthreads_and(!live || cnt >= n_max)) break;
+    for (int t = threadIdx.x; t < tile * 9; t += kRayBlock) sf[t] = F[(int64_t)base * 9 + t];
+    __syncthreads();
+    if (live) {
+      for (int k = 0; k < tile && cnt < n_max; ++k) {
+        float u, v;
+        float t = tri_test(ox, oy, oz, dx, dy, dz, sf + k * 9, blur, u, v);
+        if (!(t > 0.0f)) continue;
+        int ki = base + k;
+        for (int l = 0; l < cnt; ++l) {
+          if (t < D[3 * l]) {
+            int ti = I[l]; I[l] = ki; ki = ti;
+            float tt = D[3 * l]; D[3 * l] = t; t = tt;
+            float tu = UV[2 * l]; UV[2 * l] = u; u = tu;
+            float tv = UV[2 * l + 1]; UV[2 * l + 1] = v; v = tv;
+          }
+        }
+        I[cnt] = ki; D[3 * cnt] = t; UV[2 * cnt] = u; UV[2 * cnt + 1] = v;
+        ++cnt;
+      }
+    }
+    __syncthreads();
+  }
+  if (!live) return;
+  for (int l = 0; l < cnt; ++l) {
+    D[3 * l + 1] = (l == 0) ? -cagesize
+                            : -fminf(cagesize, __fmul_rn(0.5f, __fsub_rn(D[3 * l], D[3 * l - 3])));
+    D[3 * l + 2] = (l == cnt - 1)
+                       ? cagesize
+                       : fminf(cagesize, __fmul_rn(0.5f, __fsub_rn(D[3 * l + 3], D[3 * l])));
+  }
+  for (int l = cnt; l < n_max; ++l) {
+    I[l] = -1;
+    D[3 * l] = D[3 * l + 1] = D[3 * l + 2] = 0.0f;
+    UV[2 * l] = UV[2 * l + 1] = 0.0f;
+  }
+}
+
 // Ray pointers may be NULL when there are no rays (empty tensors).
 bool bad_common(int b, int b_pts, int n, int m, int n_max, const void *a, const void *c,
                 const void *d) {
@@ -556,6 +661,21 @@ int nsvf_svo_intersect_noalloc(int b, int b_pts, int n, int m, float voxelsize, 
   // traversal reads them, so nothing left by an earlier call is read
   return svo_launch(false, b, b_pts, n, m, voxelsize, n_max, ray_start, ray_dir, points, children,
                     idx, min_depth, max_depth, nullptr, err, scratch, stream);
+}
+
+int nsvf_triangle_intersect(int b, int b_faces, int n, int m, float cagesize, float blur,
+                            int n_max, const float *ray_start, const float *ray_dir,
+                            const float *face_points, int32_t *idx, float *depth, float *uv,
+                            void *stream) {
+  if (bad_common(b, b_faces, n, m, n_max, ray_start, ray_dir, face_points)) return NSVF_ERR_INVALID;
+  if ((int64_t)b * m == 0) return NSVF_OK;
+  if (!idx || !depth || !uv) return NSVF_ERR_INVALID;
+  int blocks_per_row = (m + kRayBlock - 1) / kRayBlock;
+  int64_t grid = (int64_t)b * blocks_per_row;
+  if (grid > 0x7fffffff) return NSVF_ERR_INVALID;
+  triangle_kernel<<<(int)grid, kRayBlock, 0, (cudaStream_t)stream>>>(
+      b, b_faces, n, m, cagesize, blur, n_max, ray_start, ray_dir, face_points, idx, depth, uv);
+  return nsvf_launch_status();
 }
 
 int nsvf_ball_intersect(int b, int b_pts, int n, int m, float radius, int n_max,

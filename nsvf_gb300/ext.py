@@ -209,6 +209,25 @@ def ball_intersect(ray_start, ray_dir, points, radius, n_max):
     return idx, lo, hi
 
 
+def triangle_intersect(ray_start, ray_dir, face_points, cagesize, blur, n_max):
+    """fairnr/clib/src/intersect.cpp:120-145: face_points [B or 1, F, 9] ->
+    (idx [B, M, n_max], depth [B, M, 3 n_max], uv [B, M, 2 n_max])."""
+    for n, t in (("ray_start", ray_start), ("ray_dir", ray_dir), ("face_points", face_points)):
+        _check_float(n, t)
+    B, M = ray_start.shape[:2]
+    bf = _batch_pts(face_points, B)
+    N = face_points.size(1)
+    dev = ray_start.device
+    idx = torch.empty(B, M, n_max, dtype=torch.int32, device=dev)
+    depth = torch.empty(B, M, 3 * n_max, dtype=torch.float32, device=dev)
+    uv = torch.empty(B, M, 2 * n_max, dtype=torch.float32, device=dev)
+    check(LIB.nsvf_triangle_intersect(B, bf, N, M, float(cagesize), float(blur), int(n_max),
+                                      _ptr(ray_start), _ptr(ray_dir), _ptr(face_points),
+                                      _ptr(idx), _ptr(depth), _ptr(uv), _stream(ray_start)),
+          "triangle_intersect")
+    return idx, depth, uv
+
+
 def uniform_ray_sampling(pts_idx, min_depth, max_depth, uniform_noise, step_size, max_steps):
     """fairnr/clib/src/sample.cpp:23-55: -> (sampled_idx, sampled_depth, sampled_dists) [B, M, max_steps]."""
     _check_int("pts_idx", pts_idx)

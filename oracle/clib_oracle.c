@@ -13,6 +13,7 @@
  *   or_aabb_intersect   fairnr/clib/src/intersect_gpu.cu:125-167 + intersect.cpp:49-75
  *   or_svo_intersect    fairnr/clib/src/intersect_gpu.cu:170-237 + intersect.cpp:84-112
  *   or_ball_intersect   fairnr/clib/src/intersect_gpu.cu:15-70   + intersect.cpp:15-41
+ *   or_triangle_intersect fairnr/clib/src/intersect_gpu.cu:238-337 + intersect.cpp:120-145
  *   or_uniform_sampling fairnr/clib/src/sample_gpu.cu:15-106     + sample.cpp:23-55
  *   or_inverse_cdf      fairnr/clib/src/sample_gpu.cu:108-202    + sample.cpp:58-96
  *   or_build_octree     fairnr/clib/src/octree.cpp:13-136
@@ -157,6 +158,93 @@ void or_ball_intersect(int b, int n, int m, float radius, int n_max,
           float blur = sqrtf(r2max - r2);
           I[cnt] = k; lo[cnt] = depth - blur; hi[cnt] = depth + blur; ++cnt;
         }
+      }
+    }
+  }
+}
+
+/* Ray-triangle test (Moller-Trumbore with a `blur` margin on the
+ * barycentrics) with the reference's float3 helpers as nvcc contracts them
+ * (fairnr/clib/include/cutil_math.h:404-413; the first product of a sum is
+ * the one fused): dot = (x*x' + y*y') + z*z' -> fma(z, z', fma(x, x', y*y')),
+ * cross components a*b - c*d -> fma(a, b, -(c*d)). Checked bit for bit
+ * against the reference's kernel body compiled for the CPU with contraction
+ * on. Returns t > 0 on a hit (with u, v), else t = -1. 1/det is IEEE (the
+ * reference's __fdividef is approximate). */
+static float or_dot(const float a[3], const float b[3]) {
+  return fmaf(a[2], b[2], fmaf(a[0], b[0], a[1] * b[1]));
+}
+static void or_cross(const float a[3], const float b[3], float c[3]) {
+  c[0] = fmaf(a[1], b[2], -(a[2] * b[1]));
+  c[1] = fmaf(a[2], b[0], -(a[0] * b[2]));
+  c[2] = fmaf(a[0], b[1], -(a[1] * b[0]));
+}
+static float or_tri(const float o[3], const float d[3], const float *v, float blur, float *u_out,
+                    float *v_out) {
+  float e1[3], e2[3], ov[3], p[3], q[3];
+  for (int k = 0; k < 3; ++k) {
+    e1[k] = v[3 + k] - v[k];
+    e2[k] = v[6 + k] - v[k];
+    ov[k] = o[k] - v[k];
+  }
+  or_cross(d, e2, p);
+  float det = or_dot(e1, p);
+  det = 1.0f / det;
+  float u = or_dot(ov, p) * det;
+  if ((u < 0.0f - blur) || (u > 1.0f + blur)) return -1.0f;
+  or_cross(ov, e1, q);
+  float w = or_dot(d, q) * det;
+  if ((w < 0.0f - blur) || (w > 1.0f + blur)) return -1.0f;
+  if (((u + w) < 0.0f - blur) || ((u + w) > 1.0f + blur)) return -1.0f;
+  *u_out = u;
+  *v_out = w;
+  return or_dot(e2, q) * det;
+}
+
+/* Triangle intersection (mesh encoder): per ray, the first n_max triangles
+ * with t > 0 in face order, kept sorted by depth by insertion (a new hit
+ * moves past every stored one with a depth <= its own). Layout: faces
+ * [b, n, 9] (three vertices), idx [b, m, n_max] (-1 pad), depth
+ * [b, m, n_max * 3] = per hit (t, min offset, max offset) with the offsets
+ * -cagesize / +cagesize at the ends of the list and otherwise minus / plus
+ * min(cagesize, half the gap to the neighbouring hit) (0 where unused), uv
+ * [b, m, n_max * 2]. */
+void or_triangle_intersect(int b, int n, int m, float cagesize, float blur, int n_max,
+                           const float *ray_start, const float *ray_dir, const float *faces,
+                           int32_t *idx, float *depth, float *uv) {
+  for (int g = 0; g < b; ++g) {
+    const float *F = faces + (int64_t)g * n * 9;
+    for (int j = 0; j < m; ++j) {
+      int64_t r = (int64_t)g * m + j;
+      const float *o = ray_start + r * 3, *d = ray_dir + r * 3;
+      int32_t *I = idx + r * n_max;
+      float *D = depth + r * n_max * 3, *UV = uv + r * n_max * 2;
+      for (int l = 0; l < n_max; ++l) {
+        I[l] = -1;
+        D[3 * l] = D[3 * l + 1] = D[3 * l + 2] = 0.0f;
+        UV[2 * l] = UV[2 * l + 1] = 0.0f;
+      }
+      int cnt = 0;
+      for (int k = 0; k < n && cnt < n_max; ++k) {
+        float u, w;
+        float t = or_tri(o, d, F + (int64_t)k * 9, blur, &u, &w);
+        if (!(t > 0.0f)) continue;
+        int ki = k;
+        for (int l = 0; l < cnt; ++l) {
+          if (t < D[3 * l]) {
+            int ti = I[l]; I[l] = ki; ki = ti;
+            float tt = D[3 * l]; D[3 * l] = t; t = tt;
+            float tu = UV[2 * l]; UV[2 * l] = u; u = tu;
+            float tv = UV[2 * l + 1]; UV[2 * l + 1] = w; w = tv;
+          }
+        }
+        I[cnt] = ki; D[3 * cnt] = t; UV[2 * cnt] = u; UV[2 * cnt + 1] = w;
+        ++cnt;
+      }
+      /* fairnr/clib/src/intersect_gpu.cu:331-345 (.5 * float is exact) */
+      for (int l = 0; l < cnt; ++l) {
+        D[3 * l + 1] = (l == 0) ? -cagesize : -fminf(cagesize, 0.5f * (D[3 * l] - D[3 * l - 3]));
+        D[3 * l + 2] = (l == cnt - 1) ? cagesize : fminf(cagesize, 0.5f * (D[3 * l + 3] - D[3 * l]));
       }
     }
   }

@@ -51,6 +51,7 @@ def lib():
         _lib.or_svo_intersect.argtypes = [i, i, i, f, i, P, P, P, P, P, P, P]
         _lib.or_svo_intersect.restype = i
         _lib.or_ball_intersect.argtypes = [i, i, i, f, i, P, P, P, P, P, P]
+        _lib.or_triangle_intersect.argtypes = [i, i, i, f, f, i, P, P, P, P, P, P]
         _lib.or_uniform_sampling.argtypes = [i, i, i, i, f, P, P, P, P, P, P, P]
         _lib.or_inverse_cdf.argtypes = [i, i, i, i, f, P, P, P, P, P, P, P, P, P, P, P]
         _lib.or_build_octree.argtypes = [P, P, i64, i, P, P, i64]
@@ -104,6 +105,19 @@ def ball_intersect(ray_start, ray_dir, points, radius, n_max):
     hi = np.empty((b, m, n_max), np.float32)
     lib().or_ball_intersect(b, n, m, radius, n_max, _p(rs), _p(rd), _p(pts), _p(idx), _p(lo), _p(hi))
     return idx, lo, hi
+
+
+def triangle_intersect(ray_start, ray_dir, faces, cagesize, blur, n_max):
+    """faces [b, n, 9] -> idx [b, m, n_max], depth [b, m, 3 n_max], uv [b, m, 2 n_max]."""
+    rs, rd, F = _c(ray_start, np.float32), _c(ray_dir, np.float32), _c(faces, np.float32)
+    b, m = rs.shape[:2]
+    n = F.shape[1]
+    idx = np.empty((b, m, n_max), np.int32)
+    depth = np.empty((b, m, 3 * n_max), np.float32)
+    uv = np.empty((b, m, 2 * n_max), np.float32)
+    lib().or_triangle_intersect(b, n, m, float(cagesize), float(blur), n_max, _p(rs), _p(rd),
+                                _p(F), _p(idx), _p(depth), _p(uv))
+    return idx, depth, uv
 
 
 def uniform_ray_sampling(pts_idx, min_depth, max_depth, noise, step_size, max_steps):

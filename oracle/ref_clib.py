@@ -28,6 +28,7 @@ def lib():
         _lib.ref_aabb_intersect.argtypes = [i, i, i, f, i, P, P, P, P, P, P]
         _lib.ref_svo_intersect.argtypes = [i, i, i, f, i, P, P, P, P, P, P, P]
         _lib.ref_ball_intersect.argtypes = [i, i, i, f, i, P, P, P, P, P, P]
+        _lib.ref_triangle_intersect.argtypes = [i, i, i, f, f, i, P, P, P, P, P, P]
         _lib.ref_uniform_ray_sampling.argtypes = [i, i, i, i, f, P, P, P, P, P, P, P]
         _lib.ref_inverse_cdf_sampling.argtypes = [i, i, i, i, f, P, P, P, P, P, P, P, P, P]
     return _lib
@@ -98,3 +99,15 @@ def inverse_cdf_sampling(pts_idx, min_depth, max_depth, noise, probs, steps, fix
     lib().ref_inverse_cdf_sampling(b, m, H, M, fixed_step_size, _p(Ipad), _p(lo), _p(hi), _p(U),
                                    _p(pr), _p(st), _p(si), _p(sd), _p(ss))
     return si, sd, ss
+
+
+def triangle_intersect(ray_start, ray_dir, faces, cagesize, blur, n_max):
+    rs, rd, F = _c(ray_start, np.float32), _c(ray_dir, np.float32), _c(faces, np.float32)
+    b, m = rs.shape[:2]
+    n = F.shape[1]
+    idx = np.zeros((b, m, n_max), np.int32)      # the reference allocates zeros
+    depth = np.zeros((b, m, 3 * n_max), np.float32)
+    uv = np.zeros((b, m, 2 * n_max), np.float32)
+    lib().ref_triangle_intersect(b, n, m, float(cagesize), float(blur), n_max, _p(rs), _p(rd),
+                                 _p(F), _p(idx), _p(depth), _p(uv))
+    return idx, depth, uv

@@ -73,6 +73,13 @@ class CpuExt:
                                             noise.numpy(), probs.numpy(), steps.numpy(), float(fixed))
         return tuple(cls._t(o) for o in out)
 
+    @classmethod
+    def triangle_intersect(cls, ray_start, ray_dir, face_points, cagesize, blur, n_max):
+        from oracle import ref_clib
+        out = ref_clib.triangle_intersect(ray_start.numpy(), ray_dir.numpy(), face_points.numpy(),
+                                          float(cagesize), float(blur), int(n_max))
+        return tuple(cls._t(o) for o in out)
+
     @staticmethod
     def build_octree(center, points, depth):
         from oracle import build_ref
@@ -110,7 +117,7 @@ def load():
     R = os.path.join(REF, "fairnr")
     ext = types.ModuleType("fairnr.clib._ext")
     for name in ["aabb_intersect", "svo_intersect", "uniform_ray_sampling",
-                 "inverse_cdf_sampling", "build_octree"]:
+                 "inverse_cdf_sampling", "build_octree", "triangle_intersect"]:
         setattr(ext, name, getattr(CpuExt, name))
     sys.modules["fairnr.clib._ext"] = ext
     ns = types.SimpleNamespace()

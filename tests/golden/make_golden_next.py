@@ -14,6 +14,9 @@ Writes golden_next.npz, on the 147-voxel "small" scene of golden_small.npz:
   (fairnr/modules/renderer.py:146-188) on the deterministic samples;
 * split_* -- SparseVoxelEncoder.splitting (fairnr/modules/encoder.py:656-676):
   new voxel centres, corner ids and re-interpolated corner embeddings.
+* tri_* -- triangle_ray_intersect (fairnr/clib/__init__.py:136-173) of the
+  c1 camera's rays against a seeded closed mesh (an icosphere-like cage of
+  320 faces, radius 0.7) with cagesize 0.05, blur 0.01, n_max 8.
 """
 import argparse
 import os
@@ -30,6 +33,35 @@ sys.path.insert(0, HERE)
 from oracle import ref_import, build_ref  # noqa: E402
 from nsvf_gb300 import scenes  # noqa: E402
 import make_golden as mg  # noqa: E402
+
+
+def cage_mesh(radius=0.7, subdiv=2, seed=3):
+    """A closed triangle cage: an icosahedron subdivided twice (320 faces),
+    vertices on a sphere of `radius` with a seeded 5 % radial jitter."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+         (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9),
+         (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(x, np.float64) / np.linalg.norm(x) for x in v]
+    for _ in range(subdiv):
+        mid = {}
+        nf = []
+        for a, b, c in f:
+            ids = []
+            for p, q in ((a, b), (b, c), (c, a)):
+                key = (min(p, q), max(p, q))
+                if key not in mid:
+                    m = verts[p] + verts[q]
+                    verts.append(m / np.linalg.norm(m))
+                    mid[key] = len(verts) - 1
+                ids.append(mid[key])
+            nf += [(a, ids[0], ids[2]), (b, ids[1], ids[0]), (c, ids[2], ids[1]), tuple(ids)]
+        f = nf
+    rng = np.random.RandomState(seed)
+    V = np.array(verts) * radius * (1 + 0.05 * rng.uniform(-1, 1, size=(len(verts), 1)))
+    return V.astype(np.float32), np.array(f, np.int64)
 
 
 def main():
@@ -96,6 +128,19 @@ def main():
     g["split_values"] = enc_s.values.weight.detach().numpy()
     g["split_num_keys"] = np.int64(int(enc_s.num_keys))
     g["split_keep"] = enc_s.keep.numpy()
+    # --- triangle intersection (mesh encoder op) ---------------------------
+    verts, faces = cage_mesh()
+    rs_t = torch.from_numpy(np.broadcast_to(rs, rd[sel].shape).copy()).reshape(1, -1, 3)
+    rd_t = torch.from_numpy(rd[sel]).reshape(1, -1, 3)
+    inds, depth, uv = ref.clib.triangle_ray_intersect(0.05, 0.01, 8, torch.from_numpy(verts),
+                                                      torch.from_numpy(faces), rs_t, rd_t)
+    g["tri_verts"] = verts
+    g["tri_faces"] = faces
+    g["tri_ray_start"] = rs_t.numpy()
+    g["tri_ray_dir"] = rd_t.numpy()
+    g["tri_inds"] = inds.numpy()
+    g["tri_depth"] = depth.numpy()
+    g["tri_uv"] = uv.numpy()
     np.savez_compressed(os.path.join(HERE, "golden_next.npz"), **g)
     print("wrote golden_next.npz", {k: getattr(v, "shape", None) for k, v in g.items()})
     print("early stop evals:", int(g["es0.01_ae"]), int(g["es0.5_ae"]))

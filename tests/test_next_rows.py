@@ -104,3 +104,56 @@ def test_early_termination_matches_reference(golden, golden_next, cuda, tol):
     np.testing.assert_allclose(out["probs"].cpu().numpy(), n["%s_probs" % tag], atol=2e-4)
     # and it does stop early: fewer evaluations than valid samples
     assert int(out["ae"]) < int((g["svo_det_sampled_point_voxel_idx"] != -1).sum())
+
+
+def _tri_golden_faces(n):
+    verts, faces = n["tri_verts"], n["tri_faces"]
+    return verts[faces].reshape(1, -1, 9).astype(np.float32)
+
+
+def test_triangle_oracle_matches_reference(golden_next):
+    """The mesh encoder's ray-triangle op: the C oracle against the
+    reference's own triangle_ray_intersect output, bit for bit."""
+    from oracle import cpu
+    n = golden_next
+    idx, depth, uv = cpu.triangle_intersect(n["tri_ray_start"], n["tri_ray_dir"],
+                                            _tri_golden_faces(n), 0.05, 0.01, 8)
+    assert np.array_equal(idx, n["tri_inds"])
+    assert np.array_equal(depth.reshape(n["tri_depth"].shape), n["tri_depth"])
+    assert np.array_equal(uv, n["tri_uv"])
+    assert (idx != -1).sum() > 200
+
+
+@pytest.mark.gpu
+def test_triangle_ray_intersect_matches_reference(golden_next, cuda):
+    from nsvf_gb300 import clib
+    n = golden_next
+    out = clib.triangle_ray_intersect(0.05, 0.01, 8, torch.from_numpy(n["tri_verts"]).to(cuda),
+                                      torch.from_numpy(n["tri_faces"]).to(cuda),
+                                      torch.from_numpy(n["tri_ray_start"]).to(cuda),
+                                      torch.from_numpy(n["tri_ray_dir"]).to(cuda))
+    for got, key in zip(out, ["tri_inds", "tri_depth", "tri_uv"]):
+        assert np.array_equal(got.cpu().numpy(), n[key]), key
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_faces,n_max,blur,shared", [(37, 4, 0.0, True), (700, 16, 0.05, False),
+                                                       (1500, 8, 0.0, True)])
+def test_triangle_kernel_matches_oracle(cuda, n_faces, n_max, blur, shared):
+    """Random triangle soups (more faces than one shared-memory tile in the
+    larger cases), faces shared by both ray rows or one set per row."""
+    from nsvf_gb300 import ext
+    from oracle import cpu
+    rng = np.random.RandomState(n_faces)
+    b, m = 2, 700
+    nb = 1 if shared else b
+    faces = rng.uniform(-1, 1, size=(nb, n_faces, 9)).astype(np.float32)
+    o = (rng.normal(size=(b, m, 3)) * 3).astype(np.float32)
+    d = (-o + rng.normal(scale=0.5, size=(b, m, 3))).astype(np.float32)
+    d = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
+    got = ext.triangle_intersect(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda),
+                                 torch.from_numpy(faces).to(cuda), 0.03, blur, n_max)
+    ref = cpu.triangle_intersect(o, d, np.broadcast_to(faces, (b, n_faces, 9)), 0.03, blur, n_max)
+    for a, r in zip(got, ref):
+        assert np.array_equal(a.cpu().numpy(), r)
+    assert (ref[0] != -1).sum() > 500
