@@ -14,6 +14,10 @@ Writes golden_next.npz, on the 147-voxel "small" scene of golden_small.npz:
   (fairnr/modules/renderer.py:146-188) on the deterministic samples;
 * split_* -- SparseVoxelEncoder.splitting (fairnr/modules/encoder.py:656-676):
   new voxel centres, corner ids and re-interpolated corner embeddings.
+* rf_* -- a seeded reference RaidanceField (inputs "emb:6:32" / "feat:0:64,
+  ray:4", widths 64/32/64, 1 feature layer, 2 texture layers) rendering the
+  deterministic samples with the reference's VolumeRenderer: its state dict
+  (rf_state_<name>) and colors/depths/missed;
 * tri_* -- triangle_ray_intersect (fairnr/clib/__init__.py:136-173) of the
   c1 camera's rays against a seeded closed mesh (an icosphere-like cage of
   320 faces, radius 0.7) with cagesize 0.05, blur 0.01, n_max 8.
@@ -120,6 +124,21 @@ def main():
         for k in ["colors", "depths", "missed", "probs"]:
             g["%s_%s" % (tag, k)] = res[k].detach().numpy()
         g["%s_ae" % tag] = np.int64(int(res["ae"]))
+    # --- a reference radiance field rendering the same samples -----------
+    torch.manual_seed(11)
+    rf_args = argparse.Namespace(inputs_to_density="emb:6:32", inputs_to_texture="feat:0:64, ray:4",
+                                 feature_embed_dim=64, density_embed_dim=32, texture_embed_dim=64,
+                                 feature_layers=1, texture_layers=2, background_stop_gradient=False)
+    rf = ref.field.RaidanceField(rf_args).eval()
+    with torch.no_grad():
+        rf.predictor.output_layer.bias.fill_(0.5)          # a partly opaque scene
+    ren = ref.renderer.VolumeRenderer(argparse.Namespace(chunk_size=64)).eval()
+    with torch.no_grad():
+        res = ren(enc, rf, rsh, rdh, dict(samples), st)
+    for k, v in rf.state_dict().items():
+        g["rf_state_" + k] = v.numpy()
+    for k in ["colors", "depths", "missed"]:
+        g["rf_%s" % k] = res[k].detach().numpy()
     # --- splitting --------------------------------------------------------
     enc_s = mg.make_encoder(ref, pts, vs, True, embed)
     enc_s.splitting()

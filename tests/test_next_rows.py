@@ -157,3 +157,34 @@ def test_triangle_kernel_matches_oracle(cuda, n_faces, n_max, blur, shared):
     for a, r in zip(got, ref):
         assert np.array_equal(a.cpu().numpy(), r)
     assert (ref[0] != -1).sum() > 500
+
+
+@pytest.mark.gpu
+def test_reference_radiance_field_renders_like_reference(golden, golden_next, cuda):
+    """A checkpoint of the reference's RaidanceField (state dict from the
+    fixture) loads into nsvf_gb300.field.RaidanceField and renders the same
+    samples through the drop-in encoder and renderer as the reference did."""
+    from nsvf_gb300.field import RaidanceField
+    from nsvf_gb300.renderer import VolumeRenderer
+    g, n = golden, golden_next
+    enc = _encoder(g, cuda)
+    st = enc.precompute(id=None)
+    args = argparse.Namespace(inputs_to_density="emb:6:32", inputs_to_texture="feat:0:64, ray:4",
+                              feature_embed_dim=64, density_embed_dim=32, texture_embed_dim=64,
+                              feature_layers=1, texture_layers=2, background_stop_gradient=False)
+    field = RaidanceField(args)
+    state = {k[len("rf_state_"):]: torch.from_numpy(n[k]) for k in n if k.startswith("rf_state_")}
+    field.load_state_dict(state, strict=True)
+    field = field.to(cuda).eval()
+    hit = g["svo_hits"][0]
+    N = int(hit.sum())
+    rs = torch.from_numpy(g["ray_start"]).to(cuda).reshape(1, 3).expand(N, 3)
+    rd = torch.from_numpy(g["ray_dir"][hit]).to(cuda)
+    samples = {k: torch.from_numpy(g["svo_det_%s" % k]).to(cuda)
+               for k in ["sampled_point_depth", "sampled_point_distance", "sampled_point_voxel_idx"]}
+    ren = VolumeRenderer(argparse.Namespace(chunk_size=64)).eval()
+    with torch.no_grad():
+        out = ren(enc, field, rs, rd, samples, st)
+    for k in ["colors", "depths", "missed"]:
+        np.testing.assert_allclose(out[k].cpu().numpy(), n["rf_%s" % k], atol=2e-4)
+    assert float(n["rf_missed"].min()) < 0.1          # an opaque enough field to test compositing
