@@ -82,6 +82,35 @@ def make_scene(dev, voxel=1.0 / 64):
                 weights=weights)
 
 
+def dist_env():
+    """(world size, rank, local rank) from the torchrun environment."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def frame_index(step, rank):
+    """Camera of `step` on `rank`: replicas render different frames of the
+    same scene (independent work per GPU, weak scaling)."""
+    return step + 7 * rank
+
+
+def max_over_ranks(x, device=None):
+    """The largest of a per-rank value over all ranks (a job's time is its
+    slowest rank's); x itself when not distributed."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(rays_per_step, steps, world, t_max):
+    """Whole-job rays/s: every rank's rays over the slowest rank's time."""
+    return rays_per_step * steps * world / t_max
+
+
 def frame_rays(index, size=800):
     from nsvf_gb300 import scenes
     rs, rd = scenes.frame_view(index % 100, size=size)
@@ -356,9 +385,7 @@ def run_ours(a):
     from nsvf_gb300._lib import LIB
     from nsvf_gb300.renderer import render_rays
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = dist_env()
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
@@ -373,7 +400,7 @@ def run_ours(a):
     n_frames = a.warmup + a.steps
     host = []
     for i in range(n_frames):
-        rs, rd = frame_rays(i + 7 * rank, a.size)
+        rs, rd = frame_rays(frame_index(i, rank), a.size)
         rdt = torch.from_numpy(rd).pin_memory()
         rst = torch.from_numpy(rs).pin_memory()
         host.append((rst, rdt))
@@ -419,11 +446,7 @@ def run_ours(a):
     clk = clocks.stop()
     ext.KERNEL_TIMING = False
     kernel_ms = ext.kernel_times_ms()
-    t_dev = sum(times)
-    if world > 1:
-        t = torch.tensor([t_dev], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(sum(times), dev)
 
     # --- end to end through the public API with host buffers ---
     torch.cuda.synchronize()
@@ -448,11 +471,7 @@ def run_ours(a):
         e2e_times.append(time.perf_counter() - t0)
         h2d = rst.numel() * 4 + rdt.numel() * 4
         d2h = col.numel() * 4 + dep.numel() * 4
-    t_e2e = sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(sum(e2e_times), dev)
 
     # the plain FP32 drop-in path on the same cameras, for the BF16-vs-FP32 ratio
     plain_fp32 = None
@@ -478,8 +497,7 @@ def run_ours(a):
         dist.destroy_process_group()
         return
     rays_frame = a.size * a.size
-    rays_total = rays_frame * a.steps * world
-    value = rays_total / t_dev
+    value = job_throughput(rays_frame, a.steps, world, t_dev)
     ms = [x * 1e3 for x in times]
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
@@ -537,7 +555,7 @@ def run_ours(a):
                    "voxels": int(sc["points"].shape[0]), "octree_nodes": Nn,
                    "samples_per_frame": (out_samples[0] // a.steps) if out_samples[0] else None,
                    "l2": "flushed (256 MB write) between timed frames", "parallelism": "replicas"},
-        "e2e": {"value": round(rays_frame * a.steps * world / t_e2e, 1), "unit": "rays/s",
+        "e2e": {"value": round(job_throughput(rays_frame, a.steps, world, t_e2e), 1), "unit": "rays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "kernels_ms": kernel_ms,
