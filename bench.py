@@ -45,8 +45,8 @@ def parse():
                     help="served: the fused BF16 path (the headline); plain: the drop-in FP32 path")
     ap.add_argument("--plain-steps", type=int, default=3,
                     help="frames of the plain FP32 path timed beside the served path")
-    ap.add_argument("--cpu-rays", type=int, default=16384,
-                    help="rays of the frame in the CPU baseline sample")
+    ap.add_argument("--cpu-rays", type=int, default=163840,
+                    help="rays of the frame in the CPU baseline sample (about 12 s on one core)")
     ap.add_argument("--size", type=int, default=800,
                     help="frame side in pixels (800 = the c2 workload; smaller for profiling)")
     ap.add_argument("--precision", type=int, default=1,

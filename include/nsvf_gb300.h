@@ -306,7 +306,9 @@ int nsvf_compact_hits(int64_t n, const uint8_t *hits, const int32_t *scan, int64
 /* gather_probs: for rows i < *n_hit, copies the sorted hit list of ray pix[i]
  * ([., max_hits] idx/min/max) and builds its sampling distribution as
  * fairnr/models/nsvf.py:65-74: d = max - min on hit slots, probs = d / sum d,
- * steps = sum d / step_size (sum in slot order). */
+ * steps = sum d / step_size. One warp per row: lane l sums slots l, l + 32,
+ * ... in order, then the 32 partial sums are added by an xor butterfly
+ * (offsets 16, 8, 4, 2, 1). */
 int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
                       const int64_t *pix, const int32_t *idx, const float *min_depth,
                       const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
@@ -395,6 +397,14 @@ int nsvf_field_samples_fp8_dev(int64_t capacity, const int64_t *n_samples_dev,
                                const int32_t *feats, const float *values,
                                const void *const weights[5], const float *const biases[5],
                                const float scales[6], float *out, int32_t *err, void *stream);
+
+/* wait_timeout_selftest: the failure path of the kernels' bounded waits,
+ * without a fault. One CTA waits on an mbarrier phase that never completes;
+ * after limit_ns (1 ns .. 1 s) the wait gives up, bit 3 (8) of *err is set
+ * (the bit the tensor-core kernels set on a timed-out wait) and the kernel
+ * returns, leaving the context usable. No reference counterpart (the
+ * reference's kernels have no waits). */
+int nsvf_wait_timeout_selftest(uint64_t limit_ns, int32_t *err, void *stream);
 
 /* prune_scores_bf16: self-pruning scores (SparseVoxelEncoder.get_scores,
  * fairnr/modules/encoder.py:620-654) in one kernel: for every voxel v,

@@ -62,6 +62,7 @@ def _load():
         "nsvf_field_samples_fp8": ([i64, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P], i32),
         "nsvf_field_samples_fp8_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P],
                                        i32),
+        "nsvf_wait_timeout_selftest": ([ctypes.c_uint64, P, P], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -93,4 +94,5 @@ def exported_symbols():
         "nsvf_prune_scores_bf16", "nsvf_pinhole_rays", "nsvf_camera_rays", "nsvf_compact_hits",
         "nsvf_gather_probs", "nsvf_sample_count_dev", "nsvf_sample_compact_dev", "nsvf_composite_segments_dev",
         "nsvf_field_samples_bf16_dev", "nsvf_field_samples_fp8", "nsvf_field_samples_fp8_dev",
+        "nsvf_wait_timeout_selftest",
     ]

@@ -81,31 +81,41 @@ __global__ void compact_hits_kernel(int64_t n, const uint8_t *__restrict__ hits,
   if (r == n - 1) *n_hit = scan[r];
 }
 
-// Row i < n_hit: copy the hit list of ray pix[i] and build its sampling
-// distribution: d = max - min where the slot is a hit, probs = d / sum(d),
-// steps = sum(d) / step (sum in slot order).
-__global__ void gather_probs_kernel(int64_t cap, const int64_t *__restrict__ n_hit, int H,
-                                    float step, const int64_t *__restrict__ pix,
-                                    const int32_t *__restrict__ idx, const float *__restrict__ lo,
-                                    const float *__restrict__ hi, int32_t *__restrict__ I,
-                                    float *__restrict__ L, float *__restrict__ U,
-                                    float *__restrict__ probs, float *__restrict__ steps) {
-  int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  int64_t n = *n_hit;
-  if (i >= cap || i >= n) return;
-  int64_t r = pix[i];
-  float tot = 0.0f;
-  for (int k = 0; k < H; ++k) {
-    int32_t id = idx[r * H + k];
-    float a = lo[r * H + k], b = hi[r * H + k];
-    I[i * H + k] = id; L[i * H + k] = a; U[i * H + k] = b;
-    tot += (id == -1) ? 0.0f : (b - a);
+// Warp per row i < *n_hit: copy the hit list of ray pix[i] and build its
+// sampling distribution: d = max - min where the slot is a hit, probs =
+// d / sum(d), steps = sum(d) / step. The lanes take slots k = lane, lane + 32,
+// ... (coalesced rows); the sum adds the lanes' partial sums by an xor
+// butterfly, which leaves the same total in every lane and on every run.
+__global__ void __launch_bounds__(kBlock) gather_probs_kernel(
+    int64_t cap, const int64_t *__restrict__ n_hit, int H, float step,
+    const int64_t *__restrict__ pix, const int32_t *__restrict__ idx,
+    const float *__restrict__ lo, const float *__restrict__ hi, int32_t *__restrict__ I,
+    float *__restrict__ L, float *__restrict__ U, float *__restrict__ probs,
+    float *__restrict__ steps) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n = *n_hit < cap ? *n_hit : cap;
+  const int64_t warps = (int64_t)gridDim.x * (kBlock / 32);
+  for (int64_t i = (blockIdx.x * (int64_t)kBlock + threadIdx.x) >> 5; i < n; i += warps) {
+    const int64_t r = pix[i];
+    const int32_t *ir = idx + r * H;
+    const float *lr = lo + r * H, *hr = hi + r * H;
+    float part = 0.0f;
+    for (int k = lane; k < H; k += 32) {
+      const int32_t id = ir[k];
+      const float a = lr[k], b = hr[k];
+      I[i * H + k] = id;
+      L[i * H + k] = a;
+      U[i * H + k] = b;
+      part += (id == -1) ? 0.0f : (b - a);
+    }
+    float tot = part;
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    for (int k = lane; k < H; k += 32) {
+      const float d = (ir[k] == -1) ? 0.0f : (hr[k] - lr[k]);
+      probs[i * H + k] = d / tot;
+    }
+    if (lane == 0) steps[i] = tot / step;
   }
-  for (int k = 0; k < H; ++k) {
-    float d = (I[i * H + k] == -1) ? 0.0f : (U[i * H + k] - L[i * H + k]);
-    probs[i * H + k] = d / tot;
-  }
-  steps[i] = tot / step;
 }
 
 }  // namespace
@@ -149,7 +159,11 @@ int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float ste
   if (!pix || !idx || !min_depth || !max_depth || !out_idx || !out_min || !out_max || !probs ||
       !steps)
     return NSVF_ERR_INVALID;
-  gather_probs_kernel<<<nsvf_grid(cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+  // warp per row, grid-stride over at most 16 blocks per SM (the row count is
+  // only known on the device)
+  int blocks = nsvf_grid(cap, kBlock / 32);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  gather_probs_kernel<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(
       cap, n_hit, max_hits, step_size, pix, idx, min_depth, max_depth, out_idx, out_min, out_max,
       probs, steps);
   return nsvf_launch_status();

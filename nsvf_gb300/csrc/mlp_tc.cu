@@ -372,9 +372,54 @@ __device__ __forceinline__ void epi_chunk(const float (&v)[32], const float *__r
         make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
 }
 
+// Output stage of one row (the whole warp calls it): the head's 16 TMEM
+// columns at taddr, plus bias, to p.out as (sigma, r, g, b); or, for pruning,
+// the row's score reduced into its voxel's.
+template <int MODE>
+__device__ __forceinline__ void head_store(const MlpParams &p, const float *bias4, uint32_t taddr,
+                                           int64_t r, int64_t ns, int lane) {
+  float v[16];
+  tmem_ld16(taddr, v);
+  tmem_wait_ld();
+  fence_before_sync();
+  float sigma = v[0] + bias4[0];
+  if (MODE != kPrune) {
+    if (r < ns)
+      reinterpret_cast<float4 *>(p.out)[r] =
+          make_float4(sigma, v[1] + bias4[1], v[2] + bias4[2], v[3] + bias4[3]);
+  } else {
+    // reference rule (fairnr/modules/encoder.py:610, 648): exp(-relu s),
+    // reduced with min; workload rule: 1 - exp(-relu(s) * step), max.
+    // Both are >= 0, so their float bits order like unsigned ints. A warp
+    // whose rows all belong to one voxel reduces before its one atomic.
+    bool live = r < ns;
+    int64_t vv = live ? r / ((int64_t)p.bits * p.bits * p.bits) : -1;
+    uint32_t val;
+    if (p.rule == 0) val = __float_as_uint(expf(-fmaxf(sigma, 0.0f)));
+    else val = __float_as_uint(fmaxf(1.0f - expf(-(fmaxf(sigma, 0.0f) * p.step)), 0.0f));
+    int64_t v0 = __shfl_sync(0xffffffffu, vv, 0);
+    if (__all_sync(0xffffffffu, vv == v0 && live)) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        uint32_t y = __shfl_xor_sync(0xffffffffu, val, o);
+        val = (p.rule == 0) ? min(val, y) : max(val, y);
+      }
+      if (lane == 0) {
+        if (p.rule == 0) atomicMin(p.score + v0, val);
+        else atomicMax(p.score + v0, val);
+      }
+    } else if (live) {
+      if (p.rule == 0) atomicMin(p.score + vv, val);
+      else atomicMax(p.score + vv, val);
+    }
+  }
+}
+
 // Persistent CTA (one per SM), roles as in Cfg:
-//   epilogue warpgroups, one per tile slot g: bias + ReLU + rounding of each
-//                   hidden layer back to shared memory, and the output stage;
+//   epilogue warps  bias + ReLU + rounding of each hidden layer back to
+//                   shared memory, and the output stage. BF16: all 8 warps
+//                   on one slot's layer at a time, alternating the slots;
+//                   FP8: one warpgroup per tile slot g;
 //   MMA warp        TMEM allocation; lane 0 issues all tcgen05.mma;
 //   loader warps    two warpgroups that build the input tiles (the embedding
 //                   gathers and interpolation) into a ring of NB buffers
@@ -404,7 +449,9 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   if (tid == 0) {
     for (int g = 0; g < C::kSlots; ++g) {
       for (int l = 0; l < 5; ++l) mbar_init(&S.mma_done[g][l], 1);
-      mbar_init(&S.act_ready[g], 128);
+      // every epilogue thread arrives: BF16 has all 8 warps on each slot's
+      // layer, FP8 one warpgroup per slot
+      mbar_init(&S.act_ready[g], F8 ? 128 : 256);
     }
     for (int q = 0; q < NB; ++q) {
       mbar_init(&S.in_full[q], 128);
@@ -536,10 +583,57 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   } else {
     if constexpr (F8 && kEpiRegs8 < kLaunchRegs8)
       asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kEpiRegs8));
-    // Epilogue warpgroups. Every wait result is taken warp-uniformly
+    // Epilogue warps. Every wait result is taken warp-uniformly
     // (__all_sync), so the .sync.aligned tcgen05.ld and the warp shuffles
     // below always run with all 32 lanes, also when a timeout makes the CTA
     // unwind.
+    if constexpr (!F8) {
+      // BF16: the 8 warps work on one slot's layer at a time (warp w: TMEM
+      // lane quarter w & 3, columns [64 (w >> 2), + 64)) and alternate the
+      // two slots layer by layer, so that one slot's MMAs run while the
+      // warps convert the other slot's activations. The MMA lane issues in
+      // the same order (per tile pair: layer by layer, slot 0 then slot 1).
+      const int q4 = warp & 3, h = warp >> 2;
+      const int row = q4 * 32 + lane;
+      const uint32_t tq = tmem + ((uint32_t)(q4 * 32) << 16);
+      bool ok = true;
+      for (int64_t i = 0; ok; i += 2) {
+        if (tile_of(i) >= n_tiles) break;
+        const int ng = tile_of(i + 1) < n_tiles ? 2 : 1;
+        const uint32_t par = (uint32_t)((i / 2) & 1);
+        for (int layer = 0; layer < 4 && ok; ++layer) {
+          const float *bias = S.bias[layer];
+          for (int g = 0; g < ng; ++g) {
+            if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) {
+              ok = false;
+              break;
+            }
+            fence_after_sync();
+            const uint32_t tl = tq + C::kSlotCols * g + 64 * h;
+            uint8_t *ah = reinterpret_cast<uint8_t *>(S.ah[g]);
+            // two 32-column chunks, the second one's TMEM load in flight
+            // while the first is converted and stored
+            float va[32], vb[32];
+            tmem_ld32(tl, va);
+            tmem_wait_ld_bind(va);
+            tmem_ld32(tl + 32, vb);
+            epi_chunk(va, bias, ah, row, 64 * h);
+            tmem_wait_ld_bind(vb);
+            epi_chunk(vb, bias, ah, row, 64 * h + 32);
+            fence_before_sync();
+            fence_async_smem();
+            mbar_arrive(&S.act_ready[g]);
+          }
+        }
+        if (!ok) break;
+        // the head of slot g is written by the warps of half h == g
+        if (h < ng) {
+          if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[h][4], par, abort))) break;
+          fence_after_sync();
+          head_store<MODE>(p, S.bias4, tq + C::head_col(h), tile_of(i + h) * TILE + row, ns, lane);
+        }
+      }
+    } else {
     const int g = warp >> 2, q4 = warp & 3;
     const int row = q4 * 32 + lane;
     const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + C::kSlotCols * g;
@@ -557,7 +651,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         // 32-column chunks, the next one's TMEM load in flight while this
         // one is converted and stored
         float va[32], vb[32];
-        if (F8) {
+        {
           // layers 0-2 feed E4M3 layers; layer 3 feeds the BF16 head. The
           // next chunk's TMEM load is in flight while this one is stored.
           if (layer < 3) {
@@ -584,19 +678,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
               epi_chunk_dq(vb, bias, dq, ah, row, c + 32);
             }
           }
-        } else {
-          tmem_ld32(tl, va);
-          tmem_wait_ld_bind(va);
-          tmem_ld32(tl + 32, vb);
-          epi_chunk(va, bias, ah, row, 0);
-          tmem_wait_ld_bind(vb);
-          tmem_ld32(tl + 64, va);
-          epi_chunk(vb, bias, ah, row, 32);
-          tmem_wait_ld_bind(va);
-          tmem_ld32(tl + 96, vb);
-          epi_chunk(va, bias, ah, row, 64);
-          tmem_wait_ld_bind(vb);
-          epi_chunk(vb, bias, ah, row, 96);
         }
         fence_before_sync();
         fence_async_smem();
@@ -605,41 +686,8 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       if (!ok) break;
       if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) { ok = false; break; }
       fence_after_sync();
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + C::head_col(g), v);
-      tmem_wait_ld();
-      fence_before_sync();
-      float sigma = v[0] + S.bias4[0];
-      if (MODE != kPrune) {
-        if (r < ns)
-          reinterpret_cast<float4 *>(p.out)[r] =
-              make_float4(sigma, v[1] + S.bias4[1], v[2] + S.bias4[2], v[3] + S.bias4[3]);
-      } else {
-        // reference rule (fairnr/modules/encoder.py:610, 648): exp(-relu s),
-        // reduced with min; workload rule: 1 - exp(-relu(s) * step), max.
-        // Both are >= 0, so their float bits order like unsigned ints. A warp
-        // whose rows all belong to one voxel reduces before its one atomic.
-        bool live = r < ns;
-        int64_t vv = live ? r / ((int64_t)p.bits * p.bits * p.bits) : -1;
-        uint32_t val;
-        if (p.rule == 0) val = __float_as_uint(expf(-fmaxf(sigma, 0.0f)));
-        else val = __float_as_uint(fmaxf(1.0f - expf(-(fmaxf(sigma, 0.0f) * p.step)), 0.0f));
-        int64_t v0 = __shfl_sync(0xffffffffu, vv, 0);
-        if (__all_sync(0xffffffffu, vv == v0 && live)) {
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            uint32_t y = __shfl_xor_sync(0xffffffffu, val, o);
-            val = (p.rule == 0) ? min(val, y) : max(val, y);
-          }
-          if (lane == 0) {
-            if (p.rule == 0) atomicMin(p.score + v0, val);
-            else atomicMax(p.score + v0, val);
-          }
-        } else if (live) {
-          if (p.rule == 0) atomicMin(p.score + vv, val);
-          else atomicMax(p.score + vv, val);
-        }
-      }
+      head_store<MODE>(p, S.bias4, tmem + ((uint32_t)(q4 * 32) << 16) + C::head_col(g), r, ns, lane);
+    }
     }
   }
   fence_before_sync();
@@ -717,6 +765,23 @@ bool set_weights_fp8(MlpParams &p, const void *const weights[5], const float *co
   p.qs[3] = 1.0f;
   for (int l = 0; l < 3; ++l) p.dqs[l] = p.dq[l] * p.qs[l];
   return true;
+}
+
+// One CTA waits, with the kernels' bounded wait, on an mbarrier phase that
+// never completes (nothing arrives). The wait gives up after limit_ns; the
+// kernel records bit 3 (8) in err, as the MLP kernels do on a timeout, and
+// returns normally.
+__global__ void wait_timeout_kernel(uint64_t limit_ns, int32_t *err) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar, 0, &abort_flag, limit_ns));
+  if (!ok && threadIdx.x == 0 && err) atomicOr(err, 8);
 }
 
 }  // namespace
@@ -874,6 +939,12 @@ int nsvf_field_samples_fp8(int64_t n_samples, const int32_t *voxel, const float 
   p.ns = n_samples;
   p.err = err;
   return launch_mlp<kSamplesIn, true>(p, (cudaStream_t)stream);
+}
+
+int nsvf_wait_timeout_selftest(uint64_t limit_ns, int32_t *err, void *stream) {
+  if (!err || limit_ns == 0 || limit_ns > 1000000000ull) return NSVF_ERR_INVALID;
+  wait_timeout_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(limit_ns, err);
+  return nsvf_launch_status();
 }
 
 }  // extern "C"

@@ -203,20 +203,35 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   return t;
 }
 
+// try_wait with a suspend-time hint: a thread whose phase is not complete
+// sleeps until the phase completes or `hint_ns` passes, instead of polling
+// the barrier (each poll is a shared-memory access).
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait: gives up after `limit_ns` (default 2 s) or as soon as
 // *abort is set by another thread; returns false then (the caller records an
-// error and unwinds).
+// error and unwinds). Between checks of *abort and the clock a thread sleeps
+// in try_wait for at most 0.5 ms.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           uint64_t limit_ns = 2000000000ull) {
   uint64_t t0 = 0;
   for (uint32_t i = 0;; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity, 500000u)) return true;
     if (*abort) return false;
-    if ((i & 255) == 0) {
-      uint64_t t = globaltimer_ns();
-      if (i == 0) t0 = t;
-      else if (t - t0 > limit_ns) break;
-    }
+    uint64_t t = globaltimer_ns();
+    if (i == 0) t0 = t;
+    else if (t - t0 > limit_ns) break;
   }
   *abort = 1;
   return false;

@@ -2,10 +2,13 @@
 paths against a float64 render of the same samples.
 
 The float64 render is the validation oracle on the GPU (FP64 is used nowhere
-else). It takes the drop-in path's own geometry, which is FP32 and
-bit-identical to the reference's operation sequence: hit lists, sample
-depths, distances and voxel ids. It recomputes interpolation, the field MLP
-and compositing in float64 with torch:
+else). It takes the FP32 geometry of the path it checks: hit lists, sample
+depths, distances and voxel ids. For the drop-in path that geometry is
+bit-identical to the reference's operation sequence; the served path's
+differs only in the order of the per-ray sum that sets its sampling
+distribution, so it gets a float64 render of its own samples. The render
+recomputes interpolation, the field MLP and compositing in float64 with
+torch:
 
   emb = sum_k w_k values[feats[v, k]]     (fairnr/modules/encoder.py:584-590)
   fe  = relu(sigma) * dist * 7            (fairnr/modules/renderer.py:117-121)
@@ -27,14 +30,41 @@ over all pixels and over the pixels that have none.
 """
 import torch
 
+from . import ext
+from ._lib import LIB, check
 from .renderer import render_rays
 from .served import SceneState, render_frame
 
 
+def _served_rows(inter, pix, step_size):
+    """The hit rows of rays `pix` with the served path's sampling
+    distribution (nsvf_gather_probs: the per-ray sum in its fixed warp
+    order)."""
+    idx = inter['intersected_voxel_idx']
+    H = idx.size(-1)
+    dev = idx.device
+    idx = idx.reshape(-1, H).int().contiguous()
+    lo = inter['min_depth'].reshape(-1, H).float().contiguous()
+    hi = inter['max_depth'].reshape(-1, H).float().contiguous()
+    n = pix.numel()
+    n_dev = torch.tensor([n], dtype=torch.int64, device=dev)
+    I = torch.empty(n, H, dtype=torch.int32, device=dev)
+    L, U, probs = (torch.empty(n, H, device=dev) for _ in range(3))
+    steps = torch.empty(n, device=dev)
+    check(LIB.nsvf_gather_probs(n, n_dev.data_ptr(), H, float(step_size), pix.data_ptr(),
+                                idx.data_ptr(), lo.data_ptr(), hi.data_ptr(), I.data_ptr(),
+                                L.data_ptr(), U.data_ptr(), probs.data_ptr(), steps.data_ptr(),
+                                ext.ctypes_stream(dev)), "gather_probs")
+    return {'intersected_voxel_idx': I, 'min_depth': L, 'max_depth': U, 'probs': probs,
+            'steps': steps}
+
+
 @torch.no_grad()
-def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
+def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768, served=False):
     """Float64 colours [R, 3] and depths [R] of the rays (ray_start [3],
-    ray_dir [R, 3] on the encoder's device)."""
+    ray_dir [R, 3] on the encoder's device). served: sample with the served
+    path's distribution (its per-ray sum order) instead of the drop-in
+    path's, so that the samples are the served frame's own."""
     dev = ray_dir.device
     R = ray_dir.shape[0]
     st = encoder.precompute(id=None)
@@ -42,13 +72,16 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
     rd4 = ray_dir.reshape(1, 1, -1, 3)
     _, _, inter, hits = encoder.ray_intersect(rs4, rd4, {k: (v.unsqueeze(0) if v is not None else None)
                                                          for k, v in st.items()})
-    d = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
-    inter['probs'] = d / d.sum(-1, keepdim=True)
-    inter['steps'] = d.sum(-1) / encoder.step_size
     hits = hits.reshape(-1)
     pix = hits.nonzero().squeeze(1)
-    sub = {k: v.reshape(-1, v.shape[-1])[pix] for k, v in inter.items() if k != 'steps'}
-    sub['steps'] = inter['steps'].reshape(-1)[pix]
+    if served:
+        sub = _served_rows(inter, pix, encoder.step_size)
+    else:
+        d = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
+        inter['probs'] = d / d.sum(-1, keepdim=True)
+        inter['steps'] = d.sum(-1) / encoder.step_size
+        sub = {k: v.reshape(-1, v.shape[-1])[pix] for k, v in inter.items() if k != 'steps'}
+        sub['steps'] = inter['steps'].reshape(-1)[pix]
     samples = encoder.ray_sample(sub)
     centers = st['voxel_center_xyz'].double()
     feats = st['voxel_vertex_idx']
@@ -100,8 +133,10 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
 
 
 def report(encoder, field, renderer, ray_start, ray_dir):
-    """Errors of the served BF16 and the drop-in FP32 frame against float64."""
+    """Errors of the served BF16 and FP8 frames and of the drop-in FP32 frame,
+    each against a float64 render of its own samples."""
     ref_c, ref_d, hits, foreign, n_foreign = fp64_render(encoder, field, ray_start, ray_dir)
+    srv_c, srv_d, _, srv_foreign, _ = fp64_render(encoder, field, ray_start, ray_dir, served=True)
     scene = SceneState(encoder, field)
     served = render_frame(scene, ray_start, ray_dir)
     served8 = render_frame(scene, ray_start, ray_dir, mlp="tc_fp8")
@@ -109,12 +144,14 @@ def report(encoder, field, renderer, ray_start, ray_dir):
         plain = render_rays(encoder, field, renderer, ray_start.reshape(1, 1, 1, 3),
                             ray_dir.reshape(1, 1, -1, 3))
     out = {}
-    for name, c, d in [("served_bf16", served["colors"], served["depths"]),
-                       ("served_fp8", served8["colors"], served8["depths"]),
-                       ("plain_fp32", plain["colors"].reshape(-1, 3), plain["depths"].reshape(-1))]:
-        e = (c.double() - ref_c).abs()
-        de = (d.double() - ref_d).abs()[hits]
-        clean = e[~foreign]
+    for name, c, d, rc, rdp, fr in [
+            ("served_bf16", served["colors"], served["depths"], srv_c, srv_d, srv_foreign),
+            ("served_fp8", served8["colors"], served8["depths"], srv_c, srv_d, srv_foreign),
+            ("plain_fp32", plain["colors"].reshape(-1, 3), plain["depths"].reshape(-1), ref_c, ref_d,
+             foreign)]:
+        e = (c.double() - rc).abs()
+        de = (d.double() - rdp).abs()[hits]
+        clean = e[~fr]
         out[name] = {"max_rgb_err": float(e.max()), "rms_rgb_err": float(e.pow(2).mean().sqrt()),
                      "max_depth_err_hit_pixels": float(de.max()) if de.numel() else 0.0,
                      "max_rgb_err_clean_pixels": float(clean.max()) if clean.numel() else 0.0,

@@ -155,3 +155,27 @@ def test_fp8_hidden_layers_match_emulation(golden, cuda):
     assert stats["median_vs_emulation"] <= 2e-3, stats
     assert stats["max_vs_emulation"] <= 5e-2, stats
     assert stats["max_vs_fp32"] <= 0.15, stats
+
+
+def test_bounded_wait_times_out_and_leaves_the_context_usable(cuda):
+    """The tensor-core kernels' waits are bounded: a wait on an mbarrier
+    phase that never completes gives up after its limit, records bit 3 (8)
+    in the error word and returns; the next launch runs normally."""
+    import time
+    from nsvf_gb300 import ext, scenes
+    from nsvf_gb300._lib import LIB
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.mlp import TensorCoreMLP
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    t0 = time.perf_counter()
+    assert LIB.nsvf_wait_timeout_selftest(2_000_000, err.data_ptr(), ext.ctypes_stream(cuda)) == 0
+    torch.cuda.synchronize(cuda)
+    assert time.perf_counter() - t0 < 5.0
+    assert int(err.item()) == 8
+    field = StandInField(weights=scenes.stand_in_mlp_weights(seed=3)).to(cuda)
+    mlp = TensorCoreMLP(field)
+    emb = torch.randn(1000, 32, device=cuda)
+    out = mlp(emb)
+    ext.check_errors(cuda)
+    np.testing.assert_allclose(out.cpu().numpy(), mlp.reference_bf16(emb).cpu().numpy(),
+                               atol=2e-3 * (out.abs().max().item() + 1e-6), rtol=1e-2)

@@ -1,9 +1,12 @@
 """The served renderer (compacted samples, tcgen05 BF16 MLP, compensated
 compositing) against the drop-in FP32 path and the float64 oracle.
 
-The geometry is shared: the served path must evaluate exactly the samples
-the drop-in path evaluates (same count, same voxel ids). Colours: BF16 field
-vs the FP32 render within 2e-3 max abs RGB error, the workload's bar."""
+The geometry is shared: given the same sampling distribution, the served
+path evaluates exactly the samples the drop-in path evaluates (same count,
+same voxel ids). Its distribution sums each ray's segment lengths in a fixed
+warp order (nsvf_gather_probs, pinned bit for bit below) rather than in
+torch's reduction order. Colours: BF16 field vs the FP32 render within 2e-3
+max abs RGB error, the workload's bar."""
 import argparse
 
 import numpy as np
@@ -76,13 +79,66 @@ def test_served_matches_dropin(cuda, voxel, size, std, ss, sb, H):
         _, _, inter, hits = enc.ray_intersect(rs_t.reshape(1, 1, 1, 3), rd_t.reshape(1, 1, -1, 3),
                                               {k: (v.unsqueeze(0) if v is not None else None)
                                                for k, v in st.items()})
+        pix = hits.reshape(-1).nonzero().squeeze(1)
+        smp = enc.ray_sample(_served_rows(inter, pix, enc.step_size))
         d = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
         inter['probs'] = d / d.sum(-1, keepdim=True)
         inter['steps'] = d.sum(-1) / enc.step_size
         sub = {k: v[hits] for k, v in inter.items()}
-        smp = enc.ray_sample(sub)
+        smp_t = enc.ray_sample(sub)
+    # the served distribution: exactly the drop-in path's samples
     assert out["n_samples"] == int(smp['sampled_point_voxel_idx'].ne(-1).sum())
     assert out["n_hit_rays"] == int(hits.sum())
+    # torch's sum order: the same samples up to the rays whose sum rounds
+    # across a step count
+    n_t = int(smp_t['sampled_point_voxel_idx'].ne(-1).sum())
+    assert abs(out["n_samples"] - n_t) <= max(2, n_t // 1000), (out["n_samples"], n_t)
+
+
+def _served_rows(inter, pix, step):
+    from nsvf_gb300.precision import _served_rows as rows
+    return rows(inter, pix, step)
+
+
+@pytest.mark.parametrize("H", [20, 64, 100])
+def test_gather_probs_fixed_warp_order(cuda, H):
+    """nsvf_gather_probs, bit for bit: rows of the listed rays, d = max - min
+    on hit slots, tot = lane partial sums (slots l, l + 32, ...) added by an
+    xor butterfly (16, 8, 4, 2, 1), probs = d / tot, steps = tot / step."""
+    from nsvf_gb300 import ext
+    from nsvf_gb300._lib import LIB
+    rng = np.random.RandomState(H)
+    R, step = 700, np.float32(1.0 / 256)
+    idx = rng.randint(0, 5000, (R, H)).astype(np.int32)
+    m = rng.randint(0, H + 1, R)
+    idx[np.arange(H)[None, :] >= m[:, None]] = -1
+    lo = (rng.rand(R, H) * 4).astype(np.float32)
+    hi = (lo + rng.rand(R, H).astype(np.float32) * np.float32(0.05)).astype(np.float32)
+    pix = np.nonzero(m > 0)[0].astype(np.int64)
+    n = pix.size
+    d = np.where(idx[pix] == -1, np.float32(0), hi[pix] - lo[pix]).astype(np.float32)
+    part = np.zeros((n, 32), np.float32)
+    for k in range(H):
+        part[:, k % 32] = part[:, k % 32] + d[:, k]
+    for o in (16, 8, 4, 2, 1):
+        part = part + part[:, np.arange(32) ^ o]
+    tot = part[:, :1]
+    assert np.array_equal(part, np.broadcast_to(tot, part.shape))
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    I = torch.empty(R, H, dtype=torch.int32, device=cuda)
+    L, U, probs = (torch.empty(R, H, device=cuda) for _ in range(3))
+    steps = torch.empty(R, device=cuda)
+    pix_d, idx_d, lo_d, hi_d = t(pix), t(idx), t(lo), t(hi)
+    n_d = torch.tensor([n], dtype=torch.int64, device=cuda)
+    assert LIB.nsvf_gather_probs(R, n_d.data_ptr(), H, float(step), pix_d.data_ptr(), idx_d.data_ptr(),
+                                 lo_d.data_ptr(), hi_d.data_ptr(), I.data_ptr(), L.data_ptr(),
+                                 U.data_ptr(), probs.data_ptr(), steps.data_ptr(),
+                                 ext.ctypes_stream(cuda)) == 0
+    assert np.array_equal(I[:n].cpu().numpy(), idx[pix])
+    assert np.array_equal(L[:n].cpu().numpy(), lo[pix])
+    assert np.array_equal(U[:n].cpu().numpy(), hi[pix])
+    assert np.array_equal(probs[:n].cpu().numpy(), d / tot)
+    assert np.array_equal(steps[:n].cpu().numpy(), tot[:, 0] / step)
 
 
 @pytest.mark.parametrize("std,ss,sb,max_err,rms_err", [
