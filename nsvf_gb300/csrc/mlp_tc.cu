@@ -59,6 +59,12 @@ struct Cfg {
   __device__ static constexpr uint32_t head_col(int g) {
     return F8 ? 384u + 16u * (uint32_t)g : 256u * (uint32_t)g + 128u;
   }
+  // BF16: TMEM column of slot g's activations, the A operand of its next
+  // layer (HID bf16 per row, two per column: 64 columns).
+  __device__ static constexpr uint32_t act_col(int g) { return 256u * (uint32_t)g + 192u; }
+  // BF16: 8 columns holding (1, 1, 1, 0, ...) in every lane: the A operand
+  // of the hidden layers' bias step.
+  __device__ static constexpr uint32_t ones_col(int g) { return 256u * (uint32_t)g + 144u; }
   static constexpr int kHidBytes = F8 ? HID * HID : HID * HID * 2;  // one hidden weight matrix
 };
 
@@ -80,7 +86,14 @@ struct __align__(128) MlpSmem {
   uint8_t wh[3][Cfg<F8>::kHidBytes];       // bf16 or E4M3 hidden weights
   __nv_bfloat16 w4[NOUT * HID];
   __nv_bfloat16 ain[NB][TILE * E];
-  __nv_bfloat16 ah[Cfg<F8>::kSlots][TILE * HID];  // E4M3 uses the first half
+  // FP8: the hidden activations (E4M3 uses the first half of each). BF16
+  // keeps its activations in tensor memory.
+  __nv_bfloat16 ah[F8 ? Cfg<F8>::kSlots : 1][F8 ? TILE * HID : 8];
+  // BF16: the bias step of each layer (an extra K = 16 MMA): B rows n =
+  // (hi, mid, lo, 0, ...) with hi + mid + lo = bias[l][n] (three bf16 terms),
+  // and, for the first layer, an A tile whose rows are (1, 1, 1, 0, ...).
+  __nv_bfloat16 bias_b[F8 ? 1 : 4][F8 ? 8 : HID * 16];
+  __nv_bfloat16 ones_a[F8 ? 8 : TILE * 16];
   // per loader warp: its 32 rows' corner keys (kSkipKey = skip) and
   // trilinear weights, written by the row's lane and read by the 8 lanes
   // that gather the row
@@ -192,6 +205,58 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const __nv_bfloat16
     uint64_t ad = sdesc(a0 + 256u * k, 128u, sbo);
     uint64_t bd = sdesc(b0 + 256u * k, 128u, sbo);
     mma_bf16(d_tmem, ad, bd, idesc, k > 0 ? 1u : 0u);
+  }
+}
+
+// The K / 16 MMAs of one BF16 layer from precomputed descriptors. A K = 16
+// step moves a no-swizzle K-major operand by 256 bytes, i.e. 16 in the
+// descriptor's address field (addresses stay below 256 KB, so the field does
+// not overflow). A from shared memory (ad) or, for issue_ts, from tensor
+// memory at column a_tmem (two bf16 per column: 8 columns per step).
+// ACC0: the first step accumulates onto D too (D holds the layer's bias).
+template <int KS, bool ACC0>
+__device__ __forceinline__ void issue_ss(uint32_t d_tmem, uint64_t ad, uint64_t bd, uint32_t idesc) {
+#pragma unroll
+  for (int k = 0; k < KS; ++k)
+    mma_bf16(d_tmem, ad + 16u * k, bd + 16u * k, idesc, (ACC0 || k > 0) ? 1u : 0u);
+}
+
+template <int KS, bool ACC0>
+__device__ __forceinline__ void issue_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bd,
+                                         uint32_t idesc) {
+#pragma unroll
+  for (int k = 0; k < KS; ++k)
+    mma_bf16_ts(d_tmem, a_tmem + 8u * k, bd + 16u * k, idesc, (ACC0 || k > 0) ? 1u : 0u);
+}
+
+// bf16 1.0 in the low half, and in both halves
+constexpr uint32_t kOne = 0x00003F80u, kOnes2 = 0x3F803F80u;
+
+// The bias step's operands (BF16), written once per CTA: row n of layer l's
+// B block is (hi, mid, lo, 0, ...) with hi = bf16(b), mid = bf16(b - hi),
+// lo = bf16(b - hi - mid) -- their sum is b to within the FP32 rounding of the
+// accumulation -- and every row of the first layer's A block is
+// (1, 1, 1, 0, ...). Both are no-swizzle K-major tiles with K = 16.
+__device__ __forceinline__ void stage_bias_step(__nv_bfloat16 (*bias_b)[HID * 16],
+                                                __nv_bfloat16 *ones_a,
+                                                const float *const *b, int tid, int nthreads) {
+  for (int i = tid; i < 4 * HID; i += nthreads) {
+    const int l = i / HID, n = i % HID;
+    const float v = b[l][n];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+    uint8_t *base = reinterpret_cast<uint8_t *>(bias_b[l]);
+    const uint32_t w01 = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(mid) << 16);
+    const uint32_t w23 = (uint32_t)__bfloat16_as_ushort(lo);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(n, 0, 16)) = make_uint4(w01, w23, 0u, 0u);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(n, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (int m = tid; m < TILE; m += nthreads) {
+    uint8_t *base = reinterpret_cast<uint8_t *>(ones_a);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(m, 0, 16)) = make_uint4(kOnes2, kOne, 0u, 0u);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(m, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
   }
 }
 
@@ -358,18 +423,18 @@ __device__ __forceinline__ void epi_chunk_dq(const float (&v)[32], const float *
         make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
 }
 
-// Hidden-layer epilogue of 32 columns [c, c + 32) of one row: bias, ReLU,
-// round to bf16, store into the K-major activation tile.
-__device__ __forceinline__ void epi_chunk(const float (&v)[32], const float *__restrict__ bias,
-                                          uint8_t *ah, int row, int c) {
-  uint32_t pk[16];
+// Hidden-layer epilogue of 32 columns [c, c + 32) of one row (the bias is
+// already in the accumulator): ReLU, round to bf16, and store the 16 packed
+// pairs into the row's activations in tensor memory (`ta`: this warp's
+// lanes, the slot's activation column).
+__device__ __forceinline__ void epi_chunk(const float (&v)[32], uint32_t ta, int c) {
 #pragma unroll
-  for (int j = 0; j < 16; ++j)
-    pk[j] = pack_relu_bf16x2(v[2 * j] + bias[c + 2 * j], v[2 * j + 1] + bias[c + 2 * j + 1]);
+  for (int q = 0; q < 2; ++q) {
+    uint32_t pk[8];
 #pragma unroll
-  for (int h = 0; h < 4; ++h)
-    *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8 * h, HID)) =
-        make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
+    for (int j = 0; j < 8; ++j) pk[j] = pack_relu_bf16x2(v[16 * q + 2 * j], v[16 * q + 2 * j + 1]);
+    tmem_st8(ta + (uint32_t)((c >> 1) + 8 * q), pk);
+  }
 }
 
 // Output stage of one row (the whole warp calls it): the head's 16 TMEM
@@ -441,6 +506,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     else stage_weights(reinterpret_cast<__nv_bfloat16 *>(S.wh[l]), p.w[l + 1], HID, HID, HID);
   }
   stage_weights(S.w4, p.w[4], NOUT, 4, HID);
+  if constexpr (!F8) stage_bias_step(S.bias_b, S.ones_a, p.b, tid, blockDim.x);
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
   if (F8)
     for (int i = tid; i < 3 * HID; i += blockDim.x)
@@ -449,12 +515,13 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   if (tid == 0) {
     for (int g = 0; g < C::kSlots; ++g) {
       for (int l = 0; l < 5; ++l) mbar_init(&S.mma_done[g][l], 1);
-      // every epilogue thread arrives: BF16 has all 8 warps on each slot's
-      // layer, FP8 one warpgroup per slot
-      mbar_init(&S.act_ready[g], F8 ? 128 : 256);
+      // one arrival per epilogue warp (lane 0, after the warp's fences and
+      // a __syncwarp): BF16 has all 8 warps on each slot's layer, FP8 one
+      // warpgroup per slot
+      mbar_init(&S.act_ready[g], F8 ? 4 : 8);
     }
     for (int q = 0; q < NB; ++q) {
-      mbar_init(&S.in_full[q], 128);
+      mbar_init(&S.in_full[q], 4);    // one arrival per loader warp
       mbar_init(&S.in_empty[q], 1);
     }
     S.abort = 0;
@@ -466,6 +533,20 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = S.tmem_base;
+  if constexpr (!F8) {
+    // BF16: each slot's ones block in tensor memory (the A operand of the
+    // hidden layers' bias step), written once by warps 0-3 (lane quarter =
+    // warp) and never changed
+    if (warp < 4) {
+      const uint32_t ones[8] = {kOnes2, kOne, 0u, 0u, 0u, 0u, 0u, 0u};
+      for (int g = 0; g < C::kSlots; ++g)
+        tmem_st8(tmem + ((uint32_t)(warp * 32) << 16) + C::ones_col(g), ones);
+      tmem_wait_st();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+  }
   volatile int *abort = &S.abort;
   // With ns_dev the row count comes from device memory (a count produced by
   // an earlier kernel on the stream), clamped to the buffers' capacity p.ns.
@@ -486,6 +567,19 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     if (warp == C::kMmaWarp && lane == 0) {
       uint32_t ph_act[C::kSlots] = {};
       bool ok = true;
+      // BF16 descriptors, computed once: the first layer's weights and input
+      // ring buffer 0 (buffer q is 8 KB further: + 512 in the address
+      // field), the first hidden layer's weights (layer l + 1: + 2048) and
+      // the head's weights.
+      const uint64_t d_in0 = sdesc(smem_u32(S.ain[0]), 128u, (E / 8) * 128u);
+      const uint64_t d_w0 = sdesc(smem_u32(S.w0), 128u, (E / 8) * 128u);
+      const uint64_t d_wh = sdesc(smem_u32(S.wh[0]), 128u, (HID / 8) * 128u);
+      const uint64_t d_w4 = sdesc(smem_u32(S.w4), 128u, (HID / 8) * 128u);
+      // the bias step: the first layer's ones block (A, shared memory) and
+      // layer l's bias block (B; + 256 per layer)
+      const uint64_t d_ones = sdesc(smem_u32(S.ones_a), 128u, 256u);
+      const uint64_t d_bias = sdesc(smem_u32(S.bias_b[0]), 128u, 256u);
+      static_assert(sizeof(S.ain[0]) == 8192 && C::kHidBytes == 32768 || F8, "descriptor steps");
 #pragma unroll 1
       for (int64_t i = 0; ok; i += C::kSlots) {
         if (tile_of(i) >= n_tiles) break;
@@ -500,7 +594,12 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
               int q = (int)(ii % NB);
               if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
               fence_after_sync();
-              issue_layer(d, S.ain[q], S.w0, E, HID);
+              if (F8) issue_layer(d, S.ain[q], S.w0, E, HID);
+              else {
+                // bias step (overwrites D), then the layer accumulating onto it
+                mma_bf16(d, d_ones, d_bias, idesc_bf16_f32(TILE, HID), 0u);
+                issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
+              }
               mma_commit(&S.mma_done[g][0]);
               mma_commit(&S.in_empty[q]);
             } else {
@@ -512,10 +611,17 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
                   issue_layer8(d, reinterpret_cast<const uint8_t *>(S.ah[g]), S.wh[layer - 1],
                                HID, HID);
                 else
-                  issue_layer(d, S.ah[g], reinterpret_cast<const __nv_bfloat16 *>(S.wh[layer - 1]),
-                              HID, HID);
-              } else {
+                {
+                  mma_bf16_ts(d, tmem + C::ones_col(g), d_bias + 256u * (uint32_t)layer,
+                              idesc_bf16_f32(TILE, HID), 0u);
+                  issue_ts<HID / 16, true>(d, tmem + C::act_col(g), d_wh + 2048u * (uint32_t)(layer - 1),
+                                           idesc_bf16_f32(TILE, HID));
+                }
+              } else if (F8) {
                 issue_layer(tmem + C::head_col(g), S.ah[g], S.w4, HID, NOUT);
+              } else {
+                issue_ts<HID / 16, false>(tmem + C::head_col(g), tmem + C::act_col(g), d_w4,
+                                   idesc_bf16_f32(TILE, NOUT));
               }
               mma_commit(&S.mma_done[g][layer]);
             }
@@ -577,8 +683,8 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       }
       if (bad && p.err) atomicOr(p.err, 4);
       fence_async_smem();
-      mbar_arrive(&S.in_full[q]);
-      __syncwarp();                     // pass 2's reads of the row table before the next pass 1
+      __syncwarp();                     // also orders pass 2's reads of the row table before the next pass 1
+      if (lane == 0) mbar_arrive(&S.in_full[q]);
     }
   } else {
     if constexpr (F8 && kEpiRegs8 < kLaunchRegs8)
@@ -602,7 +708,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         const int ng = tile_of(i + 1) < n_tiles ? 2 : 1;
         const uint32_t par = (uint32_t)((i / 2) & 1);
         for (int layer = 0; layer < 4 && ok; ++layer) {
-          const float *bias = S.bias[layer];
           for (int g = 0; g < ng; ++g) {
             if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) {
               ok = false;
@@ -610,19 +715,21 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
             }
             fence_after_sync();
             const uint32_t tl = tq + C::kSlotCols * g + 64 * h;
-            uint8_t *ah = reinterpret_cast<uint8_t *>(S.ah[g]);
+            const uint32_t ta = tq + C::act_col(g);
             // two 32-column chunks, the second one's TMEM load in flight
-            // while the first is converted and stored
+            // while the first is converted and stored back to tensor memory
+            // as the next layer's A operand
             float va[32], vb[32];
             tmem_ld32(tl, va);
             tmem_wait_ld_bind(va);
             tmem_ld32(tl + 32, vb);
-            epi_chunk(va, bias, ah, row, 64 * h);
+            epi_chunk(va, ta, 64 * h);
             tmem_wait_ld_bind(vb);
-            epi_chunk(vb, bias, ah, row, 64 * h + 32);
+            epi_chunk(vb, ta, 64 * h + 32);
+            tmem_wait_st();
             fence_before_sync();
-            fence_async_smem();
-            mbar_arrive(&S.act_ready[g]);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.act_ready[g]);
           }
         }
         if (!ok) break;
@@ -681,7 +788,8 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         }
         fence_before_sync();
         fence_async_smem();
-        mbar_arrive(&S.act_ready[g]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.act_ready[g]);
       }
       if (!ok) break;
       if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) { ok = false; break; }
