@@ -326,7 +326,11 @@ def serve_bench(dev, n_requests, rate=200.0, seed=0):
 # ------------------------------------------------------------- clocks ------
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms. start() is
+    called before the warm-up and waits for the first sample, so that
+    nvidia-smi's own start-up does not overlap the timed frames; mark() and
+    stop() bracket the timed region, whose samples (with the one just before
+    it) give the reported clocks."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -335,6 +339,7 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.first = 0
 
     def start(self):
         try:
@@ -343,8 +348,16 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 10.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
+
+    def mark(self):
+        """The timed region starts: samples from here on (and the last one
+        before) are the ones reported."""
+        self.first = max(0, len(self.lines) - 1)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -360,7 +373,7 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[self.first:]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -420,6 +433,8 @@ def run_ours(a):
                                    rd.reshape(1, 1, -1, 3), encoder_states=states)
 
     # --- device-resident timing (value) ---
+    clocks = ClockSampler(local)
+    clocks.start()
     ext.KERNEL_TIMING = True
     for i in range(a.warmup):
         step(*dev_in[i])
@@ -428,8 +443,7 @@ def run_ours(a):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
+    clocks.mark()
     times = []
     out_samples = [0]
     l0 = LIB.nsvf_launch_count()

@@ -158,14 +158,17 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
-// Store 8 consecutive 32-bit columns of this warp's 32 TMEM lanes.
+// Store 8 consecutive 32-bit columns of this warp's 32 TMEM lanes. No
+// "memory" clobber: the store touches tensor memory only, and its ordering
+// against other tcgen05 operations comes from tcgen05.wait::st and the
+// tcgen05 fences (volatile asm, which keep their order); shared-memory loads
+// may move across it.
 __device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&r)[8]) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n"
       :
       : "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
-        "r"(r[7])
-      : "memory");
+        "r"(r[7]));
 }
 
 // Wait until this thread's tcgen05.st stores are done.
