@@ -108,24 +108,28 @@ __global__ void pack_octree_kernel(int64_t total, int n, float hv, const float *
 }
 
 constexpr int kSvoLevels = 16;
-constexpr int kRaysPerWarp = 4;                       // 8 lanes per ray
-constexpr int kRaysPerBlock = kRayBlock / 8;          // 16
+constexpr int kLanesPerRay = 4;                       // lane j owns children j and j + 4
+constexpr int kRaysPerWarp = 32 / kLanesPerRay;       // 8
+constexpr int kRaysPerBlock = kRayBlock / kLanesPerRay;  // 32
 
 // Warp-cooperative depth-first traversal in the reference's visiting order
 // (children 7..0 of every hit node, fairnr/clib/src/intersect_gpu.cu:200-235).
 //
-// A warp walks 4 rays; the 8 lanes of a ray's group each own one child slot.
-// Expanding a node = lane j loads child j's id and box and runs the slab
-// test; ballots give the node's 8-bit masks of hit children and hit leaves.
-// The descent stack is spread over the group: lane j keeps, for levels j and
-// j + 8, the mask of hit children not visited yet (and which of them are
-// leaves); the child ids of each level sit in shared memory. The next node
-// to expand -- the highest unvisited child of the deepest non-empty level --
-// comes from two ballots and a shuffle, the same on all 8 lanes.
+// A warp walks 8 rays; the 4 lanes of a ray's group each own two child
+// slots (lane j: children j and j + 4). Expanding a node = each lane loads
+// its two children's ids and boxes and runs their slab tests; ballots give
+// the node's 8-bit masks of hit children and hit leaves. The descent stack
+// is spread over the group: lane j keeps, for levels j, j + 4, j + 8 and
+// j + 12 (one byte each), the mask of hit children not visited yet (and
+// which of them are leaves); the child ids of each level sit in shared
+// memory. The next node to expand -- the highest unvisited child of the
+// deepest non-empty level -- comes from four ballots and a shuffle, the same
+// on all 4 lanes. The per-ray bookkeeping (ballots, stack, pick) is shared by
+// twice as many rays per warp instruction as with one child per lane.
 // When every hit child of a node is a leaf -- always the case for trees made
 // by build_octree, whose leaves all sit under depth-0 nodes -- the DFS visits
-// them consecutively, so the group emits them at once, lane j writing at
-// cnt + (number of hit leaves with a higher index). A leaf met on the stack
+// them consecutively, so the group emits them at once, the lane of child c
+// writing at cnt + (number of hit leaves with a higher index). A leaf met on the stack
 // (a node with both leaf and internal children) is emitted on its own. The
 // emitted order, the n_max cutoff and every (lo, hi) are the reference's.
 // Hits go straight into the output row.
@@ -201,14 +205,14 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     const int32_t *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
     float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
   // per ray and stack level: the expanded node's 8 child ids (lane j writes
-  // child j) and the node's id
+  // children j and j + 4) and the node's id
   __shared__ int s_child[kSvoLevels * kRaysPerBlock * 8];
   __shared__ int s_node[kSvoLevels * kRaysPerBlock];
   const uint32_t full = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int grp = lane >> 3, j = lane & 7;           // ray slot in the warp, child slot
-  const int g0 = lane & ~7;                          // the group's first lane
-  const uint32_t gshift = 8u * grp;
+  const int grp = lane >> 2, j = lane & 3;           // ray slot in the warp, child slots j, j + 4
+  const int g0 = lane & ~3;                          // the group's first lane
+  const uint32_t gshift = 4u * grp;
   const int slot = warp * kRaysPerWarp + grp;        // ray slot in the block
   const int64_t r = (int64_t)blockIdx.x * kRaysPerBlock + slot;
   const bool live = r < rays;
@@ -223,7 +227,7 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   const float ix = nsvf_rcp(ray_dir[rr * 3 + 0]), iy = nsvf_rcp(ray_dir[rr * 3 + 1]),
               iz = nsvf_rcp(ray_dir[rr * 3 + 2]);
   // the compare/select-light slab test for rays without a zero direction
-  // component (the same on the group's 8 lanes)
+  // component (the same on the group's 4 lanes)
   const bool fast = isfinite(ix) && isfinite(iy) && isfinite(iz);
   const float sx = ix >= 0.0f ? 1.0f : -1.0f, sy = iy >= 0.0f ? 1.0f : -1.0f,
               sz = iz >= 0.0f ? 1.0f : -1.0f;
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
       level = 0;
     }
   }
-  // lane j's share of the stack: bits [0, 8) level j, bits [8, 16) level j + 8
+  // lane j's share of the stack: byte k holds level j + 4 k
   uint32_t stk = 0, stl = 0;            // unvisited hit children; those that are leaves
   int node = n - 1;                      // the node to expand next (valid when `expand`)
   bool expand = level == 0;
@@ -255,43 +259,59 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   // Every group runs the loop until all groups of the warp are done. All
   // warp-wide operations run on all 32 lanes every iteration; only
   // lane-local work is predicated on `expand` / `pick`. Every value the
-  // group steers by (level, cnt, node, top, t, u) is the same on its 8 lanes.
+  // group steers by (level, cnt, node, top, t, u) is the same on its 4 lanes.
   while (__any_sync(full, expand)) {
-    // 1. expand `node`: lane j tests child j
-    bool hit = false;
-    float lo = 0.0f, hi = 0.0f, bw = 0.0f;
-    int cid = -1;
+    // 1. expand `node`: lane j tests children j (a) and j + 4 (b)
+    bool hit_a = false, hit_b = false;
+    float lo_a = 0.0f, hi_a = 0.0f, bw_a = 0.0f, lo_b = 0.0f, hi_b = 0.0f, bw_b = 0.0f;
+    int cid_a = -1, cid_b = -1;
     if (expand) {
       const int64_t kb = (int64_t)node * 8 + j;
-      cid = KD[kb];
-      if (cid > -1) {
-        if (cid >= n) {
+      cid_a = KD[kb];
+      cid_b = KD[kb + 4];
+      if (cid_a > -1) {
+        if (cid_a >= n) {
           bad = true;
         } else {
           float4 b = CB[kb];
-          bw = b.w;
-          hit = slab(b.x, b.y, b.z, fabsf(b.w), lo, hi);
+          bw_a = b.w;
+          hit_a = slab(b.x, b.y, b.z, fabsf(b.w), lo_a, hi_a);
+        }
+      }
+      if (cid_b > -1) {
+        if (cid_b >= n) {
+          bad = true;
+        } else {
+          float4 b = CB[kb + 4];
+          bw_b = b.w;
+          hit_b = slab(b.x, b.y, b.z, fabsf(b.w), lo_b, hi_b);
         }
       }
     }
-    const uint32_t hm = (__ballot_sync(full, hit) >> gshift) & 0xffu;
-    const uint32_t lm = (__ballot_sync(full, hit && bw < 0.0f) >> gshift) & 0xffu;
+    const uint32_t hm = ((__ballot_sync(full, hit_a) >> gshift) & 0xfu) |
+                        (((__ballot_sync(full, hit_b) >> gshift) & 0xfu) << 4);
+    const uint32_t lm = ((__ballot_sync(full, hit_a && bw_a < 0.0f) >> gshift) & 0xfu) |
+                        (((__ballot_sync(full, hit_b && bw_b < 0.0f) >> gshift) & 0xfu) << 4);
     if (expand && ++steps > 8 * (int64_t)n) { bad = true; expand = false; }
     int top = level - 1;                  // deepest stack level that may hold children
     if (expand) {
       if (hm != 0 && hm == lm) {
         // all hit children are leaves: emit them now, highest index first
-        int before = __popc(hm >> (j + 1));
-        if (hit && cnt + before < n_max) {
-          I[cnt + before] = cid; LO[cnt + before] = lo; HI[cnt + before] = hi;
+        const int before_a = __popc(hm >> (j + 1)), before_b = __popc(hm >> (j + 5));
+        if (hit_a && cnt + before_a < n_max) {
+          I[cnt + before_a] = cid_a; LO[cnt + before_a] = lo_a; HI[cnt + before_a] = hi_a;
+        }
+        if (hit_b && cnt + before_b < n_max) {
+          I[cnt + before_b] = cid_b; LO[cnt + before_b] = lo_b; HI[cnt + before_b] = hi_b;
         }
         cnt = min(n_max, cnt + __popc(hm));
       } else if (hm != 0) {
         const int base = level * kRaysPerBlock + slot;
-        s_child[base * 8 + j] = cid;
+        s_child[base * 8 + j] = cid_a;
+        s_child[base * 8 + j + 4] = cid_b;
         if (j == 0) s_node[base] = node;
-        if (j == (level & 7)) {
-          const int sh = (level >> 3) * 8;
+        if (j == (level & 3)) {
+          const int sh = (level >> 2) * 8;
           stk = (stk & ~(0xffu << sh)) | (hm << sh);
           stl = (stl & ~(0xffu << sh)) | (lm << sh);
         }
@@ -305,20 +325,27 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     bool pick = expand && cnt < n_max;
     int next = -1;
     while (__any_sync(full, pick)) {
-      const uint32_t nz0 = __ballot_sync(full, pick && j <= top && (stk & 0xffu) != 0);
-      const uint32_t nz1 = __ballot_sync(full, pick && j + 8 <= top && (stk >> 8) != 0);
-      const uint32_t L = ((nz0 >> gshift) & 0xffu) | (((nz1 >> gshift) & 0xffu) << 8);
+      // bit l of L: level l (<= top) still has unvisited children. Level
+      // 4 k + j is byte k of lane j, so ballot k's group bits are levels
+      // 4 k .. 4 k + 3.
+      uint32_t L = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t nz =
+            __ballot_sync(full, pick && j + 4 * k <= top && ((stk >> (8 * k)) & 0xffu) != 0);
+        L |= ((nz >> gshift) & 0xfu) << (4 * k);
+      }
       const int t = (pick && L != 0) ? 31 - __clz(L) : -1;
       uint32_t mine = 0, isleaf = 0;
       int u = 0;
-      if (t >= 0 && j == (t & 7)) {
-        const int sh = (t >> 3) * 8;
+      if (t >= 0 && j == (t & 3)) {
+        const int sh = (t >> 2) * 8;
         mine = (stk >> sh) & 0xffu;
         u = 31 - __clz(mine);
         isleaf = (stl >> (sh + u)) & 1u;
         stk &= ~(1u << (sh + u));
       }
-      const int src = g0 + (t >= 0 ? (t & 7) : 0);
+      const int src = g0 + (t >= 0 ? (t & 3) : 0);
       u = __shfl_sync(full, u, src);
       isleaf = __shfl_sync(full, isleaf, src);
       if (pick) {
@@ -359,8 +386,8 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   // rows: sorted variant sorts (and pads) every row with a hit and pads the
   // empty ones; the raw variant pads with (-1, 0, 0)
   for (int q = 0; q < kRaysPerWarp; ++q) {
-    int cq = __shfl_sync(0xffffffffu, cnt, q * 8);
-    bool lq = __shfl_sync(0xffffffffu, (int)live, q * 8) != 0;
+    int cq = __shfl_sync(0xffffffffu, cnt, q * kLanesPerRay);
+    bool lq = __shfl_sync(0xffffffffu, (int)live, q * kLanesPerRay) != 0;
     if (!lq) continue;
     int64_t rq = (int64_t)blockIdx.x * kRaysPerBlock + warp * kRaysPerWarp + q;
     int32_t *Iq = idx + rq * n_max;
