@@ -11,6 +11,8 @@
 #include <atomic>
 #include <mutex>
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace {
@@ -108,7 +110,7 @@ __global__ void pack_octree_kernel(int64_t total, int n, float hv, const float *
 }
 
 constexpr int kSvoLevels = 16;
-constexpr int kLanesPerRay = 4;                       // lane j owns children j and j + 4
+constexpr int kLanesPerRay = 4;                       // lane j owns children j + 4 c
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;       // 8
 constexpr int kRaysPerBlock = kRayBlock / kLanesPerRay;  // 32
 
@@ -205,14 +207,14 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     const int32_t *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
     float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
   // per ray and stack level: the expanded node's 8 child ids (lane j writes
-  // children j and j + 4) and the node's id
+  // children j + P c) and the node's id
   __shared__ int s_child[kSvoLevels * kRaysPerBlock * 8];
   __shared__ int s_node[kSvoLevels * kRaysPerBlock];
   const uint32_t full = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int grp = lane >> 2, j = lane & 3;           // ray slot in the warp, child slots j, j + 4
-  const int g0 = lane & ~3;                          // the group's first lane
-  const uint32_t gshift = 4u * grp;
+  const int grp = lane / kLanesPerRay, j = lane % kLanesPerRay;  // ray slot, child slots j + P c
+  const int g0 = lane - j;                           // the group's first lane
+  const uint32_t gshift = (uint32_t)(kLanesPerRay * grp);
   const int slot = warp * kRaysPerWarp + grp;        // ray slot in the block
   const int64_t r = (int64_t)blockIdx.x * kRaysPerBlock + slot;
   const bool live = r < rays;
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   const float ix = nsvf_rcp(ray_dir[rr * 3 + 0]), iy = nsvf_rcp(ray_dir[rr * 3 + 1]),
               iz = nsvf_rcp(ray_dir[rr * 3 + 2]);
   // the compare/select-light slab test for rays without a zero direction
-  // component (the same on the group's 4 lanes)
+  // component (the same on the group's lanes)
   const bool fast = isfinite(ix) && isfinite(iy) && isfinite(iz);
   const float sx = ix >= 0.0f ? 1.0f : -1.0f, sy = iy >= 0.0f ? 1.0f : -1.0f,
               sz = iz >= 0.0f ? 1.0f : -1.0f;
@@ -251,69 +253,73 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
       level = 0;
     }
   }
-  // lane j's share of the stack: byte k holds level j + 4 k
-  uint32_t stk = 0, stl = 0;            // unvisited hit children; those that are leaves
+  // lane j's share of the stack: byte k holds level j + P k (P lanes per ray)
+  constexpr int P = kLanesPerRay, NC = 8 / P, NLV = kSvoLevels / P;
+  constexpr uint32_t PM = (1u << P) - 1u;
+  using Stack = typename std::conditional<(NLV * 8 > 32), uint64_t, uint32_t>::type;
+  Stack stk = 0, stl = 0;               // unvisited hit children; those that are leaves
   int node = n - 1;                      // the node to expand next (valid when `expand`)
   bool expand = level == 0;
   int64_t steps = 0;
   // Every group runs the loop until all groups of the warp are done. All
   // warp-wide operations run on all 32 lanes every iteration; only
   // lane-local work is predicated on `expand` / `pick`. Every value the
-  // group steers by (level, cnt, node, top, t, u) is the same on its 4 lanes.
+  // group steers by (level, cnt, node, top, t, u) is the same on its lanes.
   while (__any_sync(full, expand)) {
-    // 1. expand `node`: lane j tests children j (a) and j + 4 (b)
-    bool hit_a = false, hit_b = false;
-    float lo_a = 0.0f, hi_a = 0.0f, bw_a = 0.0f, lo_b = 0.0f, hi_b = 0.0f, bw_b = 0.0f;
-    int cid_a = -1, cid_b = -1;
+    // 1. expand `node`: lane j tests children j + P c
+    bool hit[NC];
+    float clo[NC], chi[NC], cbw[NC];
+    int cid[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      hit[c] = false;
+      clo[c] = chi[c] = cbw[c] = 0.0f;
+      cid[c] = -1;
+    }
     if (expand) {
       const int64_t kb = (int64_t)node * 8 + j;
-      cid_a = KD[kb];
-      cid_b = KD[kb + 4];
-      if (cid_a > -1) {
-        if (cid_a >= n) {
-          bad = true;
-        } else {
-          float4 b = CB[kb];
-          bw_a = b.w;
-          hit_a = slab(b.x, b.y, b.z, fabsf(b.w), lo_a, hi_a);
-        }
-      }
-      if (cid_b > -1) {
-        if (cid_b >= n) {
-          bad = true;
-        } else {
-          float4 b = CB[kb + 4];
-          bw_b = b.w;
-          hit_b = slab(b.x, b.y, b.z, fabsf(b.w), lo_b, hi_b);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        cid[c] = KD[kb + P * c];
+        if (cid[c] > -1) {
+          if (cid[c] >= n) {
+            bad = true;
+          } else {
+            float4 b = CB[kb + P * c];
+            cbw[c] = b.w;
+            hit[c] = slab(b.x, b.y, b.z, fabsf(b.w), clo[c], chi[c]);
+          }
         }
       }
     }
-    const uint32_t hm = ((__ballot_sync(full, hit_a) >> gshift) & 0xfu) |
-                        (((__ballot_sync(full, hit_b) >> gshift) & 0xfu) << 4);
-    const uint32_t lm = ((__ballot_sync(full, hit_a && bw_a < 0.0f) >> gshift) & 0xfu) |
-                        (((__ballot_sync(full, hit_b && bw_b < 0.0f) >> gshift) & 0xfu) << 4);
+    uint32_t hm = 0, lm = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      hm |= ((__ballot_sync(full, hit[c]) >> gshift) & PM) << (P * c);
+      lm |= ((__ballot_sync(full, hit[c] && cbw[c] < 0.0f) >> gshift) & PM) << (P * c);
+    }
     if (expand && ++steps > 8 * (int64_t)n) { bad = true; expand = false; }
     int top = level - 1;                  // deepest stack level that may hold children
     if (expand) {
       if (hm != 0 && hm == lm) {
         // all hit children are leaves: emit them now, highest index first
-        const int before_a = __popc(hm >> (j + 1)), before_b = __popc(hm >> (j + 5));
-        if (hit_a && cnt + before_a < n_max) {
-          I[cnt + before_a] = cid_a; LO[cnt + before_a] = lo_a; HI[cnt + before_a] = hi_a;
-        }
-        if (hit_b && cnt + before_b < n_max) {
-          I[cnt + before_b] = cid_b; LO[cnt + before_b] = lo_b; HI[cnt + before_b] = hi_b;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const int before = __popc(hm >> (j + P * c + 1));
+          if (hit[c] && cnt + before < n_max) {
+            I[cnt + before] = cid[c]; LO[cnt + before] = clo[c]; HI[cnt + before] = chi[c];
+          }
         }
         cnt = min(n_max, cnt + __popc(hm));
       } else if (hm != 0) {
         const int base = level * kRaysPerBlock + slot;
-        s_child[base * 8 + j] = cid_a;
-        s_child[base * 8 + j + 4] = cid_b;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) s_child[base * 8 + j + P * c] = cid[c];
         if (j == 0) s_node[base] = node;
-        if (j == (level & 3)) {
-          const int sh = (level >> 2) * 8;
-          stk = (stk & ~(0xffu << sh)) | (hm << sh);
-          stl = (stl & ~(0xffu << sh)) | (lm << sh);
+        if (j == level % P) {
+          const int sh = (level / P) * 8;
+          stk = (stk & ~((Stack)0xffu << sh)) | ((Stack)hm << sh);
+          stl = (stl & ~((Stack)0xffu << sh)) | ((Stack)lm << sh);
         }
         top = level;
       }
@@ -326,26 +332,26 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int next = -1;
     while (__any_sync(full, pick)) {
       // bit l of L: level l (<= top) still has unvisited children. Level
-      // 4 k + j is byte k of lane j, so ballot k's group bits are levels
-      // 4 k .. 4 k + 3.
+      // P k + j is byte k of lane j, so ballot k's group bits are levels
+      // P k .. P k + P - 1.
       uint32_t L = 0;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const uint32_t nz =
-            __ballot_sync(full, pick && j + 4 * k <= top && ((stk >> (8 * k)) & 0xffu) != 0);
-        L |= ((nz >> gshift) & 0xfu) << (4 * k);
+      for (int k = 0; k < NLV; ++k) {
+        const uint32_t nz = __ballot_sync(
+            full, pick && j + P * k <= top && ((uint32_t)(stk >> (8 * k)) & 0xffu) != 0);
+        L |= ((nz >> gshift) & PM) << (P * k);
       }
       const int t = (pick && L != 0) ? 31 - __clz(L) : -1;
       uint32_t mine = 0, isleaf = 0;
       int u = 0;
-      if (t >= 0 && j == (t & 3)) {
-        const int sh = (t >> 2) * 8;
-        mine = (stk >> sh) & 0xffu;
+      if (t >= 0 && j == t % P) {
+        const int sh = (t / P) * 8;
+        mine = (uint32_t)(stk >> sh) & 0xffu;
         u = 31 - __clz(mine);
-        isleaf = (stl >> (sh + u)) & 1u;
-        stk &= ~(1u << (sh + u));
+        isleaf = (uint32_t)(stl >> (sh + u)) & 1u;
+        stk &= ~((Stack)1u << (sh + u));
       }
-      const int src = g0 + (t >= 0 ? (t & 3) : 0);
+      const int src = g0 + (t >= 0 ? t % P : 0);
       u = __shfl_sync(full, u, src);
       isleaf = __shfl_sync(full, isleaf, src);
       if (pick) {
