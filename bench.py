@@ -202,26 +202,38 @@ def prune_bench(dev, sc, bits=8, th=0.5):
     e0.record()
     torch.cuda.synchronize(dev)
     keep_bf16 = score >= th
-    s1, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s1.record()
     alpha = torch.empty(V, device=dev)
     hv = torch.tensor(vs / 2.0, device=dev)
     chunk = 8192
-    with torch.no_grad():
-        for i in range(0, V, chunk):
-            c = centers[i:i + chunk]
-            pts = geometry.offset_points(c, hv, bits=bits).reshape(-1, 3)
-            idx = torch.arange(i, i + c.shape[0], device=dev)[:, None].expand(-1, bits ** 3).reshape(-1)
-            emb = trilinear_embed(idx, pts, centers, feats, values, vs)
-            sig = field.mlp(emb)[:, 0].reshape(-1, bits ** 3)
-            alpha[i:i + c.shape[0]] = (1 - torch.exp(-torch.relu(sig) * step)).max(-1)[0]
-    e1.record()
+
+    def fp32_pass(stop):
+        with torch.no_grad():
+            for i in range(0, stop, chunk):
+                c = centers[i:i + chunk]
+                pts = geometry.offset_points(c, hv, bits=bits).reshape(-1, 3)
+                idx = torch.arange(i, i + c.shape[0], device=dev)[:, None].expand(-1, bits ** 3).reshape(-1)
+                emb = trilinear_embed(idx, pts, centers, feats, values, vs)
+                sig = field.mlp(emb)[:, 0].reshape(-1, bits ** 3)
+                alpha[i:i + c.shape[0]] = (1 - torch.exp(-torch.relu(sig) * step)).max(-1)[0]
+
+    # the FP32 path's time varies from run to run (cuBLAS SGEMM on
+    # multi-GB activations): one chunk of warm-up, then the faster of two
+    # timed passes
+    fp32_pass(min(V, chunk))
     torch.cuda.synchronize(dev)
+    fp32_ms = []
+    for _ in range(2):
+        s1, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s1.record()
+        fp32_pass(V)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        fp32_ms.append(s1.elapsed_time(e1))
     keep_fp32 = alpha >= th
     return {"workload": "c2 pruning pass: %d voxels x %d^3 points, keep max(1-exp(-relu(s)*step)) >= %g; "
                         "density row of the field scaled by %g" % (V, bits, th, PRUNE_SIGMA_SCALE),
             "alpha_fp32_median": float(alpha.median()),
-            "bf16_fused_ms": round(s0.elapsed_time(e0), 3), "fp32_ms": round(s1.elapsed_time(e1), 3),
+            "bf16_fused_ms": round(s0.elapsed_time(e0), 3), "fp32_ms": round(min(fp32_ms), 3), "fp32_ms_both": [round(t, 1) for t in fp32_ms],
             "tflop": round(107520.0 * V * bits ** 3 / 1e12, 2),
             "bf16_tflops_achieved": round(107520.0 * V * bits ** 3 / (s0.elapsed_time(e0) / 1e3) / 1e12, 1),
             "kept_bf16": int(keep_bf16.sum()), "kept_fp32": int(keep_fp32.sum()),

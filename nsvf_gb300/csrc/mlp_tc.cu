@@ -48,9 +48,9 @@ constexpr uint32_t kTmemCols = 512;
 //   FP8:  the hidden weights and activations take half the shared memory,
 //         which makes room for a third tile slot: 24 warps; three slots of
 //         128 TMEM columns (the head output reuses the slot's first 16);
-//         epilogue warps 0-11, loader warps 12-19, MMA warp 20 (21-23 only
-//         complete its warpgroup). The warpgroups rebalance registers with
-//         setmaxnreg (below).
+//         epilogue warps 0-11, loader warps 12-19, MMA warps 20-22 (one per
+//         slot; 23 only completes the warpgroup). The warpgroups rebalance
+//         registers with setmaxnreg (below).
 template <bool F8>
 struct Cfg {
   static constexpr int kSlots = F8 ? 3 : 2;
@@ -552,12 +552,14 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   const bool loader_role = warp >= C::kLoaderWarp0 && warp < C::kLoaderWarp0 + 8;
   if (mma_role) {
     if constexpr (F8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kMmaRegs8));
-    if ((warp == C::kMmaWarp || warp == C::kMmaWarp2) && lane == 0) {
-      // BF16: one issuing thread per slot (kMmaWarp: slot 0, kMmaWarp2: slot
-      // 1), so a slot whose activations are ready never waits behind the
-      // other slot's issue; FP8: one thread issues all slots in turn
-      const int g_lo = F8 ? 0 : (warp == C::kMmaWarp ? 0 : 1);
-      const int g_hi = F8 ? C::kSlots : g_lo + 1;
+    // One issuing thread per slot, so a slot whose activations are ready
+    // never waits behind another slot's issue. BF16: lane 0 of kMmaWarp
+    // (slot 0) and of kMmaWarp2 (slot 1); FP8: lane 0 of kMmaWarp + g for
+    // slot g (warps 20-22 of the MMA warpgroup).
+    const int issue_slot = F8 ? (warp - C::kMmaWarp < C::kSlots ? warp - C::kMmaWarp : -1)
+                              : (warp == C::kMmaWarp ? 0 : (warp == C::kMmaWarp2 ? 1 : -1));
+    if (issue_slot >= 0 && lane == 0) {
+      const int g_lo = issue_slot, g_hi = issue_slot + 1;
       uint32_t ph_act[C::kSlots] = {};
       bool ok = true;
       // BF16 descriptors, computed once: the first layer's weights and input
