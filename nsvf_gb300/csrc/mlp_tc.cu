@@ -9,19 +9,20 @@
 // activations never leave the SM.
 //
 // BF16 CTA = 18 warps. Two tile slots (TMEM columns [256 g, 256 g + 256):
-// accumulator D at +0, head output at +128, the activations at +192). Warps 0-7 are the epilogue: all eight work on one
+// accumulator D at +0, head output at +128, a constant ones block at +144,
+// the activations at +192). Warps 0-7 are the epilogue: all eight work on one
 // slot's layer at a time and alternate the slots, so one slot's MMAs run
 // while the other slot is converted. Warp 8 allocates TMEM; lane 0 of warp
 // 8 issues slot 0's tcgen05.mma instructions and lane 0 of warp 17 slot 1's,
 // so the two slots' chains never wait on each other's issue. Warps 9-16 are two loader
 // warpgroups that build the input tiles (embedding gathers and trilinear
 // interpolation) into a ring of shared-memory buffers. Per layer:
-//   MMA thread: the layer's K / 16 MMAs, accumulating onto D (which holds
-//   the layer's bias) with A = the previous activations in TMEM ->
-//   tcgen05.commit arrives on mma_done[g] -> each epilogue warp reads 64
-//   columns of D (tcgen05.ld), applies ReLU, rounds to bf16 pairs, stores
-//   them back as the next layer's A (tcgen05.st) and refills its D columns
-//   with the next layer's bias -> one arrival per warp on act_ready[g].
+//   MMA thread: a bias step (the ones block x a (hi, mid, lo) bf16 split of
+//   the bias, K = 16) that starts D at the bias, then the layer's K / 16
+//   MMAs with A = the previous activations in TMEM -> tcgen05.commit arrives
+//   on mma_done[g] -> each epilogue warp reads 64 columns of D
+//   (tcgen05.ld), applies ReLU, rounds to bf16 pairs and stores them back as
+//   the next layer's A (tcgen05.st) -> one arrival per warp on act_ready[g].
 // The first layer reads its A (the input tile) from shared memory, and the
 // FP8 variant keeps the older form (activations through shared memory, bias
 // in the epilogue); see Cfg.
@@ -43,8 +44,8 @@ constexpr uint32_t kTmemCols = 512;
 
 // Warp roles and tile slots of the two variants.
 //   BF16: 18 warps; two tile slots of 256 TMEM columns (head output at
-//         +128, activations at +192); epilogue warps 0-7, MMA warps 8 (slot
-//         0) and 17 (slot 1), loader warps 9-16.
+//         +128, ones block at +144, activations at +192); epilogue warps
+//         0-7, MMA warps 8 (slot 0) and 17 (slot 1), loader warps 9-16.
 //   FP8:  the hidden weights and activations take half the shared memory,
 //         which makes room for a third tile slot: 24 warps; three slots of
 //         128 TMEM columns (the head output reuses the slot's first 16);
@@ -72,6 +73,9 @@ struct Cfg {
   // BF16: TMEM column of slot g's activations, the A operand of its next
   // layer (HID bf16 per row, two per column: 64 columns).
   __device__ static constexpr uint32_t act_col(int g) { return 256u * (uint32_t)g + 192u; }
+  // BF16: 8 columns holding (1, 1, 1, 0, ...) in every lane: the A operand
+  // of the hidden layers' bias step.
+  __device__ static constexpr uint32_t ones_col(int g) { return 256u * (uint32_t)g + 144u; }
   static constexpr int kHidBytes = F8 ? HID * HID : HID * HID * 2;  // one hidden weight matrix
 };
 
@@ -96,6 +100,11 @@ struct __align__(128) MlpSmem {
   // FP8: the hidden activations (E4M3 uses the first half of each). BF16
   // keeps its activations in tensor memory.
   __nv_bfloat16 ah[F8 ? Cfg<F8>::kSlots : 1][F8 ? TILE * HID : 8];
+  // BF16: the bias step of each layer (an extra K = 16 MMA): B rows n =
+  // (hi, mid, lo, 0, ...) with hi + mid + lo = bias[l][n] (three bf16 terms),
+  // and, for the first layer, an A tile whose rows are (1, 1, 1, 0, ...).
+  __nv_bfloat16 bias_b[F8 ? 1 : 4][F8 ? 8 : HID * 16];
+  __nv_bfloat16 ones_a[F8 ? 8 : TILE * 16];
   // per loader warp: its 32 rows' corner keys (kSkipKey = skip) and
   // trilinear weights, written by the row's lane and read by the 8 lanes
   // that gather the row
@@ -233,18 +242,34 @@ __device__ __forceinline__ void issue_ts(uint32_t d_tmem, uint32_t a_tmem, uint6
     mma_bf16_ts(d_tmem, a_tmem + 8u * k, bd + 16u * k, idesc, (ACC0 || k > 0) ? 1u : 0u);
 }
 
-// Write a layer's 64 bias values (the same in every lane) into this warp's 32
-// TMEM lanes at columns [ta, ta + 64): the layer's MMAs then accumulate onto
-// the bias, and the epilogue has no bias to add.
-__device__ __forceinline__ void bias_prestore(uint32_t ta, const float *__restrict__ bias) {
-#pragma unroll 4
-  for (int q = 0; q < 8; ++q) {
-    const float4 a = reinterpret_cast<const float4 *>(bias)[2 * q];
-    const float4 b = reinterpret_cast<const float4 *>(bias)[2 * q + 1];
-    const uint32_t r[8] = {__float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(a.z),
-                           __float_as_uint(a.w), __float_as_uint(b.x), __float_as_uint(b.y),
-                           __float_as_uint(b.z), __float_as_uint(b.w)};
-    tmem_st8(ta + 8u * q, r);
+// bf16 1.0 in the low half, and in both halves
+constexpr uint32_t kOne = 0x00003F80u, kOnes2 = 0x3F803F80u;
+
+// The bias step's operands (BF16), written once per CTA: row n of layer l's
+// B block is (hi, mid, lo, 0, ...) with hi = bf16(b), mid = bf16(b - hi),
+// lo = bf16(b - hi - mid) -- their sum is b to within the FP32 rounding of the
+// accumulation -- and every row of the first layer's A block is
+// (1, 1, 1, 0, ...). Both are no-swizzle K-major tiles with K = 16.
+__device__ __forceinline__ void stage_bias_step(__nv_bfloat16 (*bias_b)[HID * 16],
+                                                __nv_bfloat16 *ones_a,
+                                                const float *const *b, int tid, int nthreads) {
+  for (int i = tid; i < 4 * HID; i += nthreads) {
+    const int l = i / HID, n = i % HID;
+    const float v = b[l][n];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+    uint8_t *base = reinterpret_cast<uint8_t *>(bias_b[l]);
+    const uint32_t w01 = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(mid) << 16);
+    const uint32_t w23 = (uint32_t)__bfloat16_as_ushort(lo);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(n, 0, 16)) = make_uint4(w01, w23, 0u, 0u);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(n, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (int m = tid; m < TILE; m += nthreads) {
+    uint8_t *base = reinterpret_cast<uint8_t *>(ones_a);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(m, 0, 16)) = make_uint4(kOnes2, kOne, 0u, 0u);
+    *reinterpret_cast<uint4 *>(base + kmajor_off(m, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
   }
 }
 
@@ -495,6 +520,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     else stage_weights(reinterpret_cast<__nv_bfloat16 *>(S.wh[l]), p.w[l + 1], HID, HID, HID);
   }
   stage_weights(S.w4, p.w[4], NOUT, 4, HID);
+  if constexpr (!F8) stage_bias_step(S.bias_b, S.ones_a, p.b, tid, blockDim.x);
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
   if (F8)
     for (int i = tid; i < 3 * HID; i += blockDim.x)
@@ -522,13 +548,13 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   fence_after_sync();
   const uint32_t tmem = S.tmem_base;
   if constexpr (!F8) {
-    // BF16: each slot's accumulator starts from the first layer's bias
-    // (later tiles get it from the epilogue of the slot's previous tile)
-    if (warp < C::kEpiWarps) {
-      const int q4 = warp & 3, h = warp >> 2;
+    // BF16: each slot's ones block in tensor memory (the A operand of the
+    // hidden layers' bias step), written once by warps 0-3 (lane quarter =
+    // warp) and never changed
+    if (warp < 4) {
+      const uint32_t ones[8] = {kOnes2, kOne, 0u, 0u, 0u, 0u, 0u, 0u};
       for (int g = 0; g < C::kSlots; ++g)
-        bias_prestore(tmem + ((uint32_t)(q4 * 32) << 16) + C::kSlotCols * g + 64 * h,
-                      S.bias[0] + 64 * h);
+        tmem_st8(tmem + ((uint32_t)(warp * 32) << 16) + C::ones_col(g), ones);
       tmem_wait_st();
     }
     fence_before_sync();
@@ -569,6 +595,10 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       const uint64_t d_in0 = sdesc(smem_u32(S.ain[0]), 128u, (E / 8) * 128u);
       const uint64_t d_w0 = sdesc(smem_u32(S.w0), 128u, (E / 8) * 128u);
       const uint64_t d_wh = sdesc(smem_u32(S.wh[0]), 128u, (HID / 8) * 128u);
+      // the bias step: the first layer's ones block (A, shared memory) and
+      // layer l's bias block (B; + 256 per layer)
+      const uint64_t d_ones = sdesc(smem_u32(S.ones_a), 128u, 256u);
+      const uint64_t d_bias = sdesc(smem_u32(S.bias_b[0]), 128u, 256u);
       const uint64_t d_w4 = sdesc(smem_u32(S.w4), 128u, (HID / 8) * 128u);
       static_assert(sizeof(S.ain[0]) == 8192 && C::kHidBytes == 32768 || F8, "descriptor steps");
 #pragma unroll 1
@@ -586,7 +616,11 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
               if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
               fence_after_sync();
               if (F8) issue_layer(d, S.ain[q], S.w0, E, HID);
-              else issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
+              else {
+                // bias step (overwrites D), then the layer accumulating onto it
+                mma_bf16(d, d_ones, d_bias, idesc_bf16_f32(TILE, HID), 0u);
+                issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
+              }
               mma_commit(&S.mma_done[g][0]);
               mma_commit(&S.in_empty[q]);
             } else {
@@ -597,9 +631,12 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
                 if (F8)
                   issue_layer8(d, reinterpret_cast<const uint8_t *>(S.ah[g]), S.wh[layer - 1],
                                HID, HID);
-                else
+                else {
+                  mma_bf16_ts(d, tmem + C::ones_col(g), d_bias + 256u * (uint32_t)layer,
+                              idesc_bf16_f32(TILE, HID), 0u);
                   issue_ts<HID / 16, true>(d, tmem + C::act_col(g), d_wh + 2048u * (uint32_t)(layer - 1),
                                            idesc_bf16_f32(TILE, HID));
+                }
               } else if (F8) {
                 issue_layer(tmem + C::head_col(g), S.ah[g], S.w4, HID, NOUT);
               } else {
@@ -697,9 +734,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         const int ng = tile_of(i + 1) < n_tiles ? 2 : 1;
         const uint32_t par = (uint32_t)((i / 2) & 1);
         for (int layer = 0; layer < 4 && ok; ++layer) {
-          // the bias the accumulator starts from for the slot's next MMA
-          // layer: layer + 1, or layer 0 of the slot's next tile
-          const float *next_bias = S.bias[(layer + 1) & 3] + 64 * h;
           for (int g = 0; g < ng; ++g) {
             if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) {
               ok = false;
@@ -718,9 +752,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
             epi_chunk(va, ta, 64 * h);
             tmem_wait_ld_bind(vb);
             epi_chunk(vb, ta, 64 * h + 32);
-            // this warp has read its accumulator columns: refill them with
-            // the next layer's bias
-            bias_prestore(tl, next_bias);
             tmem_wait_st();
             fence_before_sync();
             __syncwarp();
