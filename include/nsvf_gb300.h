@@ -330,12 +330,17 @@ int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max
                             const int64_t *offset, int64_t sample_cap, int32_t *voxel,
                             float *xyz_dist, float *depth, int32_t *err, void *stream);
 
-/* composite_segments_dev: nsvf_composite_segments over *n_rays_dev rays. */
+/* composite_segments_dev: nsvf_composite_segments over *n_rays_dev rays,
+ * each ray's segment [offset[r], offset[r + 1]) clamped to the sample
+ * buffers' capacity sample_cap (a frame whose samples overflowed them -- the
+ * sample kernels' error bit 1 -- is to be composited again with room for all
+ * of them; nothing is read past the buffers). */
 int nsvf_composite_segments_dev(int64_t rays_cap, const int64_t *n_rays_dev,
-                                const int64_t *offset, const float *field, const float *xyz_dist,
-                                const float *depth, const int64_t *pixel, float sigma_scale,
-                                const float bg[3], float bg_depth, float *out_color,
-                                float *out_depth, float *out_missed, int kahan, void *stream);
+                                const int64_t *offset, int64_t sample_cap, const float *field,
+                                const float *xyz_dist, const float *depth, const int64_t *pixel,
+                                float sigma_scale, const float bg[3], float bg_depth,
+                                float *out_color, float *out_depth, float *out_missed, int kahan,
+                                void *stream);
 
 /* field_samples_bf16_dev: nsvf_field_samples_bf16 on *n_samples_dev samples
  * (at most `capacity`; a larger count sets err bit 1), one persistent CTA

@@ -57,7 +57,8 @@ def _load():
         "nsvf_sample_count_dev": ([i64, P, i32, P, P, P, P, P, P, P], i32),
         "nsvf_sample_compact_dev": ([i64, P, i32, P, P, P, P, P, P, i64, P, P, P, i64, P, P, P,
                                      P, P], i32),
-        "nsvf_composite_segments_dev": ([i64, P, P, P, P, P, P, f32, P, f32, P, P, P, i32, P], i32),
+        "nsvf_composite_segments_dev": ([i64, P, P, i64, P, P, P, P, f32, P, f32, P, P, P, i32, P],
+                                        i32),
         "nsvf_field_samples_bf16_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P], i32),
         "nsvf_field_samples_fp8": ([i64, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P], i32),
         "nsvf_field_samples_fp8_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P],

@@ -13,6 +13,8 @@
 // Backward, with g_i = dL/dp_i + dL/ddepth * t_i + <dL/dcolor, tex_i> - dL/dmissed:
 //   dL/dfe_j  = g_j * exp(-fe_j) * T_j - sum_{i>j} g_i p_i
 //   dL/dtex_i = dL/dcolor * p_i
+#include <cstdint>
+
 #include "common.cuh"
 
 namespace {
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(kWarps * 32) composite_segments_kernel(
     const float4 *__restrict__ xyzd, const float *__restrict__ depth,
     const int64_t *__restrict__ pix, float sigma_scale, float bg_r, float bg_g, float bg_b,
     float bg_depth, float *__restrict__ out_color, float *__restrict__ out_depth,
-    float *__restrict__ out_missed, int kahan, const int64_t *__restrict__ n_dev) {
+    float *__restrict__ out_missed, int kahan, const int64_t *__restrict__ n_dev,
+    int64_t sample_cap) {
   int lane = threadIdx.x & 31;
   int64_t r = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
   if (n_dev) {
@@ -180,7 +183,10 @@ __global__ void __launch_bounds__(kWarps * 32) composite_segments_kernel(
     if (nd < rays) rays = nd < 0 ? 0 : nd;
   }
   if (r >= rays) return;
-  int64_t a = offset[r], n = offset[r + 1] - a;
+  // the ray's segment, clamped to the sample buffers (a frame whose samples
+  // overflowed them is composited again; nothing is read past them)
+  const int64_t e = offset[r + 1] < sample_cap ? offset[r + 1] : sample_cap;
+  const int64_t a = offset[r] < e ? offset[r] : e, n = e - a;
   Prefix carry{0.f, 0.f};
   float sp = 0.f, sd = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
   for (int64_t base = 0; base < n; base += 32) {
@@ -227,23 +233,25 @@ int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *fi
     return NSVF_ERR_INVALID;
   composite_segments_kernel<<<nsvf_grid(rays, kWarps), kWarps * 32, 0, (cudaStream_t)stream>>>(
       rays, offset, (const float4 *)field, (const float4 *)xyz_dist, depth, pixel, sigma_scale,
-      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan, nullptr);
+      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan, nullptr, INT64_MAX);
   return nsvf_launch_status();
 }
 
 int nsvf_composite_segments_dev(int64_t rays_cap, const int64_t *n_rays_dev,
-                                const int64_t *offset, const float *field, const float *xyz_dist,
-                                const float *depth, const int64_t *pixel, float sigma_scale,
-                                const float bg[3], float bg_depth, float *out_color,
-                                float *out_depth, float *out_missed, int kahan, void *stream) {
-  if (rays_cap < 0 || !bg || !n_rays_dev) return NSVF_ERR_INVALID;
+                                const int64_t *offset, int64_t sample_cap, const float *field,
+                                const float *xyz_dist, const float *depth, const int64_t *pixel,
+                                float sigma_scale, const float bg[3], float bg_depth,
+                                float *out_color, float *out_depth, float *out_missed, int kahan,
+                                void *stream) {
+  if (rays_cap < 0 || sample_cap < 0 || !bg || !n_rays_dev) return NSVF_ERR_INVALID;
   if (rays_cap == 0) return NSVF_OK;
   if (!offset || !field || !xyz_dist || !depth || !pixel || !out_color || !out_depth ||
       !out_missed || ((((uintptr_t)field) | ((uintptr_t)xyz_dist)) & 15))
     return NSVF_ERR_INVALID;
   composite_segments_kernel<<<nsvf_grid(rays_cap, kWarps), kWarps * 32, 0, (cudaStream_t)stream>>>(
       rays_cap, offset, (const float4 *)field, (const float4 *)xyz_dist, depth, pixel, sigma_scale,
-      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan, n_rays_dev);
+      bg[0], bg[1], bg[2], bg_depth, out_color, out_depth, out_missed, kahan, n_rays_dev,
+      sample_cap);
   return nsvf_launch_status();
 }
 

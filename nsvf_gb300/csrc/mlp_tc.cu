@@ -305,10 +305,41 @@ __device__ __forceinline__ SampleRow load_sample(const MlpParams &p, int64_t r, 
   return s;
 }
 
+// A row's voxel (-1: none): the sample's, or the pruning point's.
+template <int MODE>
+__device__ __forceinline__ int64_t row_voxel(const MlpParams &p, int64_t r, int64_t ns,
+                                             const SampleRow &smp) {
+  if (r >= ns) return -1;
+  if (MODE == kSamplesIn) return smp.vox;
+  return r / ((int64_t)p.bits * p.bits * p.bits);
+}
+
+// The voxel data a row needs, its centre and 8 corner ids. The loaders fetch
+// it one tile ahead, as soon as the row's voxel id has arrived.
+struct VoxRow {
+  float cx, cy, cz;
+  int4 f0, f1;
+};
+
+__device__ __forceinline__ VoxRow load_vox(const MlpParams &p, int64_t v) {
+  VoxRow d;
+  d.cx = d.cy = d.cz = 0.0f;
+  d.f0 = d.f1 = make_int4(kSkipKey, kSkipKey, kSkipKey, kSkipKey);
+  if (v >= 0 && v < p.n_vox) {
+    d.cx = p.centers[v * 3];
+    d.cy = p.centers[v * 3 + 1];
+    d.cz = p.centers[v * 3 + 2];
+    d.f0 = reinterpret_cast<const int4 *>(p.feats)[v * 2];
+    d.f1 = reinterpret_cast<const int4 *>(p.feats)[v * 2 + 1];
+  }
+  return d;
+}
+
 template <int MODE>
 __device__ __forceinline__ void row_meta(const MlpParams &p, int64_t r, int64_t ns,
-                                         const SampleRow &smp, int *__restrict__ key,
-                                         float *__restrict__ w, int *__restrict__ vid, bool &bad) {
+                                         const SampleRow &smp, const VoxRow &vd,
+                                         int *__restrict__ key, float *__restrict__ w,
+                                         int *__restrict__ vid, bool &bad) {
   int k8[8];
   int vv = -1;
   float w8[8];
@@ -327,22 +358,18 @@ __device__ __forceinline__ void row_meta(const MlpParams &p, int64_t r, int64_t 
       v = r / P;
       int64_t i = r % P;
       int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits), iz = (int)(i % p.bits);
-      const float *c = p.centers + v * 3;
       float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
-      x = c[0] + ((float)(2 * ix + 1 - p.bits) / den) * hv;
-      y = c[1] + ((float)(2 * iy + 1 - p.bits) / den) * hv;
-      z = c[2] + ((float)(2 * iz + 1 - p.bits) / den) * hv;
+      x = vd.cx + ((float)(2 * ix + 1 - p.bits) / den) * hv;
+      y = vd.cy + ((float)(2 * iy + 1 - p.bits) / den) * hv;
+      z = vd.cz + ((float)(2 * iz + 1 - p.bits) / den) * hv;
     }
     if (v < 0 || v >= p.n_vox) {
       bad = true;
     } else {
       vv = (int)v;
-      const float *c = p.centers + v * 3;
-      float q[3] = {(x - c[0]) / p.voxel_size + 0.5f, (y - c[1]) / p.voxel_size + 0.5f,
-                    (z - c[2]) / p.voxel_size + 0.5f};
-      const int4 f0 = reinterpret_cast<const int4 *>(p.feats)[v * 2];
-      const int4 f1 = reinterpret_cast<const int4 *>(p.feats)[v * 2 + 1];
-      const int keys[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+      float q[3] = {(x - vd.cx) / p.voxel_size + 0.5f, (y - vd.cy) / p.voxel_size + 0.5f,
+                    (z - vd.cz) / p.voxel_size + 0.5f};
+      const int keys[8] = {vd.f0.x, vd.f0.y, vd.f0.z, vd.f0.w, vd.f1.x, vd.f1.y, vd.f1.z, vd.f1.w};
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         if (keys[k] < 0 || keys[k] >= p.n_keys) {
@@ -662,6 +689,8 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     int *mvox = S.meta_vox[warp - C::kLoaderWarp0];
     // this lane's sample row of the group's next tile, loaded a tile ahead
     SampleRow next = load_sample<MODE>(p, tile_of(L) * TILE + wq * 32 + lane, ns);
+    // and its voxel's centre and corner ids, fetched once the voxel id is in
+    VoxRow next_v = load_vox(p, row_voxel<MODE>(p, tile_of(L) * TILE + wq * 32 + lane, ns, next));
     for (int64_t i = L;; i += 2) {
       int64_t tile = tile_of(i);
       if (tile >= n_tiles) break;
@@ -674,8 +703,10 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       bool bad = false;
       if (MODE != kEmbIn) {
         const SampleRow cur = next;
+        const VoxRow cur_v = next_v;
         next = load_sample<MODE>(p, tile_of(i + 2) * TILE + wq * 32 + lane, ns);
-        row_meta<MODE>(p, r0 + lane, ns, cur, mkey + lane * 8, mw + lane * 8, mvox + lane, bad);
+        row_meta<MODE>(p, r0 + lane, ns, cur, cur_v, mkey + lane * 8, mw + lane * 8, mvox + lane,
+                       bad);
         __syncwarp();
       }
       uint8_t *ain = reinterpret_cast<uint8_t *>(S.ain[q]);
@@ -711,6 +742,10 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       fence_async_smem();
       __syncwarp();                     // also orders pass 2's reads of the row table before the next pass 1
       if (lane == 0) mbar_arrive(&S.in_full[q]);
+      // the group's next tile: its voxel ids (loaded before pass 1) are in by
+      // now, so fetch their centres and corner ids ahead of its pass 1
+      if (MODE != kEmbIn)
+        next_v = load_vox(p, row_voxel<MODE>(p, tile_of(i + 2) * TILE + wq * 32 + lane, ns, next));
     }
   } else {
     if constexpr (F8 && kEpiRegs8 < kLaunchRegs8)

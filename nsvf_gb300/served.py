@@ -83,6 +83,11 @@ class SceneState:
         return sum(t.numel() * t.element_size() for t in ts)
 
 
+# Sample capacity of a frame's first render, per ray; a frame that needs more
+# is composited again with room for all its samples, and the capacity stays.
+INITIAL_SAMPLES_PER_RAY = 32
+
+
 def _frame_buffers(scene, R, stream):
     """Device buffers of the chain for frames of R rays on `stream`, kept on
     the scene and reused while the frame size stays the same. Keyed by stream:
@@ -140,14 +145,14 @@ def _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, err, stream):
 
 def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, stream):
     """Steps 4-6 with the hit-ray and sample counts on the device only: the
-    sample buffers have the frame buffers' capacity (32 samples per ray at
+    sample buffers have the frame buffers' capacity (INITIAL_SAMPLES_PER_RAY at
     first), and the host reads the counts and the error bits once, at the
     end. A frame with more samples than the capacity (error bit 1) is
     composited again with room for all of them."""
     dev = scene.device
     err = b["err"]
     counts, err_h = b["counts_host"], b["err_host"]
-    cap = max(b["cap"], 32 * R)
+    cap = max(b["cap"], INITIAL_SAMPLES_PER_RAY * R)
     for _ in range(2):
         vox, xyzd, depth, field = _sample_buffers(b, cap)
         cap = b["cap"]
@@ -169,7 +174,7 @@ def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, stream):
                       "field_samples_fp8_dev")
         with ext._timed("composite_segments", dev):
             check(LIB.nsvf_composite_segments_dev(
-                R, _p(b["n_hit"]), _p(b["offset"]), _p(field), _p(xyzd), _p(depth), _p(b["pix"]),
+                R, _p(b["n_hit"]), _p(b["offset"]), cap, _p(field), _p(xyzd), _p(depth), _p(b["pix"]),
                 7.0, scene.bg, scene.bg_depth, _p(out["colors"]), _p(out["depths"]),
                 _p(out["missed"]), int(bool(kahan)), stream), "composite_segments_dev")
         counts[0:1].copy_(b["n_hit"], non_blocking=True)

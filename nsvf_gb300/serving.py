@@ -135,7 +135,8 @@ class ChunkPipeline:
         self.colors.copy_(self.bg.expand(C, 3))
         self.depths.fill_(sc.bg_depth)
         self.missed.fill_(1.0)
-        check(LIB.nsvf_composite_segments_dev(C, _p(self.n_hit), _p(self.offset), _p(self.field),
+        check(LIB.nsvf_composite_segments_dev(C, _p(self.n_hit), _p(self.offset), self.cap,
+                                              _p(self.field),
                                               _p(self.xyzd), _p(self.sdepth), _p(self.pix), 7.0,
                                               sc.bg, sc.bg_depth, _p(self.colors),
                                               _p(self.depths), _p(self.missed), 1, s),

@@ -185,3 +185,25 @@ def test_served_vs_float64_oracle(cuda, std, ss, sb, max_err, rms_err):
     err = np.abs(col - ref)
     assert err.max() <= max_err, err.max()
     assert np.sqrt((err ** 2).mean()) <= rms_err
+
+
+def test_sample_capacity_overflow_is_rendered_again(cuda, monkeypatch):
+    """A frame with more samples than the sample buffers hold (error bit 1
+    from the compaction and the MLP) is composited again with room for all
+    of them: the result equals a render whose buffers were large enough."""
+    from nsvf_gb300 import ext, scenes, served
+    enc, field, ren, vs = _scene(cuda, 1.0 / 32, 1.0, 30.0, 0.5, 64)
+    rs, rd = scenes.pinhole_rays(scenes.sphere_cameras(3, 4.0, seed=9)[1], 96, 96, 120.0)
+    rs_t, rd_t = torch.from_numpy(rs).to(cuda), torch.from_numpy(rd).to(cuda)
+    ref = served.render_frame(served.SceneState(enc, field), rs_t, rd_t)
+    monkeypatch.setattr(served, "INITIAL_SAMPLES_PER_RAY", 1)
+    scene = served.SceneState(enc, field)
+    out = served.render_frame(scene, rs_t, rd_t)
+    ext.check_errors(cuda)
+    # the first attempt's buffers (1.25 samples per ray) were too small
+    assert out["n_samples"] == ref["n_samples"] > rd.shape[0] * 5 // 4
+    assert next(iter(scene._frames.values()))["cap"] >= out["n_samples"]
+    assert torch.equal(out["colors"], ref["colors"]) and torch.equal(out["depths"], ref["depths"])
+    # the capacity grew to hold the frame: the next frame renders in one go
+    again = served.render_frame(scene, rs_t, rd_t)
+    assert torch.equal(again["colors"], ref["colors"])
