@@ -53,6 +53,8 @@ def parse():
                     help="1: FP8-option frames and max/RMS RGB error vs an FP64 render (c2, and c4 "
                          "with --precision-c4 1)")
     ap.add_argument("--precision-c4", type=int, default=1)
+    ap.add_argument("--serve-chunk", type=int, default=262144,
+                    help="rays per chunk of the serving pipeline")
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests of the multi-scene serving run (c5); 0 skips it")
     return ap.parse_args()
@@ -241,7 +243,7 @@ def prune_bench(dev, sc, bits=8, th=0.5):
             "max_abs_alpha_diff": float((score - alpha).abs().max())}
 
 
-def serve_bench(dev, n_requests, rate=200.0, seed=0):
+def serve_bench(dev, n_requests, rate=200.0, seed=0, chunk_rays=262144, samples_per_ray=128):
     """The c5 serving workload: eight resident seeded scenes (sphere/torus/box
     unions, 10k-400k voxels), each with its own 4x128 MLP; Poisson arrivals at
     `rate`/s, each request one scene at a random camera on the radius-4 sphere
@@ -271,7 +273,12 @@ def serve_bench(dev, n_requests, rate=200.0, seed=0):
         store.add(sid, enc, field)
         plain[sid] = (enc, field, VolumeRenderer(args).eval(), enc.precompute(id=None))
         voxels.append(int(p.shape[0]))
-    server = Server(store, chunk_rays=65536, slots=3, max_inflight=8, frame_budget_bytes=1 << 30)
+    # 256k-ray chunks: fewer, longer launches per frame (64k: 99 M rays/s at
+    # capacity, p99 20 ms; 128k: 117 M, 14 ms; 256k: 125 M, 11 ms). A chunk
+    # holds up to 128 samples per ray on average (c2 averages 29); one that
+    # needs more is rendered again without the cap.
+    server = Server(store, chunk_rays=chunk_rays, slots=3, max_inflight=8, frame_budget_bytes=1 << 30,
+                    samples_per_ray=samples_per_ray)
     server.warm(list(store.scenes))
     server.reserve_host_buffers(800 * 800, 8)
     reqs = poisson_requests(n_requests, rate, list(store.scenes), [128, 256, 512, 800], seed=seed)
@@ -319,7 +326,7 @@ def serve_bench(dev, n_requests, rate=200.0, seed=0):
         "served_bf16": {"rays_per_s": round(rays / wall, 1), "p50_ms": round(float(np.percentile(lat, 50)), 2),
                         "p99_ms": round(float(np.percentile(lat, 99)), 2),
                         "offered_rays_per_s": round(rays / reqs[-1].arrival, 1),
-                        "wall_s": round(wall, 3), "chunk_rays": 65536, "slots": 3,
+                        "wall_s": round(wall, 3), "chunk_rays": chunk_rays, "samples_per_ray_cap": samples_per_ray, "slots": 3,
                         "cuda_graphs": True},
         "served_bf16_capacity": {"rays_per_s": round(rays_b / wall_b, 1),
                                  "p50_ms": round(float(np.percentile(lat_b, 50)), 2),
@@ -565,7 +572,8 @@ def run_ours(a):
                 "algorithmic_bytes_per_launch": alg, "avg_launch_ms": round(k["avg_ms"], 4),
                 "traffic": None}
     cpu = cpu_baseline(a.cpu_rays, threads=1)
-    serving = serve_bench(dev, a.serve_requests) if a.serve_requests > 0 and world == 1 else None
+    serving = serve_bench(dev, a.serve_requests, chunk_rays=a.serve_chunk) \
+        if a.serve_requests > 0 and world == 1 else None
     pruning = prune_bench(dev, sc) if world == 1 else None
     precision = precision_bench(dev, sc, a.size, c4=bool(a.precision_c4)) \
         if (world == 1 and a.precision and a.path == "served") else None
