@@ -399,9 +399,24 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int32_t *Iq = idx + rq * n_max;
     float *Lq = min_depth + rq * n_max, *Hq = max_depth + rq * n_max;
     if (SORTED && cq > 0) {
-      if (n_max <= 32) warp_sort_row<1>(Iq, Lq, Hq, n_max, cq, lane);
-      else if (n_max <= 64) warp_sort_row<2>(Iq, Lq, Hq, n_max, cq, lane);
-      else warp_sort_row<4>(Iq, Lq, Hq, n_max, cq, lane);
+      // A row with at most 32 hits, all at depths <= 10000 (not NaN), sorts
+      // as its first 32 slots: the whole row's order puts the same misses
+      // (depth 10000, in slot order) after them.
+      const bool short_row =
+          n_max > 32 && cq <= 32 &&
+          __all_sync(0xffffffffu, lane >= cq || Lq[lane] <= NSVF_MAX_DEPTH_F);
+      if (n_max <= 32) {
+        warp_sort_row<1>(Iq, Lq, Hq, n_max, cq, lane);
+      } else if (short_row) {
+        warp_sort_row<1>(Iq, Lq, Hq, 32, cq, lane);
+        for (int l = 32 + lane; l < n_max; l += 32) {
+          Iq[l] = -1; Lq[l] = NSVF_MAX_DEPTH_F; Hq[l] = NSVF_MAX_DEPTH_F;
+        }
+      } else if (n_max <= 64) {
+        warp_sort_row<2>(Iq, Lq, Hq, n_max, cq, lane);
+      } else {
+        warp_sort_row<4>(Iq, Lq, Hq, n_max, cq, lane);
+      }
     } else {
       float pad = SORTED ? NSVF_MAX_DEPTH_F : 0.0f;
       for (int l = cq + lane; l < n_max; l += 32) { Iq[l] = -1; Lq[l] = pad; Hq[l] = pad; }

@@ -85,6 +85,11 @@ def test_svo_matches_oracle_random_rays(cuda, voxel, n_max):
     rs = cpu.sort_hits(*ref)
     for a, b in zip(srt[:3], rs):
         assert np.array_equal(_np(a), b)
+    if n_max == 64:
+        # both sort paths: rows of at most 32 hits sort as 32 slots, longer
+        # rows through the whole 64-slot network
+        cnt = (ref[0][0] != -1).sum(-1)
+        assert (cnt > 32).sum() > 100 and ((cnt > 0) & (cnt <= 32)).sum() > 1000
     ext.check_errors(cuda)
 
 
