@@ -23,9 +23,12 @@
 //   on mma_done[g] -> each epilogue warp reads 64 columns of D
 //   (tcgen05.ld), applies ReLU, rounds to bf16 pairs and stores them back as
 //   the next layer's A (tcgen05.st) -> one arrival per warp on act_ready[g].
-// The first layer reads its A (the input tile) from shared memory, and the
-// FP8 variant keeps the older form (activations through shared memory, bias
-// in the epilogue); see Cfg.
+// The first layer reads its A (the input tile) from shared memory. The FP8
+// variant has the same structure; its three hidden layers are E4M3
+// (kind::f8f6f4, K = 32 per MMA) with A = E4M3 activations in tensor memory
+// (four per column), its bias step holds bias / dq (the layer's
+// dequantisation), and its epilogue scales the accumulator by dq * qs
+// before rounding to E4M3 (or by dq before bf16, for the head's input).
 // Every wait is bounded; on a timeout the CTA records bit 3 in *err, stops,
 // and still frees its TMEM.
 #include "common.cuh"
@@ -42,54 +45,35 @@ constexpr int TILE = 128;   // samples per MMA tile (M)
 constexpr int NB = 4;       // input tile ring depth
 constexpr uint32_t kTmemCols = 512;
 
-// Warp roles and tile slots of the two variants.
-//   BF16: 18 warps; two tile slots of 256 TMEM columns (head output at
-//         +128, ones block at +144, activations at +192); epilogue warps
-//         0-7, MMA warps 8 (slot 0) and 17 (slot 1), loader warps 9-16.
-//   FP8:  the hidden weights and activations take half the shared memory,
-//         which makes room for a third tile slot: 24 warps; three slots of
-//         128 TMEM columns (the head output reuses the slot's first 16);
-//         epilogue warps 0-11, loader warps 12-19, MMA warps 20-22 (one per
-//         slot; 23 only completes the warpgroup). The warpgroups rebalance
-//         registers with setmaxnreg (below).
+// Warp roles and tile slots (both variants): 18 warps; two tile slots of
+// 256 TMEM columns (accumulator at +0, head output at +128, ones block at
+// +144, E4M3 activations at +160 (FP8), BF16 activations at +192); epilogue
+// warps 0-7, MMA warps 8 (slot 0) and 17 (slot 1), loader warps 9-16.
 template <bool F8>
 struct Cfg {
-  static constexpr int kSlots = F8 ? 3 : 2;
-  static constexpr int kEpiWarps = 4 * kSlots;
-  static constexpr int kLoaderWarp0 = F8 ? kEpiWarps : kEpiWarps + 1;
-  static constexpr int kMmaWarp = F8 ? kLoaderWarp0 + 8 : kEpiWarps;
-  static constexpr int kThreads = F8 ? 24 * 32 : 18 * 32;
-  // BF16: a second MMA warp; each MMA warp's lane 0 issues one slot's MMAs
-  static constexpr int kMmaWarp2 = F8 ? -1 : kLoaderWarp0 + 8;
-  static constexpr uint32_t kSlotCols = F8 ? 128u : 256u;
+  static constexpr int kSlots = 2;
+  static constexpr int kEpiWarps = 8;
+  static constexpr int kLoaderWarp0 = kEpiWarps + 1;
+  static constexpr int kMmaWarp = kEpiWarps;
+  static constexpr int kThreads = 18 * 32;
+  // a second MMA warp; each MMA warp's lane 0 issues one slot's MMAs
+  static constexpr int kMmaWarp2 = kLoaderWarp0 + 8;
+  static constexpr uint32_t kSlotCols = 256u;
   // TMEM column of slot g's (sigma, rgb) head output. The MMA lane issues
   // the slot's next tile's first layer without waiting for the epilogue to
-  // read the head, so the head must not share columns with it: BF16 uses the
-  // slot's spare columns [256 g + 128, + 16); FP8 has none and uses columns
-  // 384 + 16 g (after the three 128-column slots).
-  __device__ static constexpr uint32_t head_col(int g) {
-    return F8 ? 384u + 16u * (uint32_t)g : 256u * (uint32_t)g + 128u;
-  }
-  // BF16: TMEM column of slot g's activations, the A operand of its next
-  // layer (HID bf16 per row, two per column: 64 columns).
+  // read the head, so the head must not share columns with it.
+  __device__ static constexpr uint32_t head_col(int g) { return 256u * (uint32_t)g + 128u; }
+  // BF16 activations of slot g (HID bf16 per row, two per column: 64
+  // columns): the A operand of the BF16 hidden layers and of the head.
   __device__ static constexpr uint32_t act_col(int g) { return 256u * (uint32_t)g + 192u; }
-  // BF16: 8 columns holding (1, 1, 1, 0, ...) in every lane: the A operand
-  // of the hidden layers' bias step.
+  // FP8: E4M3 activations of slot g (HID per row, four per column: 32
+  // columns), the A operand of the E4M3 hidden layers.
+  __device__ static constexpr uint32_t act8_col(int g) { return 256u * (uint32_t)g + 160u; }
+  // 8 columns holding bf16 (1, 1, 1, 0, ...) in every lane: the A operand of
+  // the hidden layers' bias step.
   __device__ static constexpr uint32_t ones_col(int g) { return 256u * (uint32_t)g + 144u; }
   static constexpr int kHidBytes = F8 ? HID * HID : HID * HID * 2;  // one hidden weight matrix
 };
-
-// FP8 variant: registers per thread after the warpgroups rebalance. The MMA
-// warpgroup gives registers up and the loaders take them (two rows of
-// gathers in flight); the epilogues keep the launch count. The kernel is launched with
-// kLaunchRegs8 per thread; the split must fit in 768 * kLaunchRegs8, or the
-// loaders' setmaxnreg.inc would wait forever -- the host checks the compiled
-// register count before the first launch.
-constexpr int kLaunchRegs8 = 80, kEpiRegs8 = 80, kLoaderRegs8 = 88, kMmaRegs8 = 64;
-static_assert(Cfg<true>::kThreads * kLaunchRegs8 <= 65536, "launch registers");
-static_assert(3 * 128 * kEpiRegs8 + 2 * 128 * kLoaderRegs8 + 128 * kMmaRegs8 <=
-                  Cfg<true>::kThreads * kLaunchRegs8,
-              "register split exceeds the launch allocation");
 
 template <bool F8>
 struct __align__(128) MlpSmem {
@@ -97,14 +81,12 @@ struct __align__(128) MlpSmem {
   uint8_t wh[3][Cfg<F8>::kHidBytes];       // bf16 or E4M3 hidden weights
   __nv_bfloat16 w4[NOUT * HID];
   __nv_bfloat16 ain[NB][TILE * E];
-  // FP8: the hidden activations (E4M3 uses the first half of each). BF16
-  // keeps its activations in tensor memory.
-  __nv_bfloat16 ah[F8 ? Cfg<F8>::kSlots : 1][F8 ? TILE * HID : 8];
-  // BF16: the bias step of each layer (an extra K = 16 MMA): B rows n =
-  // (hi, mid, lo, 0, ...) with hi + mid + lo = bias[l][n] (three bf16 terms),
-  // and, for the first layer, an A tile whose rows are (1, 1, 1, 0, ...).
-  __nv_bfloat16 bias_b[F8 ? 1 : 4][F8 ? 8 : HID * 16];
-  __nv_bfloat16 ones_a[F8 ? 8 : TILE * 16];
+  // the bias step of each layer (an extra bf16 K = 16 MMA): B rows n =
+  // (hi, mid, lo, 0, ...) with hi + mid + lo = bias[l][n] / dq[l] (three
+  // bf16 terms; dq = 1 except after an FP8 layer), and, for the first layer,
+  // an A tile whose rows are (1, 1, 1, 0, ...).
+  __nv_bfloat16 bias_b[4][HID * 16];
+  __nv_bfloat16 ones_a[TILE * 16];
   // per loader warp: its 32 rows' corner keys (kSkipKey = skip) and
   // trilinear weights, written by the row's lane and read by the 8 lanes
   // that gather the row
@@ -113,7 +95,6 @@ struct __align__(128) MlpSmem {
   int meta_vox[8][32];
   float meta_w[8][32 * 8];
   float bias[4][HID];
-  float bias_q[F8 ? 3 : 1][HID];          // FP8: bias[l] * qs[l] for layers 0-2
   float bias4[NOUT];
   uint64_t mma_done[Cfg<F8>::kSlots][5];  // per slot and layer: one phase per tile
   uint64_t act_ready[Cfg<F8>::kSlots];    // epilogue -> MMA: hidden activations written
@@ -195,31 +176,6 @@ __device__ void stage_weights8(uint8_t *dst, const uint8_t *src, int rows, int K
   }
 }
 
-// One E4M3 layer: K / 32 MMAs of K = 32, A and B in the 8-bit K-major layout
-// (LBO 128 B, SBO (K / 16) * 128 B), each MMA 256 bytes further along K.
-__device__ __forceinline__ void issue_layer8(uint32_t d_tmem, const uint8_t *A, const uint8_t *B,
-                                             int K, int N) {
-  uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
-  uint32_t sbo = (uint32_t)(K / 16) * 128u;
-  uint32_t idesc = idesc_e4m3_f32(TILE, N);
-  for (int k = 0; k < K / 32; ++k) {
-    uint64_t ad = sdesc(a0 + 256u * k, 128u, sbo);
-    uint64_t bd = sdesc(b0 + 256u * k, 128u, sbo);
-    mma_e4m3(d_tmem, ad, bd, idesc, k > 0 ? 1u : 0u);
-  }
-}
-
-__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const __nv_bfloat16 *A,
-                                            const __nv_bfloat16 *B, int K, int N) {
-  uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
-  uint32_t sbo = (uint32_t)(K / 8) * 128u;
-  uint32_t idesc = idesc_bf16_f32(TILE, N);
-  for (int k = 0; k < K / 16; ++k) {
-    uint64_t ad = sdesc(a0 + 256u * k, 128u, sbo);
-    uint64_t bd = sdesc(b0 + 256u * k, 128u, sbo);
-    mma_bf16(d_tmem, ad, bd, idesc, k > 0 ? 1u : 0u);
-  }
-}
 
 // The K / 16 MMAs of one BF16 layer from precomputed descriptors. A K = 16
 // step moves a no-swizzle K-major operand by 256 bytes, i.e. 16 in the
@@ -252,10 +208,11 @@ constexpr uint32_t kOne = 0x00003F80u, kOnes2 = 0x3F803F80u;
 // (1, 1, 1, 0, ...). Both are no-swizzle K-major tiles with K = 16.
 __device__ __forceinline__ void stage_bias_step(__nv_bfloat16 (*bias_b)[HID * 16],
                                                 __nv_bfloat16 *ones_a,
-                                                const float *const *b, int tid, int nthreads) {
+                                                const float *const *b, const float *dq, int tid,
+                                                int nthreads) {
   for (int i = tid; i < 4 * HID; i += nthreads) {
     const int l = i / HID, n = i % HID;
-    const float v = b[l][n];
+    const float v = dq ? b[l][n] / dq[l] : b[l][n];
     const __nv_bfloat16 hi = __float2bfloat16_rn(v);
     const float r1 = v - __bfloat162float(hi);
     const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
@@ -432,36 +389,31 @@ __device__ __forceinline__ void store_in4(uint8_t *ain, int row, int cb, float4 
       make_uint2(pack_bf16x2(e.x, e.y), pack_bf16x2(e.z, e.w));
 }
 
-// FP8 variant: dequantise and scale for the next layer in one fmaf
-// (dqs = dq * qs, bias_q = bias * qs; ReLU commutes with the positive
-// scale), ReLU + round to E4M3 (saturating) in one cvt, store into the
-// 8-bit K-major activation tile.
-__device__ __forceinline__ void epi_chunk8(const float (&v)[32], const float *__restrict__ bias_q,
-                                           float dqs, uint8_t *ah, int row, int c) {
+// FP8 epilogue chunk feeding an E4M3 layer: 32 columns [c, c + 32) of one
+// row times dqs (the layer's dequantisation times the next layer's activation
+// scale; the bias is already in the accumulator as bias / dq), ReLU and
+// saturating E4M3 rounding in one cvt, four per 32-bit TMEM column (element
+// k in byte k % 4) at ta8 + c / 4.
+__device__ __forceinline__ void epi_chunk8(const float (&v)[32], float dqs, uint32_t ta8, int c) {
   uint32_t pk[8];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float4 bq = *reinterpret_cast<const float4 *>(bias_q + c + 4 * j);
-    pk[j] = pack_relu_e4m3x2(fmaf(v[4 * j + 0], dqs, bq.x), fmaf(v[4 * j + 1], dqs, bq.y)) |
-            (pack_relu_e4m3x2(fmaf(v[4 * j + 2], dqs, bq.z), fmaf(v[4 * j + 3], dqs, bq.w)) << 16);
-  }
-  *reinterpret_cast<uint4 *>(ah + kmajor_off8(row, c, HID)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-  *reinterpret_cast<uint4 *>(ah + kmajor_off8(row, c + 16, HID)) =
-      make_uint4(pk[4], pk[5], pk[6], pk[7]);
+  for (int j = 0; j < 8; ++j)
+    pk[j] = pack_relu_e4m3x2(v[4 * j] * dqs, v[4 * j + 1] * dqs) |
+            (pack_relu_e4m3x2(v[4 * j + 2] * dqs, v[4 * j + 3] * dqs) << 16);
+  tmem_st8(ta8 + (uint32_t)(c >> 2), pk);
 }
 
-// BF16 output after a dequantising FP8 layer: dq * acc + bias, ReLU, bf16.
-__device__ __forceinline__ void epi_chunk_dq(const float (&v)[32], const float *__restrict__ bias,
-                                             float dq, uint8_t *ah, int row, int c) {
-  uint32_t pk[16];
+// FP8 epilogue chunk after the last E4M3 layer, feeding the BF16 head: times
+// dq, ReLU, bf16 pairs at ta + c / 2.
+__device__ __forceinline__ void epi_chunk_dq(const float (&v)[32], float dq, uint32_t ta, int c) {
 #pragma unroll
-  for (int j = 0; j < 16; ++j)
-    pk[j] = pack_relu_bf16x2(fmaf(v[2 * j], dq, bias[c + 2 * j]),
-                             fmaf(v[2 * j + 1], dq, bias[c + 2 * j + 1]));
+  for (int q = 0; q < 2; ++q) {
+    uint32_t pk[8];
 #pragma unroll
-  for (int h = 0; h < 4; ++h)
-    *reinterpret_cast<uint4 *>(ah + kmajor_off(row, c + 8 * h, HID)) =
-        make_uint4(pk[4 * h], pk[4 * h + 1], pk[4 * h + 2], pk[4 * h + 3]);
+    for (int j = 0; j < 8; ++j)
+      pk[j] = pack_relu_bf16x2(v[16 * q + 2 * j] * dq, v[16 * q + 2 * j + 1] * dq);
+    tmem_st8(ta + (uint32_t)((c >> 1) + 8 * q), pk);
+  }
 }
 
 // Hidden-layer epilogue of 32 columns [c, c + 32) of one row (the bias is
@@ -522,11 +474,12 @@ __device__ __forceinline__ void head_store(const MlpParams &p, const float *bias
 }
 
 // Persistent CTA (one per SM), roles as in Cfg:
-//   epilogue warps  bias + ReLU + rounding of each hidden layer back to
-//                   shared memory, and the output stage. BF16: all 8 warps
-//                   on one slot's layer at a time, alternating the slots;
-//                   FP8: one warpgroup per tile slot g;
-//   MMA warp        TMEM allocation; lane 0 issues all tcgen05.mma;
+//   epilogue warps  ReLU + rounding of each hidden layer back to tensor
+//                   memory as the next layer's A operand, and the output
+//                   stage; all 8 warps on one slot's layer at a time,
+//                   alternating the slots;
+//   MMA warps       warp 8 allocates TMEM; lane 0 of warp 8 issues slot 0's
+//                   tcgen05.mma, lane 0 of warp 17 slot 1's;
 //   loader warps    two warpgroups that build the input tiles (the embedding
 //                   gathers and interpolation) into a ring of NB buffers
 //                   ahead of the MMAs.
@@ -547,19 +500,15 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     else stage_weights(reinterpret_cast<__nv_bfloat16 *>(S.wh[l]), p.w[l + 1], HID, HID, HID);
   }
   stage_weights(S.w4, p.w[4], NOUT, 4, HID);
-  if constexpr (!F8) stage_bias_step(S.bias_b, S.ones_a, p.b, tid, blockDim.x);
+  stage_bias_step(S.bias_b, S.ones_a, p.b, F8 ? p.dq : nullptr, tid, blockDim.x);
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
-  if (F8)
-    for (int i = tid; i < 3 * HID; i += blockDim.x)
-      S.bias_q[i / HID][i % HID] = p.b[i / HID][i % HID] * p.qs[i / HID];
   if (tid < NOUT) S.bias4[tid] = tid < 4 ? p.b[4][tid] : 0.0f;
   if (tid == 0) {
     for (int g = 0; g < C::kSlots; ++g) {
       for (int l = 0; l < 5; ++l) mbar_init(&S.mma_done[g][l], 1);
       // one arrival per epilogue warp (lane 0, after the warp's fences and
-      // a __syncwarp): BF16 has all 8 warps on each slot's layer, FP8 one
-      // warpgroup per slot
-      mbar_init(&S.act_ready[g], F8 ? 4 : 8);
+      // a __syncwarp): all 8 warps work on each slot's layer
+      mbar_init(&S.act_ready[g], C::kEpiWarps);
     }
     for (int q = 0; q < NB; ++q) {
       mbar_init(&S.in_full[q], 4);    // one arrival per loader warp
@@ -574,10 +523,10 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = S.tmem_base;
-  if constexpr (!F8) {
-    // BF16: each slot's ones block in tensor memory (the A operand of the
-    // hidden layers' bias step), written once by warps 0-3 (lane quarter =
-    // warp) and never changed
+  {
+    // each slot's ones block in tensor memory (the A operand of the hidden
+    // layers' bias step), written once by warps 0-3 (lane quarter = warp)
+    // and never changed
     if (warp < 4) {
       const uint32_t ones[8] = {kOnes2, kOne, 0u, 0u, 0u, 0u, 0u, 0u};
       for (int g = 0; g < C::kSlots; ++g)
@@ -601,33 +550,32 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   const int64_t G = gridDim.x, b = blockIdx.x;
   auto tile_of = [&](int64_t i) { return b + i * G; };
 
-  const bool mma_role = F8 ? warp >= C::kMmaWarp : (warp == C::kMmaWarp || warp == C::kMmaWarp2);
+  const bool mma_role = warp == C::kMmaWarp || warp == C::kMmaWarp2;
   const bool loader_role = warp >= C::kLoaderWarp0 && warp < C::kLoaderWarp0 + 8;
   if (mma_role) {
-    if constexpr (F8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kMmaRegs8));
     // One issuing thread per slot, so a slot whose activations are ready
-    // never waits behind another slot's issue. BF16: lane 0 of kMmaWarp
-    // (slot 0) and of kMmaWarp2 (slot 1); FP8: lane 0 of kMmaWarp + g for
-    // slot g (warps 20-22 of the MMA warpgroup).
-    const int issue_slot = F8 ? (warp - C::kMmaWarp < C::kSlots ? warp - C::kMmaWarp : -1)
-                              : (warp == C::kMmaWarp ? 0 : (warp == C::kMmaWarp2 ? 1 : -1));
+    // never waits behind the other slot's issue: lane 0 of kMmaWarp (slot 0)
+    // and of kMmaWarp2 (slot 1).
+    const int issue_slot = warp == C::kMmaWarp ? 0 : 1;
     if (issue_slot >= 0 && lane == 0) {
       const int g_lo = issue_slot, g_hi = issue_slot + 1;
       uint32_t ph_act[C::kSlots] = {};
       bool ok = true;
-      // BF16 descriptors, computed once: the first layer's weights and input
+      // Descriptors, computed once: the first layer's weights and input
       // ring buffer 0 (buffer q is 8 KB further: + 512 in the address
-      // field), the first hidden layer's weights (layer l + 1: + 2048) and
-      // the head's weights.
+      // field), the first hidden layer's weights (layer l + 1: one matrix
+      // further, + kHidBytes / 16; a K step of 16 bf16 or 32 E4M3 elements
+      // is 256 bytes, + 16) and the head's weights.
       const uint64_t d_in0 = sdesc(smem_u32(S.ain[0]), 128u, (E / 8) * 128u);
       const uint64_t d_w0 = sdesc(smem_u32(S.w0), 128u, (E / 8) * 128u);
-      const uint64_t d_wh = sdesc(smem_u32(S.wh[0]), 128u, (HID / 8) * 128u);
+      const uint64_t d_wh = sdesc(smem_u32(S.wh[0]), 128u, (F8 ? HID / 16 : HID / 8) * 128u);
+      constexpr uint32_t kHidStep = C::kHidBytes / 16;
       // the bias step: the first layer's ones block (A, shared memory) and
       // layer l's bias block (B; + 256 per layer)
       const uint64_t d_ones = sdesc(smem_u32(S.ones_a), 128u, 256u);
       const uint64_t d_bias = sdesc(smem_u32(S.bias_b[0]), 128u, 256u);
       const uint64_t d_w4 = sdesc(smem_u32(S.w4), 128u, (HID / 8) * 128u);
-      static_assert(sizeof(S.ain[0]) == 8192 && C::kHidBytes == 32768 || F8, "descriptor steps");
+      static_assert(sizeof(S.ain[0]) == 8192 && C::kHidBytes % 16 == 0, "descriptor steps");
 #pragma unroll 1
       for (int64_t i = 0; ok; i += C::kSlots) {
         if (tile_of(i) >= n_tiles) break;
@@ -642,12 +590,9 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
               int q = (int)(ii % NB);
               if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
               fence_after_sync();
-              if (F8) issue_layer(d, S.ain[q], S.w0, E, HID);
-              else {
-                // bias step (overwrites D), then the layer accumulating onto it
-                mma_bf16(d, d_ones, d_bias, idesc_bf16_f32(TILE, HID), 0u);
-                issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
-              }
+              // bias step (overwrites D), then the layer accumulating onto it
+              mma_bf16(d, d_ones, d_bias, idesc_bf16_f32(TILE, HID), 0u);
+              issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
               mma_commit(&S.mma_done[g][0]);
               mma_commit(&S.in_empty[q]);
             } else {
@@ -655,20 +600,23 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
               ph_act[g] ^= 1u;
               fence_after_sync();
               if (layer < 4) {
-                if (F8)
-                  issue_layer8(d, reinterpret_cast<const uint8_t *>(S.ah[g]), S.wh[layer - 1],
-                               HID, HID);
-                else {
-                  mma_bf16_ts(d, tmem + C::ones_col(g), d_bias + 256u * (uint32_t)layer,
-                              idesc_bf16_f32(TILE, HID), 0u);
-                  issue_ts<HID / 16, true>(d, tmem + C::act_col(g), d_wh + 2048u * (uint32_t)(layer - 1),
-                                           idesc_bf16_f32(TILE, HID));
+                // bias step (bias / dq, bf16), then the layer accumulating
+                // onto it: BF16 K steps of 16 with A = the bf16 activations,
+                // or E4M3 K steps of 32 with A = the E4M3 activations
+                mma_bf16_ts(d, tmem + C::ones_col(g), d_bias + 256u * (uint32_t)layer,
+                            idesc_bf16_f32(TILE, HID), 0u);
+                const uint64_t bd = d_wh + kHidStep * (uint32_t)(layer - 1);
+                if constexpr (F8) {
+#pragma unroll
+                  for (int k = 0; k < HID / 32; ++k)
+                    mma_e4m3_ts(d, tmem + C::act8_col(g) + 8u * k, bd + 16u * k,
+                                idesc_e4m3_f32(TILE, HID), 1u);
+                } else {
+                  issue_ts<HID / 16, true>(d, tmem + C::act_col(g), bd, idesc_bf16_f32(TILE, HID));
                 }
-              } else if (F8) {
-                issue_layer(tmem + C::head_col(g), S.ah[g], S.w4, HID, NOUT);
               } else {
                 issue_ts<HID / 16, false>(tmem + C::head_col(g), tmem + C::act_col(g), d_w4,
-                                   idesc_bf16_f32(TILE, NOUT));
+                                          idesc_bf16_f32(TILE, NOUT));
               }
               mma_commit(&S.mma_done[g][layer]);
             }
@@ -678,7 +626,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     }
     __syncwarp();
   } else if (loader_role) {
-    if constexpr (F8) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(kLoaderRegs8));
     // loaders: every wait result is taken warp-uniformly. Warp wq of group
     // L builds rows [32 wq, 32 wq + 32) of the group's tiles: pass 1 with
     // lane = row, pass 2 with 8 lanes per row (4 rows at a time).
@@ -748,18 +695,16 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         next_v = load_vox(p, row_voxel<MODE>(p, tile_of(i + 2) * TILE + wq * 32 + lane, ns, next));
     }
   } else {
-    if constexpr (F8 && kEpiRegs8 < kLaunchRegs8)
-      asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kEpiRegs8));
     // Epilogue warps. Every wait result is taken warp-uniformly
     // (__all_sync), so the .sync.aligned tcgen05.ld and the warp shuffles
     // below always run with all 32 lanes, also when a timeout makes the CTA
     // unwind.
-    if constexpr (!F8) {
-      // BF16: the 8 warps work on one slot's layer at a time (warp w: TMEM
-      // lane quarter w & 3, columns [64 (w >> 2), + 64)) and alternate the
-      // two slots layer by layer, so that one slot's MMAs run while the
-      // warps convert the other slot's activations. The MMA lane issues in
-      // the same order (per tile pair: layer by layer, slot 0 then slot 1).
+    {
+      // The 8 warps work on one slot's layer at a time (warp w: TMEM lane
+      // quarter w & 3, columns [64 (w >> 2), + 64)) and alternate the two
+      // slots layer by layer, so that one slot's MMAs run while the warps
+      // convert the other slot's activations. The MMA lanes issue in the
+      // same order (per tile pair: layer by layer, slot 0 then slot 1).
       const int q4 = warp & 3, h = warp >> 2;
       const int row = q4 * 32 + lane;
       const uint32_t tq = tmem + ((uint32_t)(q4 * 32) << 16);
@@ -776,17 +721,30 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
             }
             fence_after_sync();
             const uint32_t tl = tq + C::kSlotCols * g + 64 * h;
-            const uint32_t ta = tq + C::act_col(g);
+            // the next layer's A operand: bf16 pairs (BF16, and the FP8
+            // variant's head input) or E4M3 quadruples (FP8 hidden layers)
+            const uint32_t ta = tq + C::act_col(g), ta8 = tq + C::act8_col(g);
             // two 32-column chunks, the second one's TMEM load in flight
             // while the first is converted and stored back to tensor memory
-            // as the next layer's A operand
             float va[32], vb[32];
             tmem_ld32(tl, va);
             tmem_wait_ld_bind(va);
             tmem_ld32(tl + 32, vb);
-            epi_chunk(va, ta, 64 * h);
-            tmem_wait_ld_bind(vb);
-            epi_chunk(vb, ta, 64 * h + 32);
+            if (!F8) {
+              epi_chunk(va, ta, 64 * h);
+              tmem_wait_ld_bind(vb);
+              epi_chunk(vb, ta, 64 * h + 32);
+            } else if (layer < 3) {
+              const float dqs = p.dqs[layer];
+              epi_chunk8(va, dqs, ta8, 64 * h);
+              tmem_wait_ld_bind(vb);
+              epi_chunk8(vb, dqs, ta8, 64 * h + 32);
+            } else {
+              const float dq = p.dq[layer];
+              epi_chunk_dq(va, dq, ta, 64 * h);
+              tmem_wait_ld_bind(vb);
+              epi_chunk_dq(vb, dq, ta, 64 * h + 32);
+            }
             tmem_wait_st();
             fence_before_sync();
             __syncwarp();
@@ -801,62 +759,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
           head_store<MODE>(p, S.bias4, tq + C::head_col(h), tile_of(i + h) * TILE + row, ns, lane);
         }
       }
-    } else {
-    const int g = warp >> 2, q4 = warp & 3;
-    const int row = q4 * 32 + lane;
-    const uint32_t tl = tmem + ((uint32_t)(q4 * 32) << 16) + C::kSlotCols * g;
-    uint8_t *ah = reinterpret_cast<uint8_t *>(S.ah[g]);
-    bool ok = true;
-    for (int64_t i = g; ok; i += C::kSlots) {
-      int64_t tile = tile_of(i);
-      if (tile >= n_tiles) break;
-      const uint32_t par = (uint32_t)((i / C::kSlots) & 1);
-      int64_t r = tile * TILE + row;
-      for (int layer = 0; layer < 4; ++layer) {
-        if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) { ok = false; break; }
-        fence_after_sync();
-        const float *bias = S.bias[layer];
-        // 32-column chunks, the next one's TMEM load in flight while this
-        // one is converted and stored
-        float va[32], vb[32];
-        {
-          // layers 0-2 feed E4M3 layers; layer 3 feeds the BF16 head. The
-          // next chunk's TMEM load is in flight while this one is stored.
-          if (layer < 3) {
-            const float dqs = p.dqs[layer];
-            const float *bq = S.bias_q[layer];
-#pragma unroll 1
-            for (int c = 0; c < HID; c += 64) {
-              tmem_ld32(tl + c, va);
-              tmem_wait_ld_bind(va);
-              tmem_ld32(tl + c + 32, vb);
-              epi_chunk8(va, bq, dqs, ah, row, c);
-              tmem_wait_ld_bind(vb);
-              epi_chunk8(vb, bq, dqs, ah, row, c + 32);
-            }
-          } else {
-            const float dq = p.dq[layer];
-#pragma unroll 1
-            for (int c = 0; c < HID; c += 64) {
-              tmem_ld32(tl + c, va);
-              tmem_wait_ld_bind(va);
-              tmem_ld32(tl + c + 32, vb);
-              epi_chunk_dq(va, bias, dq, ah, row, c);
-              tmem_wait_ld_bind(vb);
-              epi_chunk_dq(vb, bias, dq, ah, row, c + 32);
-            }
-          }
-        }
-        fence_before_sync();
-        fence_async_smem();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&S.act_ready[g]);
-      }
-      if (!ok) break;
-      if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) { ok = false; break; }
-      fence_after_sync();
-      head_store<MODE>(p, S.bias4, tmem + ((uint32_t)(q4 * 32) << 16) + C::head_col(g), r, ns, lane);
-    }
     }
   }
   fence_before_sync();
@@ -885,15 +787,6 @@ int launch_mlp_grid(const MlpParams &p, cudaStream_t stream, int64_t grid_overri
   static bool attr_set = false;
   size_t smem = sizeof(MlpSmem<F8>) + 1024;
   if (!attr_set) {
-    if (F8) {
-      // the setmaxnreg split is sized for kLaunchRegs8 registers per thread;
-      // with any other compiled count it might not fit, and the loaders'
-      // setmaxnreg.inc would never return: refuse to launch
-      cudaFuncAttributes fa;
-      if (cudaFuncGetAttributes(&fa, mlp_tc_kernel<MODE, F8>) != cudaSuccess ||
-          fa.numRegs != kLaunchRegs8)
-        return NSVF_ERR_CUDA;
-    }
     if (cudaFuncSetAttribute(mlp_tc_kernel<MODE, F8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return NSVF_ERR_CUDA;

@@ -103,6 +103,19 @@ __device__ __forceinline__ void mma_bf16_ts(uint32_t tmem_d, uint32_t tmem_a, ui
       : "memory");
 }
 
+// E4M3 variant of mma_bf16_ts (kind::f8f6f4, K = 32): A in tensor memory,
+// four E4M3 per 32-bit column (element k in byte k % 4), from column tmem_a.
+__device__ __forceinline__ void mma_e4m3_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t b,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n\t}\n"
+      :
+      : "r"(tmem_d), "r"(tmem_a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // Arrive once on `bar` when all previously issued MMAs of this thread are done.
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile(

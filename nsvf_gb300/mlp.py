@@ -120,12 +120,12 @@ class TensorCoreMLP:
         return x
 
     def reference_fp8(self, emb):
-        """torch emulation of the FP8 kernel: bf16 input layer; for layers 0-2
-        the output relu(fmaf(acc, dq*qs, bias*qs)) rounded to saturating E4M3
-        (dq = 1 / (a_scale * w_scale) of the layer, qs = a_scale of the next,
-        all scalars in float32 as the library computes them; fmaf emulated in
-        float64); E4M3 weights; layer 3 relu(fmaf(acc, dq, bias)) in bf16;
-        bf16 head."""
+        """torch emulation of the FP8 kernel: bf16 input layer; the
+        accumulator of layer l starts at bias / dq (dq = 1 / (a_scale *
+        w_scale) of the layer, 1 for layer 0; float32 scalars as the library
+        computes them); for layers 0-2 the output relu(acc * dq * qs) (qs =
+        a_scale of the next layer) rounded to saturating E4M3, E4M3 weights;
+        layer 3 relu(acc * dq) in bf16; bf16 head."""
         import numpy as np
         f = self.fp8
         f32 = np.float32
@@ -136,13 +136,11 @@ class TensorCoreMLP:
         qs = as_ + [f32(1.0)]
         x = emb.float().to(torch.bfloat16).float() @ self.w[0].float().t()
         for l in range(4):
+            z = x + self.b[l].float() / float(dq[l])
             if l < 3:
-                dqs = float(f32(dq[l] * qs[l]))
-                bq = self.b[l] * float(qs[l])
-                y = (x.double() * dqs + bq.double()).float()
+                y = z * float(f32(dq[l] * qs[l]))
                 x = torch.relu(y).clamp(max=self.E4M3_MAX).to(e4).float()
                 x = x @ f["w8"][l].float().t()
             else:
-                y = (x.double() * float(dq[3]) + self.b[3].double()).float()
-                x = torch.relu(y).to(torch.bfloat16).float()
+                x = torch.relu(z * float(dq[3])).to(torch.bfloat16).float()
         return x @ self.w[4].float().t() + self.b[4]
