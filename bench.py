@@ -488,22 +488,42 @@ def run_ours(a):
     e2e_times = []
     h2d = d2h = 0
     # results land in pinned host buffers (as a serving front end would keep)
-    col_h = torch.empty(a.size * a.size, 3, dtype=torch.float32).pin_memory()
-    dep_h = torch.empty(a.size * a.size, dtype=torch.float32).pin_memory()
-    for i in range(a.steps):
-        flush.zero_()
+    col_h = [torch.empty(a.size * a.size, 3, dtype=torch.float32).pin_memory() for _ in range(2)]
+    dep_h = [torch.empty(a.size * a.size, dtype=torch.float32).pin_memory() for _ in range(2)]
+    h2d = host[a.warmup][0].numel() * 4 + host[a.warmup][1].numel() * 4
+    d2h = col_h[0].numel() * 4 + dep_h[0].numel() * 4
+    e2e_overlap = a.path == "served"
+    if e2e_overlap:
+        # served.HostFrames: frame i + 1's rays are copied in and frame i - 1's
+        # results copied out while frame i renders; the L2 flush between
+        # frames runs inside the timed region, on the rendering stream
+        from nsvf_gb300.served import HostFrames
+        pipe = HostFrames(scene, a.size * a.size)
+        frames = [(host[a.warmup + i][0], host[a.warmup + i][1], col_h[i % 2], dep_h[i % 2])
+                  for i in range(a.steps)]
+        with torch.no_grad():
+            pipe.render(frames[:2])   # allocates the frame buffers
         torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
         t0 = time.perf_counter()
-        rst, rdt = host[a.warmup + i]
-        rs_d = rst.to(dev, non_blocking=True)
-        rd_d = rdt.to(dev, non_blocking=True)
-        out = step(rs_d, rd_d)
-        col = col_h.copy_(out["colors"].reshape(-1, 3), non_blocking=True)
-        dep = dep_h.copy_(out["depths"].reshape(-1), non_blocking=True)
+        with torch.no_grad():
+            pipe.render(frames, before_frame=lambda i: flush.zero_())
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-        h2d = rst.numel() * 4 + rdt.numel() * 4
-        d2h = col.numel() * 4 + dep.numel() * 4
+    else:
+        for i in range(a.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rst, rdt = host[a.warmup + i]
+            rs_d = rst.to(dev, non_blocking=True)
+            rd_d = rdt.to(dev, non_blocking=True)
+            out = step(rs_d, rd_d)
+            col_h[0].copy_(out["colors"].reshape(-1, 3), non_blocking=True)
+            dep_h[0].copy_(out["depths"].reshape(-1), non_blocking=True)
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
     t_e2e = max_over_ranks(sum(e2e_times), dev)
 
     # the plain FP32 drop-in path on the same cameras, for the BF16-vs-FP32 ratio
@@ -590,7 +610,9 @@ def run_ours(a):
                    "samples_per_frame": (out_samples[0] // a.steps) if out_samples[0] else None,
                    "l2": "flushed (256 MB write) between timed frames", "parallelism": "replicas"},
         "e2e": {"value": round(job_throughput(rays_frame, a.steps, world, t_e2e), 1), "unit": "rays/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "copies": ("overlapped with the neighbouring frames' rendering (served.HostFrames); "
+                           "L2 flush inside the timed region") if e2e_overlap else "serial"},
         "gpu_launches": int(launches),
         "kernels_ms": kernel_ms,
         "roofline": roof,

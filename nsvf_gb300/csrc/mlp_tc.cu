@@ -129,14 +129,15 @@ struct MlpParams {
   const __nv_bfloat16 *w[5];         // row-major [N, K]: 128x32, 3x 128x128, 4x128
   const float *b[5];                 // [128] x4, [4]
   // FP8 variant: the hidden layers 1-3 as E4M3 bytes (row-major [128, 128],
-  // W * w_scale); the accumulators of layer l are multiplied by dq[l] =
-  // 1 / (a_scale[l] * w_scale[l]) before the bias, and the output of layer l
-  // (input of FP8 layer l + 1) is multiplied by qs[l] = a_scale[l + 1] before
-  // rounding to E4M3. Layer 0 (dq 1) and the head stay BF16.
+  // W * w_scale). Layer l's accumulator starts at bias / dq[l] (dq[l] =
+  // 1 / (a_scale[l] * w_scale[l]), 1 for layer 0) and is multiplied by dq[l]
+  // in the epilogue; the output of layer l (input of FP8 layer l + 1) is
+  // also multiplied by qs[l] = a_scale[l + 1] before rounding to E4M3.
+  // Layer 0 and the head stay BF16.
   const uint8_t *w8[3];
   float dq[4];
   float qs[4];
-  float dqs[3];                      // dq[l] * qs[l]: FP8 outputs are relu(fmaf(acc, dqs, bias * qs))
+  float dqs[3];                      // dq[l] * qs[l]: FP8 outputs are relu(acc * dqs)
   float *out;                        // [ns, 4]: sigma, r, g, b
   int64_t ns;                        // rows (the capacity when ns_dev is set)
   const int64_t *ns_dev;             // optional: row count read on the device

@@ -274,3 +274,75 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
             scene.bg_depth, _p(out["colors"]), _p(out["depths"]), _p(out["missed"]),
             int(bool(kahan)), stream), "composite_segments")
     return out
+
+
+class HostFrames:
+    """Frames whose rays sit in pinned host memory, rendered with their
+    results returned to pinned host memory, the copies overlapped with the
+    rendering: frame i + 1's rays go to the device on one copy stream while
+    frame i renders, and frame i's colours and depths come back on a second
+    copy stream while frame i + 1 renders. Two device slots per direction;
+    events order every reuse of a slot after the copy or frame that last
+    used it.
+
+    render(frames) takes a sequence of (ray_start [3] or [R, 3], ray_dir
+    [R, 3], colors [R, 3], depths [R]) host tensors (the last two pinned,
+    written) and returns when every frame's results are in host memory.
+    Frames have R rays each."""
+
+    def __init__(self, scene, R, mlp="tc", kahan=True):
+        dev = scene.device
+        self.scene, self.R, self.mlp, self.kahan = scene, R, mlp, kahan
+        self.copy_in = torch.cuda.Stream(dev)
+        self.copy_out = torch.cuda.Stream(dev)
+        e = lambda *s: torch.empty(*s, dtype=torch.float32, device=dev)
+        self.ro = [None, None]
+        self.rd = [e(R, 3), e(R, 3)]
+        self.out = [{"colors": e(R, 3), "depths": e(R), "missed": e(R)} for _ in range(2)]
+        ev = lambda: [torch.cuda.Event(), torch.cuda.Event()]
+        self.in_ready, self.in_free, self.done, self.out_free = ev(), ev(), ev(), ev()
+        self.n_samples = 0
+
+    def _stage_in(self, i, ro_h, rd_h):
+        s = i % 2
+        if self.ro[s] is None or self.ro[s].shape != ro_h.shape:
+            # a new origin buffer only after every use of the old one
+            self.in_free[s].synchronize()
+            self.ro[s] = torch.empty(ro_h.shape, dtype=torch.float32, device=self.scene.device)
+        with torch.cuda.stream(self.copy_in):
+            if i >= 2:
+                self.copy_in.wait_event(self.in_free[s])
+            self.ro[s].copy_(ro_h, non_blocking=True)
+            self.rd[s].copy_(rd_h, non_blocking=True)
+            self.in_ready[s].record(self.copy_in)
+
+    def render(self, frames, before_frame=None):
+        """before_frame(i), if given, runs on the rendering stream before
+        frame i is enqueued (for example an L2 flush between timed frames)."""
+        frames = list(frames)
+        if not frames:
+            return
+        cur = torch.cuda.current_stream(self.scene.device)
+        self._stage_in(0, frames[0][0], frames[0][1])
+        for i, (_, rd_h, col_h, dep_h) in enumerate(frames):
+            if rd_h.shape[0] != self.R:
+                raise ValueError("frame %d has %d rays, the pipeline %d" % (i, rd_h.shape[0], self.R))
+            if i + 1 < len(frames):
+                self._stage_in(i + 1, frames[i + 1][0], frames[i + 1][1])
+            s = i % 2
+            if before_frame is not None:
+                before_frame(i)
+            cur.wait_event(self.in_ready[s])
+            if i >= 2:
+                cur.wait_event(self.out_free[s])
+            out = render_frame(self.scene, self.ro[s], self.rd[s], kahan=self.kahan,
+                               out=self.out[s], mlp=self.mlp)
+            self.n_samples += int(out.get("n_samples", 0) or 0)
+            self.in_free[s].record(cur)
+            self.done[s].record(cur)
+            with torch.cuda.stream(self.copy_out):
+                self.copy_out.wait_event(self.done[s])
+                col_h.copy_(out["colors"], non_blocking=True)
+                dep_h.copy_(out["depths"], non_blocking=True)
+                self.out_free[s].record(self.copy_out)
+        self.copy_out.synchronize()

@@ -207,3 +207,35 @@ def test_sample_capacity_overflow_is_rendered_again(cuda, monkeypatch):
     # the capacity grew to hold the frame: the next frame renders in one go
     again = served.render_frame(scene, rs_t, rd_t)
     assert torch.equal(again["colors"], ref["colors"])
+
+
+def test_host_frames_match_render_frame(cuda):
+    """Frames rendered through served.HostFrames (rays from pinned host
+    memory, copies on two streams overlapping the neighbouring frames) equal
+    render_frame on device tensors, frame by frame, also when a frame's host
+    output slot is reused two frames later."""
+    from nsvf_gb300 import ext, scenes, served
+    enc, field, ren, vs = _scene(cuda, 1.0 / 32, 1.0, 30.0, 0.5, 64)
+    scene = served.SceneState(enc, field)
+    size = 96
+    cams = scenes.sphere_cameras(5, 4.0, seed=11)
+    host, refs = [], []
+    for c in cams:
+        rs, rd = scenes.pinhole_rays(c, size, size, 120.0)
+        rs_h = torch.from_numpy(np.ascontiguousarray(rs)).pin_memory()
+        rd_h = torch.from_numpy(np.ascontiguousarray(rd)).pin_memory()
+        host.append((rs_h, rd_h))
+        r = served.render_frame(scene, rs_h.to(cuda), rd_h.to(cuda))
+        refs.append((r["colors"].cpu(), r["depths"].cpu()))
+    R = size * size
+    outs = [(torch.empty(R, 3).pin_memory(), torch.empty(R).pin_memory()) for _ in cams]
+    pipe = served.HostFrames(scene, R)
+    pipe.render([(h[0], h[1], o[0], o[1]) for h, o in zip(host, outs)])
+    ext.check_errors(cuda)
+    for (col, dep), (rc, rdp) in zip(outs, refs):
+        assert torch.equal(col, rc) and torch.equal(dep, rdp)
+    # two host slots for five frames: each slot holds the last frame copied into it
+    ring = [(torch.empty(R, 3).pin_memory(), torch.empty(R).pin_memory()) for _ in range(2)]
+    pipe.render([(h[0], h[1]) + ring[i % 2] for i, h in enumerate(host)])
+    assert torch.equal(ring[0][0], refs[4][0]) and torch.equal(ring[1][0], refs[3][0])
+    assert pipe.n_samples > 0
