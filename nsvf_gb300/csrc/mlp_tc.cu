@@ -348,40 +348,49 @@ __device__ __forceinline__ void row_meta(const MlpParams &p, int64_t r, int64_t 
 
 // Input stage, pass 2 (8 lanes per row, lane cb owns channels 4cb..4cb+3):
 // sum_k w_k values[key_k][4cb..4cb+3] over the corners in order 0..7, one
-// fmaf per corner and channel -- per channel the interpolation kernel's
-// exact sequence. One load instruction reads four rows' 128-byte corner
-// rows whole. corner_loads issues the 8 loads of a row and returns the mask
-// of its valid corners; corner_blend (after the loads of the next row are
-// issued too) applies the weights.
-__device__ __forceinline__ uint32_t corner_loads(const MlpParams &p, int4 ka, int4 kb, int cb,
-                                                 float4 (&val)[8]) {
+// fused multiply-add per corner and channel -- per channel the interpolation
+// kernel's exact sequence. One load instruction reads four rows' 128-byte
+// corner rows whole. corner_loads issues the 8 loads of a row; a corner
+// without a valid key reads zeros, and its weight is zero too, so it leaves
+// the sum unchanged. corner_blend applies the weights, two channels per
+// instruction (fma.rn.f32x2 rounds each lane like fmaf).
+__device__ __forceinline__ void corner_loads(const MlpParams &p, int4 ka, int4 kb, int cb,
+                                             float4 (&val)[8]) {
   const int keys[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
-  uint32_t valid = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     val[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (keys[k] != kSkipKey) {
-      val[k] = __ldg(p.values + (int64_t)keys[k] * 8 + cb);
-      valid |= 1u << k;
-    }
+    if (keys[k] != kSkipKey) val[k] = __ldg(p.values + (int64_t)keys[k] * 8 + cb);
   }
-  return valid;
 }
 
-__device__ __forceinline__ float4 corner_blend(const float *__restrict__ w, uint32_t valid,
-                                               const float4 (&val)[8]) {
+__device__ __forceinline__ uint64_t pack_f32x2(float lo, float hi) {
+  uint64_t d;
+  asm("mov.b64 %0, {%1, %2};\n" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+
+// d = b * c + a on two FP32 lanes, each rounded once (round to nearest even)
+__device__ __forceinline__ uint64_t fma_f32x2(uint64_t b, uint64_t c, uint64_t a) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;\n" : "=l"(d) : "l"(b), "l"(c), "l"(a));
+  return d;
+}
+
+__device__ __forceinline__ float4 corner_blend(const float *__restrict__ w, const float4 (&val)[8]) {
   const float4 wa = reinterpret_cast<const float4 *>(w)[0];
   const float4 wb = reinterpret_cast<const float4 *>(w)[1];
   const float ws[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-  float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  uint64_t exy = 0, ezw = 0;  // (+0, +0)
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    if (!((valid >> k) & 1u)) continue;
-    e.x = fmaf(ws[k], val[k].x, e.x);
-    e.y = fmaf(ws[k], val[k].y, e.y);
-    e.z = fmaf(ws[k], val[k].z, e.z);
-    e.w = fmaf(ws[k], val[k].w, e.w);
+    const uint64_t wk = pack_f32x2(ws[k], ws[k]);
+    exy = fma_f32x2(wk, pack_f32x2(val[k].x, val[k].y), exy);
+    ezw = fma_f32x2(wk, pack_f32x2(val[k].z, val[k].w), ezw);
   }
+  float4 e;
+  asm("mov.b64 {%0, %1}, %2;\n" : "=f"(e.x), "=f"(e.y) : "l"(exy));
+  asm("mov.b64 {%0, %1}, %2;\n" : "=f"(e.z), "=f"(e.w) : "l"(ezw));
   return e;
 }
 
@@ -675,15 +684,14 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         // already in registers and loads nothing.
         const int4 *mk = reinterpret_cast<const int4 *>(mkey);
         float4 vc[8];
-        uint32_t mc = 0;
         int vc_id = 0;
 #pragma unroll 1
         for (int j = 0; j < 8; ++j) {
           const int r = rsub * 8 + ((2 * rsub + j) & 7);
           const int id = mvox[r];
-          if (j == 0 || id != vc_id) mc = corner_loads(p, mk[r * 2], mk[r * 2 + 1], cb, vc);
+          if (j == 0 || id != vc_id) corner_loads(p, mk[r * 2], mk[r * 2 + 1], cb, vc);
           vc_id = id;
-          store_in4(ain, wq * 32 + r, cb, corner_blend(mw + r * 8, mc, vc));
+          store_in4(ain, wq * 32 + r, cb, corner_blend(mw + r * 8, vc));
         }
       }
       if (bad && p.err) atomicOr(p.err, 4);
