@@ -77,11 +77,15 @@ __global__ void __launch_bounds__(kRayBlock) aabb_kernel(
 // ----------------------------------------------------------------- SVO ----
 
 // Packed octree, per point set of n nodes: for node k, its 8 children side
-// by side -- ids kids[8k + j] and boxes cbox[8k + j] -- and the root's own
-// box at cbox[8n]. A box is (cx, cy, cz, +half) for an internal node and
-// (cx, cy, cz, -half) for a leaf (children[8] == 1); absent children get a
-// zero box. Expanding a node is then two independent loads per lane, and a
-// node's whole child set lies in two 128-byte lines.
+// by side -- ids kids[8k + c] and boxes in cbox[8k .. 8k + 7] -- and the
+// root's own box at cbox[8n]. A box is (cx, cy, cz, +half) for an internal
+// node and (cx, cy, cz, -half) for a leaf (children[8] == 1); absent
+// children get a zero box. The boxes of children c and c + 4 (the two that
+// one traversal lane tests) are interleaved component by component:
+// cbox[8k + 2c] = (cx_c, cx_c+4, cy_c, cy_c+4) and cbox[8k + 2c + 1] =
+// (cz_c, cz_c+4, h_c, h_c+4), c = 0..3, so two 16-byte loads give a lane
+// both boxes as pairs for the two-lane (f32x2) slab test. A node's whole
+// child set lies in two 128-byte lines.
 __device__ __forceinline__ float4 node_box(const float *__restrict__ P,
                                            const int32_t *__restrict__ C, int k, float hv) {
   int size = C[(int64_t)k * 9 + 8];
@@ -104,13 +108,19 @@ __global__ void pack_octree_kernel(int64_t total, int n, float hv, const float *
   int cid = C[(int64_t)k * 9 + j];
   float4 cb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (cid > -1 && cid < n) cb = node_box(P, C, cid, hv);
-  B[(int64_t)k * 8 + j] = cb;
+  float *Bf = reinterpret_cast<float *>(B + (int64_t)k * 8 + 2 * (j & 3));
+  const int e = j >> 2;                 // first or second of the lane's pair
+  Bf[0 + e] = cb.x;
+  Bf[2 + e] = cb.y;
+  Bf[4 + e] = cb.z;
+  Bf[6 + e] = cb.w;
   kids[t] = cid;
   if (k == n - 1 && j == 0) B[(int64_t)n * 8] = node_box(P, C, n - 1, hv);
 }
 
 constexpr int kSvoLevels = 16;
-constexpr int kLanesPerRay = 4;                       // lane j owns children j + 4 c
+constexpr int kLanesPerRay = 4;                       // lane j owns children j and j + 4
+static_assert(kLanesPerRay == 4, "the packed octree pairs children c and c + 4 for one lane");
 constexpr int kRaysPerWarp = 32 / kLanesPerRay;       // 8
 constexpr int kRaysPerBlock = kRayBlock / kLanesPerRay;  // 32
 
@@ -200,6 +210,65 @@ __device__ __forceinline__ void warp_sort_row(int32_t *__restrict__ I, float *__
   }
 }
 
+// f32x2 helpers: two FP32 lanes per instruction, each rounded as the
+// scalar __fadd_rn / __fsub_rn / __fmul_rn would.
+__device__ __forceinline__ uint64_t f2(float lo, float hi) {
+  uint64_t d;
+  asm("mov.b64 %0, {%1, %2};\n" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ void f2_split(uint64_t v, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;\n" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;\n" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;\n" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;\n" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// nsvf_slab_fast on two boxes at once, given as pairs of their components
+// (c = (c_0, c_1) per axis, h = (|h_0|, |h_1|)): the same operations in the
+// same order on each lane, so each result equals nsvf_slab_fast's.
+__device__ __forceinline__ void slab_fast_pair(float ox, float oy, float oz, float ix, float iy,
+                                               float iz, float sx, float sy, float sz,
+                                               uint64_t cx, uint64_t cy, uint64_t cz, uint64_t h,
+                                               bool (&hit)[2], float (&t_lo)[2],
+                                               float (&t_hi)[2]) {
+  float lo[2] = {0.0f, 0.0f}, hi[2] = {100000.0f, 100000.0f};
+  const uint64_t zero = 0;
+  auto axis = [&](uint64_t c, float s, float o, float inv) {
+    const uint64_t sh = f2_mul(f2(s, s), h), oo = f2(o, o), ii = f2(inv, inv);
+    const uint64_t l = f2_add(f2_mul(f2_sub(f2_sub(c, sh), oo), ii), zero);
+    const uint64_t u = f2_mul(f2_sub(f2_add(c, sh), oo), ii);
+    float l0, l1, u0, u1;
+    f2_split(l, l0, l1);
+    f2_split(u, u0, u1);
+    lo[0] = fmaxf(lo[0], l0);
+    lo[1] = fmaxf(lo[1], l1);
+    hi[0] = (u0 < hi[0]) ? u0 : hi[0];
+    hi[1] = (u1 < hi[1]) ? u1 : hi[1];
+  };
+  axis(cx, sx, ox, ix);
+  axis(cy, sy, oy, iy);
+  axis(cz, sz, oz, iz);
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    t_lo[e] = lo[e];
+    t_hi[e] = hi[e];
+    hit[e] = !(lo[e] > hi[e]);
+  }
+}
+
 template <bool SORTED>
 __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int64_t rays, int m, int b_pts, int n, int n_max, const float *__restrict__ ray_start,
@@ -278,17 +347,24 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     }
     if (expand) {
       const int64_t kb = (int64_t)node * 8 + j;
+      // children j and j + 4: ids, and both boxes as component pairs
+      const float4 qa = CB[(int64_t)node * 8 + 2 * j], qb = CB[(int64_t)node * 8 + 2 * j + 1];
+      bool sh[NC];
+      if (fast) {
+        slab_fast_pair(ox, oy, oz, ix, iy, iz, sx, sy, sz, f2(qa.x, qa.y), f2(qa.z, qa.w),
+                       f2(qb.x, qb.y), f2(fabsf(qb.z), fabsf(qb.w)), sh, clo, chi);
+      } else {
+        sh[0] = nsvf_slab(ox, oy, oz, ix, iy, iz, qa.x, qa.z, qb.x, fabsf(qb.z), clo[0], chi[0]);
+        sh[1] = nsvf_slab(ox, oy, oz, ix, iy, iz, qa.y, qa.w, qb.y, fabsf(qb.w), clo[1], chi[1]);
+      }
+      cbw[0] = qb.z;
+      cbw[1] = qb.w;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         cid[c] = KD[kb + P * c];
         if (cid[c] > -1) {
-          if (cid[c] >= n) {
-            bad = true;
-          } else {
-            float4 b = CB[kb + P * c];
-            cbw[c] = b.w;
-            hit[c] = slab(b.x, b.y, b.z, fabsf(b.w), clo[c], chi[c]);
-          }
+          if (cid[c] >= n) bad = true;
+          else hit[c] = sh[c];
         }
       }
     }
@@ -363,9 +439,11 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
           top = t;
           if (isleaf) {
             if (j == 0) {
-              float4 cb = CB[(int64_t)s_node[base] * 8 + u];
+              const float *cb =
+                  reinterpret_cast<const float *>(CB + (int64_t)s_node[base] * 8 + 2 * (u & 3)) +
+                  (u >> 2);
               float a, b2;
-              slab(cb.x, cb.y, cb.z, -cb.w, a, b2);
+              slab(cb[0], cb[2], cb[4], -cb[6], a, b2);
               I[cnt] = ch; LO[cnt] = a; HI[cnt] = b2;
             }
             ++cnt;

@@ -685,7 +685,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
         const int4 *mk = reinterpret_cast<const int4 *>(mkey);
         float4 vc[8];
         int vc_id = 0;
-#pragma unroll 1
+#pragma unroll 2
         for (int j = 0; j < 8; ++j) {
           const int r = rsub * 8 + ((2 * rsub + j) & 7);
           const int id = mvox[r];
