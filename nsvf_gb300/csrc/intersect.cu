@@ -77,14 +77,15 @@ __global__ void __launch_bounds__(kRayBlock) aabb_kernel(
 // ----------------------------------------------------------------- SVO ----
 
 // Packed octree, per point set of n nodes: for node k, its 8 children side
-// by side -- ids kids[8k + c] and boxes in cbox[8k .. 8k + 7] -- and the
-// root's own box at cbox[8n]. A box is (cx, cy, cz, +half) for an internal
+// by side -- ids in kids[8k .. 8k + 7] and boxes in cbox[8k .. 8k + 7] --
+// and the root's own box at cbox[8n]. A box is (cx, cy, cz, +half) for an internal
 // node and (cx, cy, cz, -half) for a leaf (children[8] == 1); absent
 // children get a zero box. The boxes of children c and c + 4 (the two that
 // one traversal lane tests) are interleaved component by component:
 // cbox[8k + 2c] = (cx_c, cx_c+4, cy_c, cy_c+4) and cbox[8k + 2c + 1] =
 // (cz_c, cz_c+4, h_c, h_c+4), c = 0..3, so two 16-byte loads give a lane
-// both boxes as pairs for the two-lane (f32x2) slab test. A node's whole
+// both boxes as pairs for the two-lane (f32x2) slab test; the ids likewise,
+// kids[8k + 2c] = id_c and kids[8k + 2c + 1] = id_c+4, one 8-byte load. A node's whole
 // child set lies in two 128-byte lines.
 __device__ __forceinline__ float4 node_box(const float *__restrict__ P,
                                            const int32_t *__restrict__ C, int k, float hv) {
@@ -114,7 +115,7 @@ __global__ void pack_octree_kernel(int64_t total, int n, float hv, const float *
   Bf[2 + e] = cb.y;
   Bf[4 + e] = cb.z;
   Bf[6 + e] = cb.w;
-  kids[t] = cid;
+  kids[gk * 8 + 2 * (j & 3) + e] = cid;
   if (k == n - 1 && j == 0) B[(int64_t)n * 8] = node_box(P, C, n - 1, hv);
 }
 
@@ -346,8 +347,8 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
       cid[c] = -1;
     }
     if (expand) {
-      const int64_t kb = (int64_t)node * 8 + j;
       // children j and j + 4: ids, and both boxes as component pairs
+      const int2 ids = *reinterpret_cast<const int2 *>(KD + (int64_t)node * 8 + 2 * j);
       const float4 qa = CB[(int64_t)node * 8 + 2 * j], qb = CB[(int64_t)node * 8 + 2 * j + 1];
       bool sh[NC];
       if (fast) {
@@ -359,9 +360,10 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
       }
       cbw[0] = qb.z;
       cbw[1] = qb.w;
+      cid[0] = ids.x;
+      cid[1] = ids.y;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        cid[c] = KD[kb + P * c];
         if (cid[c] > -1) {
           if (cid[c] >= n) bad = true;
           else hit[c] = sh[c];
