@@ -32,6 +32,14 @@ sys.path.insert(0, ROOT)
 
 RAYS_PER_FRAME = 800 * 800
 MAX_HITS = 64
+# DRAM bytes per sample of the fused interpolation + MLP kernel, from ncu on a
+# 400x400 c2 frame: dram__bytes_read.sum + dram__bytes_write.sum = 125,100,288
+# + 46,736,384 bytes for 4,808,670 samples. Most of it is per sample (voxel id
+# and position in, sigma and RGB out: 36 B); the 21.9 MB corner table is read
+# about once per launch, so scaling by the samples overstates a full frame's
+# table reads, while some of the small launch's output writes were still in L2
+# when it ended.
+MLP_DRAM_BYTES_PER_SAMPLE = (125100288 + 46736384) / 4808670
 METRIC = "rays/s (full 800x800 frames)"
 
 
@@ -583,7 +591,10 @@ def run_ours(a):
                 "peak": tpk, "unit": "TFLOP/s", "frac": round(ach / tpk, 4),
                 "peak_source": "measured (bf16 burst)" if peaks else "fallback",
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": km["avg_ms"],
-                "traffic": None}
+                "traffic": round(MLP_DRAM_BYTES_PER_SAMPLE * out_samples[0] / max(1, km["launches"])),
+                "traffic_unit": "bytes per launch",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 400x400 launch "
+                                  "(4,808,670 samples: 171.8 MB), scaled by the samples per launch"}
     elif k:
         ach = alg / (k["avg_ms"] / 1e3) / 1e9
         roof = {"kernel": "svo_intersect_sorted", "bound": "hbm", "achieved": round(ach, 1),
