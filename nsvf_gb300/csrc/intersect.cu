@@ -410,15 +410,22 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int next = -1;
     while (__any_sync(full, pick)) {
       // bit l of L: level l (<= top) still has unvisited children. Level
-      // P k + j is byte k of lane j, so ballot k's group bits are levels
-      // P k .. P k + P - 1.
-      uint32_t L = 0;
-#pragma unroll
-      for (int k = 0; k < NLV; ++k) {
-        const uint32_t nz = __ballot_sync(
-            full, pick && j + P * k <= top && ((uint32_t)(stk >> (8 * k)) & 0xffu) != 0);
-        L |= ((nz >> gshift) & PM) << (P * k);
+      // P k + j is byte k of lane j: each lane sets bits j + P k for its
+      // non-empty bytes, and two xor shuffles OR them over the group.
+      static_assert(P == 4 && NLV == 4, "four one-byte levels per lane");
+      uint32_t own = 0;
+      if (pick && top >= 0) {
+        const uint32_t s32 = (uint32_t)stk;
+        // the high bit of every non-zero byte
+        const uint32_t nzb = (((s32 & 0x7f7f7f7fu) + 0x7f7f7f7fu) | s32) & 0x80808080u;
+        // bytes 0..3 (bits 7, 15, 23, 31) to bits 0, 4, 8, 12
+        const uint32_t sp = ((nzb >> 7) & 0x1u) | ((nzb >> 11) & 0x10u) | ((nzb >> 15) & 0x100u) |
+                            ((nzb >> 19) & 0x1000u);
+        own = (sp << j) & ((2u << top) - 1u);  // levels 0..top (top <= 15)
       }
+      uint32_t L = own;
+      L |= __shfl_xor_sync(full, L, 1);
+      L |= __shfl_xor_sync(full, L, 2);
       const int t = (pick && L != 0) ? 31 - __clz(L) : -1;
       uint32_t mine = 0, isleaf = 0;
       int u = 0;
