@@ -136,9 +136,11 @@ constexpr int kRaysPerBlock = kRayBlock / kLanesPerRay;  // 32
 // j + 12 (one byte each), the mask of hit children not visited yet (and
 // which of them are leaves); the child ids of each level sit in shared
 // memory. The next node to expand -- the highest unvisited child of the
-// deepest non-empty level -- comes from four ballots and a shuffle, the same
-// on all 4 lanes. The per-ray bookkeeping (ballots, stack, pick) is shared by
-// twice as many rays per warp instruction as with one child per lane.
+// deepest non-empty level -- comes from the group's mask of non-empty levels
+// (each lane's stack bytes as bits, OR-ed over the group by two xor
+// shuffles) and one shuffle from the level's owner lane, the same on all 4
+// lanes. The per-ray bookkeeping (ballots, stack, pick) is shared by twice
+// as many rays per warp instruction as with one child per lane.
 // When every hit child of a node is a leaf -- always the case for trees made
 // by build_octree, whose leaves all sit under depth-0 nodes -- the DFS visits
 // them consecutively, so the group emits them at once, the lane of child c
