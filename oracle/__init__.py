@@ -1,8 +1,9 @@
 """CPU oracle for the NSVF sparse-voxel hot path.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg, always as the checker. The product package
-(nsvf_gb300) never imports it.
+by bench.py's CPU-baseline leg, always to check or to time against, never as
+the thing measured or shipped. The product package (nsvf_gb300) never
+imports it.
 
 * ``oracle.cpu``       -- ctypes front end of the C restatement (clib_oracle.c)
                           plus numpy float64 restatements of the torch-level
