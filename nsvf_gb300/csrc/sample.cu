@@ -321,27 +321,50 @@ __device__ __forceinline__ WarpRay build_tab(RayTab &T, int H, const int32_t *__
   return w;
 }
 
-// Main-sequence sample j (0 <= j < M): voxel id, depth, distance.
-__device__ __forceinline__ void tab_sample(const RayTab &T, const WarpRay &w, int j, int32_t &id,
-                                           float &t, float &dist) {
-  int a = 0, e = w.nb;                     // b = #{b' < nb : end[b'] <= j}
+// Main-sequence sample j (0 <= j < M): voxel id, depth, distance, in two
+// steps so that a warp can pass each step's depth to the next sample's lane.
+// tab_step finds sample j's bin b and, for a step sample (not b's closing
+// segment), its step st and depth z. tab_finish takes z_prev, the depth of
+// sample j - 1, which is the lower edge whenever sample j - 1 is a step of
+// the same bin (st > sf[b] for a step; sf[b + 1] > sf[b] for the closing
+// segment), and gives the sample's id, depth t and distance.
+struct TabStep {
+  int b = 0, st = 0;
+  bool closing = false;
+  float z = 0.0f;
+};
+
+__device__ __forceinline__ TabStep tab_step(const RayTab &T, const WarpRay &w, int j) {
+  TabStep sp;
+  int a = 0, e = w.nb;
   while (a < e) {
     int mid = (a + e) >> 1;
     if (T.end[mid] <= j) a = mid + 1;
     else e = mid;
   }
-  const int b = a;
+  sp.b = a;
+  sp.closing = a < w.nb && j == T.end[a] - 1;
+  if (!sp.closing) {
+    sp.st = j - a;
+    sp.z = tab_z(T, sp.st, a, w.step);
+  }
+  return sp;
+}
+
+__device__ __forceinline__ void tab_finish(const RayTab &T, const WarpRay &w, const TabStep &sp,
+                                           float z_prev, int32_t &id, float &t, float &dist) {
+  const int b = sp.b;
   id = T.id[b];
-  if (b < w.nb && j == T.end[b] - 1) {
-    float zl = tab_zlow_close(T, b, w.step);
+  if (sp.closing) {
+    // tab_zlow_close: bin b's last step (sample j - 1), or its min depth
+    float zl = T.sf[b + 1] > T.sf[b] ? z_prev : T.lo[b];
     t = __fmul_rn(__fadd_rn(T.hi[b], zl), 0.5f);
     dist = __fsub_rn(T.hi[b], zl);
   } else {
-    const int st = j - b;
-    float z = tab_z(T, st, b, w.step);
-    float zl = st > T.sf[b] ? tab_z(T, st - 1, b, w.step) : T.lo[b];
-    t = __fmul_rn(__fadd_rn(z, zl), 0.5f);
-    dist = __fsub_rn(z, zl);
+    // the previous step of this bin is sample j - 1
+    float zl = sp.st > T.sf[b] ? z_prev : T.lo[b];
+    t = __fmul_rn(__fadd_rn(sp.z, zl), 0.5f);
+    dist = __fsub_rn(sp.z, zl);
   }
 }
 
@@ -459,12 +482,21 @@ __global__ void __launch_bounds__(32 * kWarpRays) icdf_warp_kernel(
       const float ox = o[0], oy = o[1], oz = o[2];
       const float dx = ray_dir[rr * 3], dy = ray_dir[rr * 3 + 1], dz = ray_dir[rr * 3 + 2];
       const int64_t base = offset[r], lim = offset[r + 1] < sample_cap ? offset[r + 1] : sample_cap;
+      // Sample j's lower edge is sample j - 1's depth z when both are steps
+      // of one bin: lane - 1 computed it (lane 31 of the previous round for
+      // lane 0), so each step's division runs once.
+      float z_last = 0.0f;
       for (int j0 = 0; j0 < w.M; j0 += 32) {
         const int j = j0 + lane;
+        TabStep sp;
+        if (j < w.M) sp = tab_step(T, w, j);
+        float z_prev = __shfl_up_sync(0xffffffffu, sp.z, 1);
+        if (lane == 0) z_prev = z_last;
+        z_last = __shfl_sync(0xffffffffu, sp.z, 31);
         if (j < w.M) {
           int32_t id;
           float t, dist;
-          tab_sample(T, w, j, id, t, dist);
+          tab_finish(T, w, sp, z_prev, id, t, dist);
           const int64_t pos = base + j;
           if (pos < lim) {
             vox[pos] = id;
