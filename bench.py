@@ -55,6 +55,8 @@ def parse():
                     help="frames of the plain FP32 path timed beside the served path")
     ap.add_argument("--cpu-rays", type=int, default=163840,
                     help="rays of the frame in the CPU baseline sample (about 12 s on one core)")
+    ap.add_argument("--ref-rays", type=int, default=0,
+                    help="reference arm: seeded rays per frame (0: full 800x800 frames)")
     ap.add_argument("--size", type=int, default=800,
                     help="frame side in pixels (800 = the c2 workload; smaller for profiling)")
     ap.add_argument("--precision", type=int, default=1,
@@ -240,15 +242,101 @@ def prune_bench(dev, sc, bits=8, th=0.5):
         torch.cuda.synchronize(dev)
         fp32_ms.append(s1.elapsed_time(e1))
     keep_fp32 = alpha >= th
+    # the exact pass: BF16 screen with the error scale M, double-float
+    # evaluation of the undecided points (TensorCoreMLP.prune_mask)
+    mlp.prune_mask(centers[:256], feats[:256], values, vs, th=th, bits=bits, rule=1, step=step)
+    torch.cuda.synchronize(dev)
+    ex_ms = []
+    for _ in range(2):
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s2.record()
+        keep_exact, _, n_undecided = mlp.prune_mask(centers, feats, values, vs, th=th, bits=bits,
+                                                    rule=1, step=step)
+        e2.record()
+        torch.cuda.synchronize(dev)
+        ex_ms.append(s2.elapsed_time(e2))
     return {"workload": "c2 pruning pass: %d voxels x %d^3 points, keep max(1-exp(-relu(s)*step)) >= %g; "
                         "density row of the field scaled by %g" % (V, bits, th, PRUNE_SIGMA_SCALE),
+            "exact_ms": round(min(ex_ms), 3),
+            "exact_path": "BF16 tensor-core screen (error scale M = sum |W4[0]| h) + double-float "
+                          "evaluation of the undecided points; mask of the rule without rounding error",
+            "undecided_points": n_undecided, "points": V * bits ** 3,
+            "kept_exact": int(keep_exact.sum()),
+            "mask_mismatches_exact_vs_fp32": int((keep_exact != keep_fp32).sum()),
             "alpha_fp32_median": float(alpha.median()),
             "bf16_fused_ms": round(s0.elapsed_time(e0), 3), "fp32_ms": round(min(fp32_ms), 3), "fp32_ms_both": [round(t, 1) for t in fp32_ms],
             "tflop": round(107520.0 * V * bits ** 3 / 1e12, 2),
             "bf16_tflops_achieved": round(107520.0 * V * bits ** 3 / (s0.elapsed_time(e0) / 1e3) / 1e12, 1),
             "kept_bf16": int(keep_bf16.sum()), "kept_fp32": int(keep_fp32.sum()),
-            "mask_mismatches": int((keep_bf16 != keep_fp32).sum()),
+            "mask_mismatches_bf16_scores_vs_fp32": int((keep_bf16 != keep_fp32).sum()),
             "max_abs_alpha_diff": float((score - alpha).abs().max())}
+
+
+def train_bench(dev, steps=5, warmup=2):
+    """The differentiation workload (c3): the c2 shell, a batch of 4 views
+    (cameras 0, 25, 50, 75) x 2,048 pixels drawn among those whose ray hits
+    a voxel, targets rendered from a second embedding set, the field's density
+    row scaled 30x (bias 0.5). One step = intersection + sampling, the FP32
+    forward, the hand-written backward with per-chunk recomputation
+    (nsvf_gb300.train), and an Adam step on the embeddings and the field."""
+    import torch
+    from nsvf_gb300 import ext, scenes, train
+    from nsvf_gb300.encoder import SparseVoxelEncoder
+    from nsvf_gb300.field import StandInField
+    p, vs = scenes.scene_shell(1.0 / 64)
+    args = argparse.Namespace(voxel_size=vs, max_hits=MAX_HITS, raymarching_stepsize_ratio=0.125,
+                              voxel_embed_dim=32, use_octree=True, deterministic_step=True)
+    enc = SparseVoxelEncoder(args, points=p)
+    with torch.no_grad():
+        enc.values.weight.copy_(scenes.voxel_embeddings(enc.values.weight.shape[0], 32, 0.01, seed=1))
+    field = StandInField(weights=scenes.stand_in_mlp_weights(seed=2, sigma_scale=30.0,
+                                                             sigma_bias=0.5))
+    enc, field = enc.to(dev), field.to(dev)
+    st = enc.precompute(id=None)
+    rng = np.random.RandomState(21)
+    ro, rd = [], []
+    for v in (0, 25, 50, 75):
+        rs, rdv = scenes.frame_view(v)
+        rdt = torch.from_numpy(rdv).to(dev)
+        _, _, _, hits = ext.svo_intersect_sorted(
+            torch.from_numpy(rs).to(dev).reshape(1, 1, 3).expand(1, rdt.shape[0], 3).contiguous(),
+            rdt[None], st["voxel_octree_center_xyz"].float()[None].contiguous(),
+            st["voxel_octree_children_idx"].int()[None].contiguous(), vs, MAX_HITS)
+        hit = hits[0].nonzero().squeeze(1).cpu().numpy()
+        pix = np.sort(rng.choice(hit, 2048, replace=False))
+        ro.append(np.broadcast_to(rs, (2048, 3)))
+        rd.append(rdv[pix])
+    ro = torch.from_numpy(np.concatenate(ro).astype(np.float32)).to(dev)
+    rd = torch.from_numpy(np.concatenate(rd).astype(np.float32)).to(dev)
+    with torch.no_grad():
+        v0 = enc.values.weight.clone()
+        enc.values.weight.copy_(scenes.voxel_embeddings(v0.shape[0], 32, 0.01, seed=7).to(dev))
+        target = train.render_batch(enc, field, ro, rd, states=st)
+        enc.values.weight.copy_(v0)
+    opt = torch.optim.Adam(list(enc.parameters()) + list(field.parameters()), lr=1e-3)
+    for _ in range(warmup):
+        train.train_step(enc, field, ro, rd, target, optimizer=opt, states=st)
+    torch.cuda.synchronize(dev)
+    torch.cuda.reset_peak_memory_stats(dev)
+    base = torch.cuda.memory_allocated(dev)
+    ts, losses = [], []
+    for _ in range(steps):
+        s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        loss = train.train_step(enc, field, ro, rd, target, optimizer=opt, states=st)
+        e0.record()
+        torch.cuda.synchronize(dev)
+        ts.append(s0.elapsed_time(e0))
+        losses.append(float(loss))
+    smp = train.sample_rays(enc, ro, rd, st)
+    return {"workload": "c3: 125,476-voxel shell, 4 views x 2,048 hit pixels, targets from a second "
+                        "embedding set, field density x30 (bias 0.5); FP32 forward, hand-written "
+                        "backward with per-chunk recomputation (1,024-ray chunks), Adam",
+            "ms_per_step": round(statistics.mean(ts), 3), "steps": steps,
+            "rays_per_s": round(8192 / (statistics.mean(ts) / 1e3), 1),
+            "samples_per_step": int(smp[1].ne(-1).sum()),
+            "peak_mem_mb_above_resident": round((torch.cuda.max_memory_allocated(dev) - base) / 2 ** 20, 1),
+            "loss_first_last": [round(losses[0], 6), round(losses[-1], 6)]}
 
 
 def serve_bench(dev, n_requests, rate=200.0, seed=0, chunk_rays=262144, samples_per_ray=128):
@@ -473,6 +561,7 @@ def run_ours(a):
     clocks.mark()
     times = []
     out_samples = [0]
+    far_n = [0, 0]
     l0 = LIB.nsvf_launch_count()
     for i in range(a.steps):
         flush.zero_()
@@ -483,11 +572,18 @@ def run_ours(a):
         torch.cuda.synchronize()
         times.append(s.elapsed_time(e) / 1e3)
         out_samples[0] += int(out.get("n_samples", 0) or 0)
+        far_n[0] += int(out.get("n_far_outside", 0) or 0)
+        far_n[1] += int(out.get("n_rays_refined_fp32", 0) or 0)
     launches = LIB.nsvf_launch_count() - l0
     clk = clocks.stop()
     ext.KERNEL_TIMING = False
     kernel_ms = ext.kernel_times_ms()
     t_dev = max_over_ranks(sum(times), dev)
+    far_stats = {"samples_far_outside_per_frame": far_n[0] / a.steps,
+                 "rays_refined_fp32_per_frame": far_n[1] / a.steps,
+                 "note": "samples with a trilinear coordinate outside [-0.5, 1.5] (the reference's "
+                         "sampling tail) are re-evaluated in double-float; rays where such a "
+                         "sample's colour exceeds 1000 get their other samples in FP32"}
 
     # --- end to end through the public API with host buffers ---
     torch.cuda.synchronize()
@@ -534,25 +630,40 @@ def run_ours(a):
             e2e_times.append(time.perf_counter() - t0)
     t_e2e = max_over_ranks(sum(e2e_times), dev)
 
-    # the plain FP32 drop-in path on the same cameras, for the BF16-vs-FP32 ratio
-    plain_fp32 = None
-    if a.path == "served" and a.plain_steps > 0:
-        def plain_step(rs, rd):
-            with torch.no_grad():
-                return render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3),
-                                   encoder_states=states)
-        plain_step(*dev_in[0])
+    # the plain FP32 kernels on the same cameras, for the BF16-vs-FP32 ratio:
+    # (1) the same served chain with the field's FP32 layers (nn.Linear,
+    # cuBLAS SGEMM) instead of the tensor-core BF16 kernel -- the ratio's
+    # denominator; (2) the drop-in module path (the reference's structure)
+    plain_fp32 = plain_dropin = None
+
+    def time_frames(fn, n):
+        fn(*dev_in[0])
         pt = []
-        for i in range(min(a.plain_steps, a.steps)):
+        for i in range(min(n, a.steps)):
             flush.zero_()
             s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s_.record()
-            plain_step(*dev_in[a.warmup + i])
+            fn(*dev_in[a.warmup + i])
             e_.record()
             torch.cuda.synchronize()
             pt.append(s_.elapsed_time(e_))
-        plain_fp32 = {"value": round(a.size * a.size * len(pt) / (sum(pt) / 1e3), 1), "unit": "rays/s",
-                      "ms_per_step": round(sum(pt) / len(pt), 3), "steps": len(pt)}
+        return {"value": round(a.size * a.size * len(pt) / (sum(pt) / 1e3), 1), "unit": "rays/s",
+                "ms_per_step": round(sum(pt) / len(pt), 3), "steps": len(pt)}
+
+    if a.path == "served" and a.plain_steps > 0:
+        def chain_fp32(rs, rd):
+            with torch.no_grad():
+                return render_frame(scene, rs, rd, mlp="fp32")
+
+        def dropin_fp32(rs, rd):
+            with torch.no_grad():
+                return render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3),
+                                   encoder_states=states)
+        plain_fp32 = time_frames(chain_fp32, a.plain_steps)
+        plain_fp32["path"] = ("served chain (same kernels, same samples) with the field's FP32 layers "
+                              "(torch nn.Linear, cuBLAS SGEMM, TF32 off) and the double-float pass")
+        plain_dropin = time_frames(dropin_fp32, a.plain_steps)
+        plain_dropin["path"] = "drop-in modules (SparseVoxelEncoder / VolumeRenderer), FP32 field"
 
     if rank != 0:
         dist.destroy_process_group()
@@ -606,6 +717,7 @@ def run_ours(a):
     serving = serve_bench(dev, a.serve_requests, chunk_rays=a.serve_chunk) \
         if a.serve_requests > 0 and world == 1 else None
     pruning = prune_bench(dev, sc) if world == 1 else None
+    training = train_bench(dev) if world == 1 else None
     precision = precision_bench(dev, sc, a.size, c4=bool(a.precision_c4)) \
         if (world == 1 and a.precision and a.path == "served") else None
     line = {
@@ -630,9 +742,14 @@ def run_ours(a):
         "roofline_intersection": roof_isect,
         "plain_fp32": plain_fp32,
         "speedup_vs_plain_fp32": (round(value / plain_fp32["value"], 2) if plain_fp32 else None),
+        "plain_fp32_dropin": plain_dropin,
+        "speedup_vs_plain_fp32_dropin": (round(value / plain_dropin["value"], 2) if plain_dropin
+                                         else None),
+        "far_outside": far_stats,
         "cpu_baseline": cpu,
         "serving": serving,
         "pruning": pruning,
+        "training": training,
         "precision": precision,
         "clocks": clk,
     }
@@ -640,29 +757,43 @@ def run_ours(a):
 
 
 # ------------------------------------------------------------ CPU arm --------
+# The CPU legs run only the oracle (oracle/: the C restatement of the
+# reference's traversal and sampling kernels plus float64 numpy for the
+# torch-level parts) on the oracle's own copy of the workload
+# (oracle/workload.py): no product module and no product library is loaded.
+# Work is spread over spawned worker processes, one ray chunk per task.
 
-def cpu_render(rays_o, rays_d, sc, threads=1):
-    """The hot path on the CPU with the oracle: C restatement of the SVO
-    traversal and inverse-CDF sampling (ctypes, GIL released, `threads` ray
-    chunks in parallel), float64 numpy interpolation, MLP and compositing."""
-    from concurrent.futures import ThreadPoolExecutor
+_CPU_SCENE = None
+
+
+def _cpu_worker_init(scene):
+    global _CPU_SCENE
+    _CPU_SCENE = scene
+
+
+def _cpu_chunk(args):
+    rays_o, rays_d = args
+    return cpu_render_chunk(rays_o, rays_d, _CPU_SCENE)
+
+
+def cpu_render_chunk(rays_o, rays_d, sc):
+    """One chunk of rays through the oracle: SVO traversal + depth sort,
+    probs/steps (slot-order sum), the reference wrapper's inverse-CDF sampling
+    (deterministic jitter), float64 interpolation, MLP and compositing, white
+    background. Returns colours [n, 3] and missed [n] (float64)."""
     from oracle import cpu
     vs = sc["voxel_size"]
     cen, chi = sc["octree"]
     step = vs / 8
-    R = rays_d.shape[0]
-    chunks = np.array_split(np.arange(R), max(1, threads * 4))
-
-    def one(ix):
-        o = np.broadcast_to(rays_o, (len(ix), 3))[None]
-        idx, lo, hi = cpu.sort_hits(*cpu.svo_intersect(o, rays_d[ix][None], cen[None], chi[None],
-                                                       vs, MAX_HITS))
-        idx, lo, hi = idx[0], lo[0], hi[0]
-        hit = (idx != -1).any(-1)
-        col = np.zeros((len(ix), 3))
-        mis = np.ones(len(ix))
-        if hit.sum() == 0:
-            return col, mis
+    n = rays_d.shape[0]
+    o = np.broadcast_to(rays_o, (n, 3))[None]
+    idx, lo, hi = cpu.sort_hits(*cpu.svo_intersect(o, rays_d[None], cen[None], chi[None], vs,
+                                                   MAX_HITS))
+    idx, lo, hi = idx[0], lo[0], hi[0]
+    hit = (idx != -1).any(-1)
+    col = np.zeros((n, 3))
+    mis = np.ones(n)
+    if hit.sum() > 0:
         I, L, Hh = idx[hit], lo[hit], hi[hit]
         pr, st = cpu.probs_steps(I, L, Hh, step)
         N = I.shape[0]
@@ -670,7 +801,7 @@ def cpu_render(rays_o, rays_d, sc, threads=1):
         si, sd, ss = cpu.inverse_cdf_op(I, L, Hh, pr, st, np.full((N, M), 0.5, np.float32))
         ss = np.maximum(ss, 0)
         mask = si != -1
-        xyz = rays_o[None, None].astype(np.float64) + rays_d[ix][hit][:, None, :] * sd[..., None]
+        xyz = rays_o[None, None].astype(np.float64) + rays_d[hit][:, None, :] * sd[..., None]
         emb = cpu.trilinear_embed(xyz[mask], si[mask], sc["centers_shifted"], sc["feats"],
                                   sc["values"], vs)
         sig, rgb = cpu.mlp_forward(emb, sc["weights_np"])
@@ -680,74 +811,100 @@ def cpu_render(rays_o, rays_d, sc, threads=1):
         out = cpu.composite(S, C, sd.astype(np.float64), ss.astype(np.float64), mask)
         col[hit] = out["colors"]
         mis[hit] = out["missed"]
-        return col, mis
-
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        res = list(ex.map(one, chunks))
-    col = np.concatenate([r[0] for r in res])
-    mis = np.concatenate([r[1] for r in res])
     return col + mis[:, None] * 1.0, mis
 
 
+class CpuPool:
+    """`workers` spawned processes holding the scene (1 = this process).
+    BLAS threads are pinned to one per process."""
+
+    def __init__(self, sc, workers):
+        self.sc, self.workers, self.ex = sc, workers, None
+        if workers > 1:
+            import multiprocessing
+            from concurrent.futures import ProcessPoolExecutor
+            for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+                os.environ[k] = "1"
+            self.ex = ProcessPoolExecutor(max_workers=workers,
+                                          mp_context=multiprocessing.get_context("spawn"),
+                                          initializer=_cpu_worker_init, initargs=(sc,))
+            # start every worker (and its scene copy) before any timing
+            list(self.ex.map(_cpu_chunk, [(np.zeros(3, np.float32), np.zeros((1, 3), np.float32)
+                                           + np.float32(0.5))] * workers))
+
+    def render(self, rays_o, rays_d, chunk=8192):
+        if self.ex is None:
+            return cpu_render_chunk(rays_o, rays_d, self.sc)
+        parts = [(rays_o, rays_d[i:i + chunk]) for i in range(0, rays_d.shape[0], chunk)]
+        res = list(self.ex.map(_cpu_chunk, parts))
+        return np.concatenate([r[0] for r in res]), np.concatenate([r[1] for r in res])
+
+    def close(self):
+        if self.ex is not None:
+            self.ex.shutdown()
+
+
 def cpu_scene():
-    import torch
-    from nsvf_gb300 import geometry, scenes
-    p, vs = scenes.scene_shell(1.0 / 64)
-    pts = torch.from_numpy(p)
-    cen, chi = geometry.build_easy_octree(pts, vs / 2)
-    keys, feats = geometry.voxel_corner_table(pts, vs)
-    values = scenes.voxel_embeddings(keys.shape[0], 32, 0.01, seed=1).numpy()
-    shifted = p.copy()
-    shifted[:, 0] += np.float32(vs / 10)
-    weights = scenes.stand_in_mlp_weights(seed=2)
-    return dict(voxel_size=vs, octree=(cen.numpy(), chi.numpy()), feats=feats.numpy(),
-                values=values, centers_shifted=shifted,
-                weights_np=[(W.numpy(), b.numpy()) for W, b in weights])
+    from oracle import workload
+    return workload.c2_scene()
 
 
 def cpu_baseline(n_rays, threads=1):
-    """Oracle CPU render of a fixed seeded sample of n_rays rays of frame 0."""
+    """Oracle CPU render of a fixed seeded sample of n_rays rays of frame 0,
+    in this process (one core)."""
+    from oracle import workload
     sc = cpu_scene()
-    rs, rd = frame_rays(0)
+    rs, rd = workload.frame(0)
     sel = np.random.RandomState(0).choice(rd.shape[0], n_rays, replace=False)
+    pool = CpuPool(sc, threads)
     t0 = time.perf_counter()
-    cpu_render(rs, rd[sel], sc, threads=threads)
+    pool.render(rs, rd[sel])
     dt = time.perf_counter() - t0
+    pool.close()
     return {"value": round(n_rays / dt, 1), "unit": "rays/s", "cores": threads, "kind": "port",
             "sample": "%d seeded rays of the 800x800 frame 0 (oracle C traversal/sampling, "
-                      "float64 numpy interpolation/MLP/compositing)" % n_rays,
+                      "float64 numpy interpolation/MLP/compositing; oracle workload copy)" % n_rays,
             "seconds": round(dt, 2), "nproc": os.cpu_count()}
 
 
 def run_reference(a):
+    """The CPU reference arm: the oracle port of the reference's path on
+    every host core (spawned processes), on full 800x800 frames of the same
+    cameras (a.ref_rays > 0 times that many seeded rays per frame instead)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    import torch
-    torch.set_num_threads(threads)
+    from oracle import workload
+    workers = os.cpu_count() or 1
     sc = cpu_scene()
-    n = a.cpu_rays
+    pool = CpuPool(sc, workers)
+    n = a.ref_rays if a.ref_rays > 0 else RAYS_PER_FRAME
     times = []
     for i in range(a.warmup + a.steps):
-        rs, rd = frame_rays(i)
-        sel = np.random.RandomState(i).choice(rd.shape[0], n, replace=False)
+        rs, rd = workload.frame(i)
+        if n < rd.shape[0]:
+            rd = rd[np.sort(np.random.RandomState(i).choice(rd.shape[0], n, replace=False))]
         t0 = time.perf_counter()
-        cpu_render(rs, rd[sel], sc, threads=threads)
+        pool.render(rs, rd)
         if i >= a.warmup:
             times.append(time.perf_counter() - t0)
+    pool.close()
     value = n * len(times) / sum(times)
+    full = n == RAYS_PER_FRAME
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "rays/s",
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": round(1e3 * sum(times) / len(times), 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
             "config": {"workload": "c2: 125,476-voxel shell, 800x800 frames, SVO, max_hits 64, "
-                                   "step 1/512, 4x128 MLP", "sample_rays_per_step": n},
-            "cpu_baseline": {"value": round(value, 1), "unit": "rays/s", "cores": threads,
+                                   "step 1/512, 4x128 MLP",
+                       "rays_per_step": n, "full_frames": full},
+            "cpu_baseline": {"value": round(value, 1), "unit": "rays/s", "cores": workers,
                              "kind": "port",
-                             "sample": "%d seeded rays per frame, oracle port (C traversal and "
-                                       "sampling, numpy float64 rest), %d threads" % (n, threads)},
+                             "sample": ("full 800x800 frames" if full else
+                                        "%d seeded rays per frame" % n) +
+                                       ", oracle port (C traversal and sampling, numpy float64 "
+                                       "rest), %d worker processes" % workers},
             "e2e": {"value": round(value, 1), "unit": "rays/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

@@ -83,10 +83,13 @@ int nsvf_svo_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_ma
  * (b_pts * n, 176 bytes each: 44 MiB, held by every GPU that loads the
  * library until the process exits). Larger octrees are rejected with
  * NSVF_ERR_CAPACITY. It allocates nothing: the first call on a device looks
- * the array's device address up (cudaGetSymbolAddress, once per device), so
- * make that first call before any stream capture. All calls share the one
- * array: calls that overlap on the GPU (other streams, other threads) race
- * and must be serialised by the caller. */
+ * the array's device address up (cudaGetSymbolAddress, once per device,
+ * cached), so make that first call before any stream capture. The cached
+ * address does not survive a device reset (cudaDeviceReset, or a primary
+ * context released and created again): do not call this entry point on a
+ * device after resetting it. All calls share the one array: calls that
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. */
 #define NSVF_NOALLOC_MAX_NODES (1 << 18)
 int nsvf_svo_intersect_noalloc(int b, int b_pts, int n, int m, float voxelsize, int n_max,
                                const float *ray_start, const float *ray_dir, const float *points,
@@ -143,6 +146,31 @@ int nsvf_uniform_ray_sampling(int b, int m, int max_hits, int max_steps, float s
                               const float *max_depth, const float *noise, int32_t *sampled_idx,
                               float *sampled_depth, float *sampled_dists, int32_t *err,
                               void *stream);
+
+/* parallel_ray_sampling: the reference's back-up uniform sampler
+ * (`_parallel_ray_sampling`, fairnr/clib/__init__.py:303-349, pure torch
+ * there), one chunk of rows. Per row (pts_idx/min_depth/max_depth
+ * [rows, max_hits], sorted hit lists with MAX_DEPTH in missing slots): steps
+ * u_k = min_depth[0] + (k + j_k) * march_size, k < n_steps (j = noise
+ * [rows, n_steps], or 0.5 when noise is NULL), each with the id of slot
+ * #{i : min_depth_i <= u_k} - 1; the exits, entries and steps sorted
+ * (ties in that order, so that at a face shared by two voxels the next
+ * segment takes the entered voxel's id; the reference's torch.sort leaves
+ * such ties unspecified); between consecutive depths a segment with midpoint
+ * .5 (a + b), length b - a and the first depth's id, kept when it lies in one
+ * voxel (#{min_depth <= mid} - 1 == #{max_depth <= mid}), not beyond the last
+ * exit (MAX_DEPTH exits read as 0) and not of length 0. Writes the kept
+ * segments in order into sampled_idx / sampled_depth / sampled_dists
+ * [rows, out_width] (then -1 / 10000 / 0) and their number to count[rows]
+ * (may be NULL). out_width >= 2 max_hits + n_steps - 1 holds every segment.
+ * NSVF_ERR_CAPACITY if a row's lists exceed the shared memory (4 rows per
+ * block, nsvf_parallel_sampling_smem_bytes each, 224 KB in all). */
+int64_t nsvf_parallel_sampling_smem_bytes(int max_hits, int n_steps);
+int nsvf_parallel_ray_sampling(int64_t rows, int max_hits, int n_steps, float march_size,
+                               const int32_t *pts_idx, const float *min_depth,
+                               const float *max_depth, const float *noise, int out_width,
+                               int32_t *sampled_idx, float *sampled_depth, float *sampled_dists,
+                               int32_t *count, void *stream);
 
 /* inverse_cdf_sampling: replaces `inverse_cdf_sampling(pts_idx, min_depth,
  * max_depth, uniform_noise, probs, steps, fixed_step_size)`
@@ -303,12 +331,22 @@ int nsvf_camera_rays(int64_t n, const float *cam, float *ray_start, float *ray_d
 int nsvf_compact_hits(int64_t n, const uint8_t *hits, const int32_t *scan, int64_t *pix,
                       int64_t *n_hit, void *stream);
 
+/* ray_probs: the sampling distribution of NSVFModel.intersecting
+ * (fairnr/models/nsvf.py:65-74) for rows [rows, max_hits] of sorted hit
+ * lists: d_k = max_depth_k - min_depth_k on hit slots (idx != -1), else 0;
+ * tot = d_0 + d_1 + ... added in slot order in FP32 (the order of a plain
+ * loop; torch's reduction order is unspecified and differs between builds
+ * and devices); probs [rows, max_hits] = d / tot; steps [rows] = tot /
+ * step_size. Rows without hits get 0 / 0 = NaN probs and 0 steps, as the
+ * reference's division does. max_hits <= 128. */
+int nsvf_ray_probs(int64_t rows, int max_hits, float step_size, const int32_t *idx,
+                   const float *min_depth, const float *max_depth, float *probs, float *steps,
+                   void *stream);
+
 /* gather_probs: for rows i < *n_hit, copies the sorted hit list of ray pix[i]
- * ([., max_hits] idx/min/max) and builds its sampling distribution as
- * fairnr/models/nsvf.py:65-74: d = max - min on hit slots, probs = d / sum d,
- * steps = sum d / step_size. One warp per row: lane l sums slots l, l + 32,
- * ... in order, then the 32 partial sums are added by an xor butterfly
- * (offsets 16, 8, 4, 2, 1). */
+ * ([., max_hits] idx/min/max) and builds its sampling distribution exactly as
+ * nsvf_ray_probs does (same sum order, same roundings), so the served chain
+ * samples exactly the drop-in path's samples. max_hits <= 128. */
 int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
                       const int64_t *pix, const int32_t *idx, const float *min_depth,
                       const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
@@ -344,13 +382,80 @@ int nsvf_composite_segments_dev(int64_t rays_cap, const int64_t *n_rays_dev,
 
 /* field_samples_bf16_dev: nsvf_field_samples_bf16 on *n_samples_dev samples
  * (at most `capacity`; a larger count sets err bit 1), one persistent CTA
- * per SM. */
+ * per SM. If n_outliers is not NULL, every sample lying far outside its
+ * voxel (a trilinear coordinate outside [-0.5, 1.5]) is also appended to
+ * outliers (int64 sample indices, in no particular order; *n_outliers, zeroed
+ * by the caller, counts them; past outlier_cap entries err bit 4 (16) is set)
+ * for nsvf_field_exact_dev. */
 int nsvf_field_samples_bf16_dev(int64_t capacity, const int64_t *n_samples_dev,
                                 const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
                                 int64_t n_keys, float voxel_size, const float *centers,
                                 const int32_t *feats, const float *values,
                                 const void *const weights[5], const float *const biases[5],
-                                float *out, int32_t *err, void *stream);
+                                float *out, int64_t *outliers, int64_t *n_outliers,
+                                int64_t outlier_cap, int32_t *err, void *stream);
+
+/* flag_outliers: the outlier list of nsvf_field_samples_bf16_dev for a field
+ * evaluated elsewhere: samples s < min(*n_samples_dev, capacity)
+ * (n_samples_dev may be NULL: capacity samples) with a trilinear coordinate
+ * outside [-0.5, 1.5] in voxel[s] (computed as nsvf_trilinear_embed does)
+ * are appended to list (*n_list zeroed by the caller; err bit 4 past
+ * list_cap). No reference counterpart. */
+int nsvf_flag_outliers(int64_t capacity, const int64_t *n_samples_dev, const int32_t *voxel,
+                       const float *xyz_dist, int64_t n_voxels, float voxel_size,
+                       const float *centers, int64_t *list, int64_t *n_list, int64_t list_cap,
+                       int32_t *err, void *stream);
+
+/* field_exact_dev: the workloads' field (32 -> 4 x 128 -> 4, ReLU) at the
+ * listed samples, in double-float arithmetic (pairs of FP32 numbers:
+ * error-free TwoSum / TwoProduct transformations and the compensated Dot2
+ * dot product), written over out[s] = (sigma, r, g, b), rounded once to FP32.
+ * No reference counterpart: the reference evaluates these samples in FP32,
+ * where their extrapolated trilinear weights (up to 1e5 and more) turn the
+ * field's relative rounding error into colour errors far above 2e-3.
+ * Samples are the served layout: ray row i < min(*n_rows_dev, rows_cap) owns
+ * samples [offset[i], offset[i + 1]); its ray is ray_index[i] (NULL:
+ * identity) with origin ray_start[ray * ray_start_stride] (stride 3, or 0 for
+ * one shared origin) and direction ray_dir[ray * 3]; sample s sits at depth[s]
+ * in voxel[s]. The position o + d t, the trilinear weights, the embedding and
+ * every layer are computed in double-float. weights_t[l] = W_l transposed,
+ * [in, out] FP32 (32x128, 128x128 x3, 128x4); biases FP32. The list is read
+ * on the device: min(*n_list, list_cap) entries. out 16-byte aligned.
+ * If n_refine_rows is not NULL, the row of every listed sample whose
+ * re-evaluated |r|, |g| or |b| exceeds refine_above is appended to
+ * refine_rows (*n_refine_rows zeroed by the caller; err bit 4 past
+ * refine_cap) for nsvf_field_refine_fp32_dev. */
+int nsvf_field_exact_dev(int64_t rows_cap, const int64_t *n_rows_dev, const int64_t *offset,
+                         const int64_t *ray_index, const float *ray_start,
+                         int64_t ray_start_stride, const float *ray_dir, const float *depth,
+                         const int32_t *voxel, int64_t n_voxels, int64_t n_keys,
+                         float voxel_size, const float *centers, const int32_t *feats,
+                         const float *values, const float *const weights_t[5],
+                         const float *const biases[5], const int64_t *list,
+                         const int64_t *n_list, int64_t list_cap, float *out,
+                         float refine_above, int64_t *refine_rows, int64_t *n_refine_rows,
+                         int64_t refine_cap, int32_t *err, void *stream);
+
+/* field_refine_fp32_dev: the rows (rays) listed by nsvf_field_exact_dev --
+ * those whose far-outside sample has a colour magnitude above refine_above --
+ * get every other sample's (sigma, r, g, b) evaluated again in FP32 on the
+ * CUDA cores (interpolation as nsvf_trilinear_embed, the layers with FP32
+ * weights and activations), written over out. Such a sample's colour C
+ * multiplies the error of the transmittance in front of it; in BF16 that
+ * error is about 1e-6 (800x800 c4 frame), so rays with C above ~1000 would
+ * leave more than 1e-3 of colour error. Samples far outside their voxel keep
+ * their double-float values. rows / *n_rows_list (capacity rows_list_cap)
+ * index ray rows < min(*n_rays_dev, rays_cap) of the served layout
+ * (offset [rows + 1]); samples past sample_cap are not touched. No reference
+ * counterpart. */
+int nsvf_field_refine_fp32_dev(const int64_t *rows, const int64_t *n_rows_list,
+                               int64_t rows_list_cap, int64_t rays_cap,
+                               const int64_t *n_rays_dev, const int64_t *offset,
+                               int64_t sample_cap, const int32_t *voxel, const float *xyz_dist,
+                               int64_t n_voxels, int64_t n_keys, float voxel_size,
+                               const float *centers, const int32_t *feats, const float *values,
+                               const float *const weights_t[5], const float *const biases[5],
+                               float *out, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Field MLP on the tensor cores                                             */
@@ -395,13 +500,16 @@ int nsvf_field_samples_fp8(int64_t n_samples, const int32_t *voxel, const float 
                            const float scales[6], float *out, int32_t *err, void *stream);
 
 /* field_samples_fp8_dev: nsvf_field_samples_fp8 on *n_samples_dev samples
- * (at most `capacity`), one persistent CTA per SM. */
+ * (at most `capacity`), one persistent CTA per SM; outlier list as
+ * nsvf_field_samples_bf16_dev. */
 int nsvf_field_samples_fp8_dev(int64_t capacity, const int64_t *n_samples_dev,
                                const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
                                int64_t n_keys, float voxel_size, const float *centers,
                                const int32_t *feats, const float *values,
                                const void *const weights[5], const float *const biases[5],
-                               const float scales[6], float *out, int32_t *err, void *stream);
+                               const float scales[6], float *out, int64_t *outliers,
+                               int64_t *n_outliers, int64_t outlier_cap, int32_t *err,
+                               void *stream);
 
 /* wait_timeout_selftest: the failure path of the kernels' bounded waits,
  * without a fault. One CTA waits on an mbarrier phase that never completes;
@@ -425,6 +533,41 @@ int nsvf_prune_scores_bf16(int64_t n_voxels, int bits, int rule, float step, int
                            const float *values, const void *const weights[5],
                            const float *const biases[5], uint32_t *score, int32_t *err,
                            void *stream);
+
+/* prune_screen_bf16 + prune_exact_dev: the pruning mask of
+ * SparseVoxelEncoder.pruning (fairnr/modules/encoder.py:605-618, get_scores
+ * :620-654), decided exactly. With T = -ln(1 - th) (rule 0, the reference's
+ * rule: keep = 1 - min exp(-relu sigma) > th, i.e. max sigma > T) or
+ * T = -ln(1 - th) / step (rule 1: keep = max 1 - exp(-relu(sigma) step) >=
+ * th, i.e. max sigma >= T), 0 < th < 1:
+ *  - prune_screen_bf16 runs the tensor-core pass of nsvf_prune_scores_bf16
+ *    (score as there) and also computes, per point, M = sum_j |W4[0][j]| h_j
+ *    from its BF16 activations h. A point with sigma - band * M above T sets
+ *    keep[v] = 1 (uint8, zeroed by the caller); a point with sigma + band * M
+ *    >= T that did not is appended (row v * bits^3 + i, int64) to list
+ *    (*n_list zeroed by the caller; past list_cap err bit 4 (16) is set: call
+ *    again with a larger list). The BF16 error of sigma measured on the
+ *    workloads' fields stays below 0.005 M; band = 0.02 leaves a factor 4.
+ *  - prune_exact_dev evaluates the listed points of voxels not yet kept in
+ *    double-float arithmetic (as nsvf_field_exact_dev; point positions with
+ *    offset_points' FP32 operations, fairnr/data/geometry.py:229-238) and sets
+ *    keep[v] = 1 when sigma reaches T (T passed as a double, compared as a
+ *    double-float). weights_t / biases as nsvf_field_exact_dev.
+ * The mask is that of the reference's rule evaluated without rounding error;
+ * an FP32 evaluation agrees with it except for voxels whose max sigma lies
+ * within FP32 rounding of T. */
+int nsvf_prune_screen_bf16(int64_t n_voxels, int bits, int rule, float step, float threshold,
+                           float band, int64_t n_keys, float voxel_size, const float *centers,
+                           const int32_t *feats, const float *values,
+                           const void *const weights[5], const float *const biases[5],
+                           uint32_t *score, uint8_t *keep, int64_t *list, int64_t *n_list,
+                           int64_t list_cap, int32_t *err, void *stream);
+int nsvf_prune_exact_dev(int64_t n_voxels, int bits, int rule, double threshold, int64_t n_keys,
+                         float voxel_size, const float *centers, const int32_t *feats,
+                         const float *values, const float *const weights_t[5],
+                         const float *const biases[5], const int64_t *list,
+                         const int64_t *n_list, int64_t list_cap, uint8_t *keep, int32_t *err,
+                         void *stream);
 
 #ifdef __cplusplus
 }

@@ -54,15 +54,28 @@ def _load():
         "nsvf_camera_rays": ([i64, P, P, P, P], i32),
         "nsvf_compact_hits": ([i64, P, P, P, P, P], i32),
         "nsvf_gather_probs": ([i64, P, i32, f32, P, P, P, P, P, P, P, P, P, P], i32),
+        "nsvf_ray_probs": ([i64, i32, f32, P, P, P, P, P, P], i32),
+        "nsvf_parallel_ray_sampling": ([i64, i32, i32, f32, P, P, P, P, i32, P, P, P, P, P], i32),
+        "nsvf_parallel_sampling_smem_bytes": ([i32, i32], i64),
+        "nsvf_prune_screen_bf16": ([i64, i32, i32, f32, f32, f32, i64, f32, P, P, P, P, P, P, P,
+                                    P, P, i64, P, P], i32),
+        "nsvf_prune_exact_dev": ([i64, i32, i32, ctypes.c_double, i64, f32, P, P, P, P, P, P, P,
+                                  i64, P, P, P], i32),
         "nsvf_sample_count_dev": ([i64, P, i32, P, P, P, P, P, P, P], i32),
         "nsvf_sample_compact_dev": ([i64, P, i32, P, P, P, P, P, P, i64, P, P, P, i64, P, P, P,
                                      P, P], i32),
         "nsvf_composite_segments_dev": ([i64, P, P, i64, P, P, P, P, f32, P, f32, P, P, P, i32, P],
                                         i32),
-        "nsvf_field_samples_bf16_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P], i32),
+        "nsvf_field_samples_bf16_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, i64,
+                                         P, P], i32),
         "nsvf_field_samples_fp8": ([i64, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P], i32),
-        "nsvf_field_samples_fp8_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P],
-                                       i32),
+        "nsvf_field_samples_fp8_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, P,
+                                        i64, P, P], i32),
+        "nsvf_flag_outliers": ([i64, P, P, P, i64, f32, P, P, P, i64, P, P], i32),
+        "nsvf_field_exact_dev": ([i64, P, P, P, P, i64, P, P, P, i64, i64, f32, P, P, P, P, P, P,
+                                  P, i64, P, f32, P, P, i64, P, P], i32),
+        "nsvf_field_refine_fp32_dev": ([P, P, i64, i64, P, P, i64, P, P, i64, i64, f32, P, P, P, P,
+                                        P, P, P], i32),
         "nsvf_wait_timeout_selftest": ([ctypes.c_uint64, P, P], i32),
     }
     for name, (args, res) in sig.items():
@@ -95,5 +108,8 @@ def exported_symbols():
         "nsvf_prune_scores_bf16", "nsvf_pinhole_rays", "nsvf_camera_rays", "nsvf_compact_hits",
         "nsvf_gather_probs", "nsvf_sample_count_dev", "nsvf_sample_compact_dev", "nsvf_composite_segments_dev",
         "nsvf_field_samples_bf16_dev", "nsvf_field_samples_fp8", "nsvf_field_samples_fp8_dev",
-        "nsvf_wait_timeout_selftest",
+        "nsvf_wait_timeout_selftest", "nsvf_flag_outliers", "nsvf_field_exact_dev",
+        "nsvf_ray_probs", "nsvf_prune_screen_bf16", "nsvf_prune_exact_dev",
+        "nsvf_field_refine_fp32_dev", "nsvf_parallel_ray_sampling",
+        "nsvf_parallel_sampling_smem_bytes",
     ]

@@ -22,7 +22,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "-I", os.path.join(HERE, "..", "include")]
-EXACT_FP = {"intersect.cu", "sample.cu", "chunk.cu"}
+EXACT_FP = {"intersect.cu", "sample.cu", "chunk.cu", "exact.cu"}
 
 
 def sources():

@@ -192,67 +192,62 @@ inverse_cdf_sampling = InverseCDFRaySampling.apply
 
 
 @torch.no_grad()
-def _parallel_ray_sampling(MARCH_SIZE, pts_idx, min_depth, max_depth, deterministic=False):
-    """Pure-torch uniform sampler kept by the reference as a back-up
-    (fairnr/clib/__init__.py:303-351): uniform steps from the first entry
-    point plus every interval boundary, sorted; midpoints outside a voxel are
-    dropped."""
-    _min_depth = min_depth.min(1)[0]
-    _max_depth = max_depth.masked_fill(max_depth.eq(MAX_DEPTH), 0).max(1)[0]
-    max_ray_length = (_max_depth - _min_depth).max()
-    delta = torch.arange(int(max_ray_length / MARCH_SIZE), device=min_depth.device,
-                         dtype=min_depth.dtype)
-    delta = delta[None, :].expand(min_depth.size(0), delta.size(-1))
-    if deterministic:
-        delta = delta + 0.5
-    else:
-        delta = delta + delta.clone().uniform_().clamp(min=0.01, max=0.99)
-    delta = delta * MARCH_SIZE
-    sampled_depth = min_depth[:, :1] + delta
-    sampled_idx = (sampled_depth[:, :, None] >= min_depth[:, None, :]).sum(-1) - 1
-    sampled_idx = pts_idx.gather(1, sampled_idx)
-    sampled_depth = torch.cat([min_depth, max_depth, sampled_depth], -1)
-    sampled_idx = torch.cat([pts_idx, pts_idx, sampled_idx], -1)
-    sampled_depth, order = sampled_depth.sort(-1)
-    sampled_idx = sampled_idx.gather(1, order)
-    sampled_dists = sampled_depth[:, 1:] - sampled_depth[:, :-1]
-    sampled_depth = .5 * (sampled_depth[:, 1:] + sampled_depth[:, :-1])
-    min_ids = (sampled_depth[:, :, None] >= min_depth[:, None, :]).sum(-1) - 1
-    max_ids = (sampled_depth[:, :, None] >= max_depth[:, None, :]).sum(-1)
-    sampled_depth.masked_fill_(
-        (max_ids.ne(min_ids)) | (sampled_depth > _max_depth[:, None]) | (sampled_dists == 0.0),
-        MAX_DEPTH)
-    sampled_depth, order = sampled_depth.sort(-1)
-    masks = sampled_depth.eq(MAX_DEPTH)
-    n = (~masks).sum(-1).max()
-    sampled_depth = sampled_depth[:, :n]
-    sampled_dists = sampled_dists.gather(1, order).masked_fill_(masks, 0.0)[:, :n]
-    sampled_idx = sampled_idx.gather(1, order).masked_fill_(masks, -1)[:, :n]
-    return sampled_idx, sampled_depth, sampled_dists
-
-
-@torch.no_grad()
 def parallel_ray_sampling(MARCH_SIZE, pts_idx, min_depth, max_depth, deterministic=False):
-    chunk_size = 4096
-    full_size = min_depth.shape[0]
-    if full_size <= chunk_size:
-        return _parallel_ray_sampling(MARCH_SIZE, pts_idx, min_depth, max_depth,
-                                      deterministic=deterministic)
-    outs = list(zip(*[
-        _parallel_ray_sampling(MARCH_SIZE, pts_idx[i:i + chunk_size],
-                               min_depth[i:i + chunk_size], max_depth[i:i + chunk_size],
-                               deterministic=deterministic)
-        for i in range(0, full_size, chunk_size)]))
+    """The reference's back-up uniform sampler (fairnr/clib/__init__.py:
+    303-383) on the GPU: nsvf_parallel_ray_sampling, a warp per ray. Same
+    arguments and outputs (sampled_idx, sampled_depth, sampled_dists)
+    [rays, width] with -1 / MAX_DEPTH / 0 padding.
 
-    def pad(xs, value):
-        if len(xs) == 1:
-            return xs[0]
-        width = max(x.size(1) for x in xs)
-        out = xs[0].new_full((sum(x.size(0) for x in xs), width), value)
+    The reference works on chunks of 4096 rays; each chunk's number of
+    uniform steps is int(longest ray / MARCH_SIZE) over that chunk (its
+    rays' last exit minus first entry), its jitter a [rays, steps] uniform
+    draw clamped to [0.01, 0.99] (0.5 with deterministic), and its output
+    width the largest number of kept segments in the chunk; the chunks are
+    then padded to the widest. All of that is kept, so a seeded call gives the
+    reference's depths and distances. Ties between equal depths are ordered
+    like a stable sort of [exits, entries, steps]: at a face shared by two
+    voxels the segment after it takes the entered voxel's id (the reference's
+    torch.sort leaves that order unspecified)."""
+    chunk_size = 4096
+    R, H = pts_idx.shape
+    dev = pts_idx.device
+    idx = pts_idx.int().contiguous()
+    lo = min_depth.float().contiguous()
+    hi = max_depth.float().contiguous()
+    parts = []
+    for i in range(0, max(R, 1), chunk_size):
+        I, L, U = idx[i:i + chunk_size], lo[i:i + chunk_size], hi[i:i + chunk_size]
+        n = I.shape[0]
+        first = L.min(1)[0]
+        last = U.masked_fill(U.eq(MAX_DEPTH), 0).max(1)[0]
+        K = int((last - first).max() / MARCH_SIZE) if n else 0
+        noise = None
+        if not deterministic:
+            noise = torch.empty(n, K, dtype=torch.float32, device=dev).uniform_() \
+                .clamp(min=0.01, max=0.99).contiguous()
+        W = max(2 * H + K - 1, 0)
+        si = torch.empty(n, W, dtype=torch.int32, device=dev)
+        sd = torch.empty(n, W, dtype=torch.float32, device=dev)
+        ss = torch.empty(n, W, dtype=torch.float32, device=dev)
+        cnt = torch.zeros(n, dtype=torch.int32, device=dev)
+        ext.parallel_ray_sampling_rows(I, L, U, noise, float(MARCH_SIZE), K, si, sd, ss, cnt)
+        w = int(cnt.max()) if n else 0
+        parts.append((si[:, :w], sd[:, :w], ss[:, :w]))
+    if len(parts) == 1:
+        si, sd, ss = parts[0]
+        return si.long() if pts_idx.dtype == torch.int64 else si, sd.type_as(min_depth), \
+            ss.type_as(min_depth)
+    width = max(p[0].shape[1] for p in parts)
+
+    def pad(xs, value, dtype):
+        out = torch.full((R, width), value, dtype=dtype, device=dev)
         st = 0
         for x in xs:
-            out[st:st + x.size(0), :x.size(1)] = x
-            st += x.size(0)
+            out[st:st + x.shape[0], :x.shape[1]] = x
+            st += x.shape[0]
         return out
 
-    return pad(outs[0], -1), pad(outs[1], MAX_DEPTH), pad(outs[2], 0.0)
+    si = pad([p[0] for p in parts], -1, torch.int32)
+    return si.long() if pts_idx.dtype == torch.int64 else si, \
+        pad([p[1] for p in parts], MAX_DEPTH, torch.float32).type_as(min_depth), \
+        pad([p[2] for p in parts], 0.0, torch.float32).type_as(min_depth)

@@ -3,7 +3,8 @@
 //   * pinhole ray generation from camera parameters in device memory;
 //   * order-preserving compaction of the hit rays (count stays on device);
 //   * gather of the hit rays' sorted hit lists with their sampling
-//     distribution (probs, steps: fairnr/models/nsvf.py:65-74).
+//     distribution (probs, steps: fairnr/models/nsvf.py:65-74), and the same
+//     distribution for padded rows (the drop-in path).
 #include "common.cuh"
 
 namespace {
@@ -81,11 +82,56 @@ __global__ void compact_hits_kernel(int64_t n, const uint8_t *__restrict__ hits,
   if (r == n - 1) *n_hit = scan[r];
 }
 
+// The sampling distribution of one ray (fairnr/models/nsvf.py:65-74): d_k =
+// max_k - min_k where slot k is a hit (0 elsewhere), tot = d_0 + d_1 + ... +
+// d_{H-1} added one slot at a time in slot order (FP32, the order of a
+// plain loop), probs_k = d_k / tot, steps = tot / step. One warp per row:
+// lane l holds slots l, l + 32, ...; every lane adds the row's values in slot
+// order from shuffles, so all lanes hold the same total. Rows are coalesced.
+// Both the drop-in path (nsvf_ray_probs) and the served chain
+// (nsvf_gather_probs) use it, so their samples are identical.
+template <int kMaxChunks>
+__device__ __forceinline__ float row_total(const float (&d)[kMaxChunks], int H, int lane) {
+  float tot = 0.0f;
+#pragma unroll
+  for (int c = 0; c < kMaxChunks; ++c) {
+    const int base = 32 * c;
+    if (base >= H) break;
+    const int n = H - base < 32 ? H - base : 32;
+    for (int j = 0; j < n; ++j) tot = __fadd_rn(tot, __shfl_sync(0xffffffffu, d[c], j));
+  }
+  (void)lane;
+  return tot;
+}
+
+constexpr int kProbChunks = 4;  // rows of up to 128 slots
+
+__global__ void __launch_bounds__(kBlock) ray_probs_kernel(
+    int64_t rows, int H, float step, const int32_t *__restrict__ idx,
+    const float *__restrict__ lo, const float *__restrict__ hi, float *__restrict__ probs,
+    float *__restrict__ steps) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (kBlock / 32);
+  for (int64_t r = (blockIdx.x * (int64_t)kBlock + threadIdx.x) >> 5; r < rows; r += warps) {
+    float d[kProbChunks];
+#pragma unroll
+    for (int c = 0; c < kProbChunks; ++c) {
+      const int k = 32 * c + lane;
+      d[c] = 0.0f;
+      if (k < H && idx[r * H + k] != -1) d[c] = __fsub_rn(hi[r * H + k], lo[r * H + k]);
+    }
+    const float tot = row_total(d, H, lane);
+#pragma unroll
+    for (int c = 0; c < kProbChunks; ++c) {
+      const int k = 32 * c + lane;
+      if (k < H) probs[r * H + k] = __fdiv_rn(d[c], tot);
+    }
+    if (lane == 0) steps[r] = __fdiv_rn(tot, step);
+  }
+}
+
 // Warp per row i < *n_hit: copy the hit list of ray pix[i] and build its
-// sampling distribution: d = max - min where the slot is a hit, probs =
-// d / sum(d), steps = sum(d) / step. The lanes take slots k = lane, lane + 32,
-// ... (coalesced rows); the sum adds the lanes' partial sums by an xor
-// butterfly, which leaves the same total in every lane and on every run.
+// sampling distribution with row_total (the drop-in path's sum order).
 __global__ void __launch_bounds__(kBlock) gather_probs_kernel(
     int64_t cap, const int64_t *__restrict__ n_hit, int H, float step,
     const int64_t *__restrict__ pix, const int32_t *__restrict__ idx,
@@ -99,22 +145,27 @@ __global__ void __launch_bounds__(kBlock) gather_probs_kernel(
     const int64_t r = pix[i];
     const int32_t *ir = idx + r * H;
     const float *lr = lo + r * H, *hr = hi + r * H;
-    float part = 0.0f;
-    for (int k = lane; k < H; k += 32) {
-      const int32_t id = ir[k];
-      const float a = lr[k], b = hr[k];
-      I[i * H + k] = id;
-      L[i * H + k] = a;
-      U[i * H + k] = b;
-      part += (id == -1) ? 0.0f : (b - a);
+    float d[kProbChunks];
+#pragma unroll
+    for (int c = 0; c < kProbChunks; ++c) {
+      const int k = 32 * c + lane;
+      d[c] = 0.0f;
+      if (k < H) {
+        const int32_t id = ir[k];
+        const float a = lr[k], b = hr[k];
+        I[i * H + k] = id;
+        L[i * H + k] = a;
+        U[i * H + k] = b;
+        if (id != -1) d[c] = __fsub_rn(b, a);
+      }
     }
-    float tot = part;
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-    for (int k = lane; k < H; k += 32) {
-      const float d = (ir[k] == -1) ? 0.0f : (hr[k] - lr[k]);
-      probs[i * H + k] = d / tot;
+    const float tot = row_total(d, H, lane);
+#pragma unroll
+    for (int c = 0; c < kProbChunks; ++c) {
+      const int k = 32 * c + lane;
+      if (k < H) probs[i * H + k] = __fdiv_rn(d[c], tot);
     }
-    if (lane == 0) steps[i] = tot / step;
+    if (lane == 0) steps[i] = __fdiv_rn(tot, step);
   }
 }
 
@@ -150,11 +201,24 @@ int nsvf_camera_rays(int64_t n, const float *cam, float *ray_start, float *ray_d
   return nsvf_launch_status();
 }
 
+int nsvf_ray_probs(int64_t rows, int max_hits, float step_size, const int32_t *idx,
+                   const float *min_depth, const float *max_depth, float *probs, float *steps,
+                   void *stream) {
+  if (rows < 0 || max_hits < 1 || max_hits > 32 * kProbChunks) return NSVF_ERR_INVALID;
+  if (rows == 0) return NSVF_OK;
+  if (!idx || !min_depth || !max_depth || !probs || !steps) return NSVF_ERR_INVALID;
+  int blocks = nsvf_grid(rows, kBlock / 32);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  ray_probs_kernel<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(rows, max_hits, step_size, idx,
+                                                               min_depth, max_depth, probs, steps);
+  return nsvf_launch_status();
+}
+
 int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
                       const int64_t *pix, const int32_t *idx, const float *min_depth,
                       const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
                       float *probs, float *steps, void *stream) {
-  if (cap < 0 || max_hits < 1 || !n_hit) return NSVF_ERR_INVALID;
+  if (cap < 0 || max_hits < 1 || max_hits > 32 * kProbChunks || !n_hit) return NSVF_ERR_INVALID;
   if (cap == 0) return NSVF_OK;
   if (!pix || !idx || !min_depth || !max_depth || !out_idx || !out_min || !out_max || !probs ||
       !steps)

@@ -95,6 +95,24 @@ __device__ __forceinline__ bool nsvf_slab_fast(float ox, float oy, float oz, flo
   return !(lo > hi);
 }
 
+// A sample lies far outside its voxel when a trilinear coordinate p = (x -
+// c) / voxel_size + 0.5 leaves [-0.5, 1.5] (half a voxel past a face). Its
+// corner weights then extrapolate, and the field there is re-evaluated in
+// compensated arithmetic (exact.cu). NaN coordinates are not flagged.
+__device__ __forceinline__ bool nsvf_far_outside(float qx, float qy, float qz) {
+  return fabsf(__fsub_rn(qx, 0.5f)) > 1.0f || fabsf(__fsub_rn(qy, 0.5f)) > 1.0f ||
+         fabsf(__fsub_rn(qz, 0.5f)) > 1.0f;
+}
+
+// Appends sample s to a device list (count *n_list, capacity list_cap); a
+// full list sets bit 4 (16) of *err.
+__device__ __forceinline__ void nsvf_push_outlier(int64_t *list, unsigned long long *n_list,
+                                                  int64_t list_cap, int64_t s, int32_t *err) {
+  const unsigned long long k = atomicAdd(n_list, 1ull);
+  if ((int64_t)k < list_cap) list[k] = s;
+  else if (err) atomicOr(err, 16);
+}
+
 // Correctly rounded reciprocal (the reference uses the approximate
 // __fdividef(1, d); see the note in include/nsvf_gb300.h).
 __device__ __forceinline__ float nsvf_rcp(float d) { return __frcp_rn(d); }

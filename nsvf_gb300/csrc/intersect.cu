@@ -754,15 +754,18 @@ int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, i
 //
 // For callers that cannot allocate device memory on the call path -- a
 // real-time render loop or a host engine that pre-partitions GPU memory and
-// hands this library only its own input and output buffers, or code that is
-// about to be captured into a CUDA graph -- the packed-octree scratch that
-// nsvf_svo_intersect takes as `workspace` lives here in a file-scope device
-// array instead. Its size is fixed: NSVF_NOALLOC_MAX_NODES nodes (b_pts * n)
-// at 176 bytes each (160 for the packed node, 16 for a point set's root box
-// in the worst case of one node per set), 44 MiB, which every GPU that loads
-// this library holds until the process exits. Host code only sees a stand-in for the array's
-// name, never its device address, so the address is looked up once per
-// device with cudaGetSymbolAddress (with that device current) and cached.
+// hands this library only its own input and output buffers -- the
+// packed-octree scratch that nsvf_svo_intersect takes as `workspace` lives
+// here in a file-scope device array instead. Its size is fixed:
+// NSVF_NOALLOC_MAX_NODES nodes (b_pts * n) at 176 bytes each (160 for the
+// packed node, 16 for a point set's root box in the worst case of one node
+// per set), 44 MiB, which every GPU that loads this library holds until the
+// process exits. Host code only sees a stand-in for the array's name, never
+// its device address, so the address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) and cached. The cache
+// does not survive a device reset: after cudaDeviceReset (or a released and
+// re-created primary context) the module may load at another address, and a
+// process that resets a device must not call this entry point on it again.
 static __device__ __align__(256) unsigned char g_svo_noalloc_scratch[(size_t)NSVF_NOALLOC_MAX_NODES * 176];
 
 static void *noalloc_scratch_for_current_device(int *status) {

@@ -126,6 +126,16 @@ struct MlpParams {
   float step;                        // kPrune: rule 1 step
   int rule;                          // kPrune: 0 = min exp(-relu s), 1 = max 1-exp(-relu(s) step)
   unsigned int *score;               // kPrune: [n_vox] float bits
+  // kPrune screen of the exact pruning pass (keep != NULL): with M = sum_j
+  // |W4[0][j]| h_j (an extra head column), a point with sigma - c M above
+  // the threshold T (>= for rule 1, > for rule 0) keeps its voxel
+  // (keep[v] = 1); a point with sigma + c M >= T is undecided and its row is
+  // appended to plist for the double-float pass (exact.cu)
+  uint8_t *keep;
+  float prune_T, prune_c;
+  int64_t *plist;
+  unsigned long long *n_plist;
+  int64_t plist_cap;
   const __nv_bfloat16 *w[5];         // row-major [N, K]: 128x32, 3x 128x128, 4x128
   const float *b[5];                 // [128] x4, [4]
   // FP8 variant: the hidden layers 1-3 as E4M3 bytes (row-major [128, 128],
@@ -142,6 +152,11 @@ struct MlpParams {
   int64_t ns;                        // rows (the capacity when ns_dev is set)
   const int64_t *ns_dev;             // optional: row count read on the device
   int32_t *err;
+  // kSamplesIn, optional: samples far outside their voxel are appended to
+  // outl (count *n_outl, capacity outl_cap) for the compensated pass
+  int64_t *outl;
+  unsigned long long *n_outl;
+  int64_t outl_cap;
 };
 
 // The trilinear weights of the interpolation kernel (interp.cu), same
@@ -316,10 +331,12 @@ __device__ __forceinline__ void row_meta(const MlpParams &p, int64_t r, int64_t 
       v = r / P;
       int64_t i = r % P;
       int ix = (int)(i / (p.bits * p.bits)), iy = (int)((i / p.bits) % p.bits), iz = (int)(i % p.bits);
+      // offset_points' FP32 operations: fl(fl(o / (bits - 1)) * hv), then
+      // added to the centre (separate roundings, no contraction)
       float hv = p.voxel_size / 2.0f, den = (float)(p.bits - 1);
-      x = vd.cx + ((float)(2 * ix + 1 - p.bits) / den) * hv;
-      y = vd.cy + ((float)(2 * iy + 1 - p.bits) / den) * hv;
-      z = vd.cz + ((float)(2 * iz + 1 - p.bits) / den) * hv;
+      x = __fadd_rn(vd.cx, __fmul_rn(__fdiv_rn((float)(2 * ix + 1 - p.bits), den), hv));
+      y = __fadd_rn(vd.cy, __fmul_rn(__fdiv_rn((float)(2 * iy + 1 - p.bits), den), hv));
+      z = __fadd_rn(vd.cz, __fmul_rn(__fdiv_rn((float)(2 * iz + 1 - p.bits), den), hv));
     }
     if (v < 0 || v >= p.n_vox) {
       bad = true;
@@ -327,6 +344,8 @@ __device__ __forceinline__ void row_meta(const MlpParams &p, int64_t r, int64_t 
       vv = (int)v;
       float q[3] = {(x - vd.cx) / p.voxel_size + 0.5f, (y - vd.cy) / p.voxel_size + 0.5f,
                     (z - vd.cz) / p.voxel_size + 0.5f};
+      if (MODE == kSamplesIn && p.n_outl && nsvf_far_outside(q[0], q[1], q[2]))
+        nsvf_push_outlier(p.outl, p.n_outl, p.outl_cap, r, p.err);
       const int keys[8] = {vd.f0.x, vd.f0.y, vd.f0.z, vd.f0.w, vd.f1.x, vd.f1.y, vd.f1.z, vd.f1.w};
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
@@ -465,6 +484,27 @@ __device__ __forceinline__ void head_store(const MlpParams &p, const float *bias
     uint32_t val;
     if (p.rule == 0) val = __float_as_uint(expf(-fmaxf(sigma, 0.0f)));
     else val = __float_as_uint(fmaxf(1.0f - expf(-(fmaxf(sigma, 0.0f) * p.step)), 0.0f));
+    if (p.keep) {
+      // exact-pass screen (whole warp): certain keeps, and undecided rows
+      // appended to plist with one atomic per warp
+      const float M = v[4];
+      const float lo = sigma - p.prune_c * M, hi = sigma + p.prune_c * M;
+      const bool certain = live && (p.rule == 1 ? lo >= p.prune_T : lo > p.prune_T);
+      const bool maybe = live && !certain && hi >= p.prune_T;
+      if (certain) p.keep[vv] = 1;
+      const unsigned m = __ballot_sync(0xffffffffu, maybe);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(p.n_plist, (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (maybe) {
+          const unsigned long long k = base + __popc(m & ((1u << lane) - 1u));
+          if ((int64_t)k < p.plist_cap) p.plist[k] = r;
+          else if (p.err) atomicOr(p.err, 16);
+        }
+      }
+    }
     int64_t v0 = __shfl_sync(0xffffffffu, vv, 0);
     if (__all_sync(0xffffffffu, vv == v0 && live)) {
 #pragma unroll
@@ -510,6 +550,19 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     else stage_weights(reinterpret_cast<__nv_bfloat16 *>(S.wh[l]), p.w[l + 1], HID, HID, HID);
   }
   stage_weights(S.w4, p.w[4], NOUT, 4, HID);
+  if (MODE == kPrune && p.keep) {
+    // head row 4 = |W4[0]|: column 4 of the head output is M = sum_j
+    // |W4[0][j]| h_j, the scale of sigma's BF16 rounding error
+    // (each chunk written by the thread stage_weights gave it, after its
+    // zero fill, so no barrier is needed in between)
+    for (int c = threadIdx.x; c < NOUT * (HID / 8); c += blockDim.x) {
+      if (c / (HID / 8) != 4) continue;
+      const int kc = c % (HID / 8);
+      uint4 v = *reinterpret_cast<const uint4 *>(p.w[4] + kc * 8);
+      v.x &= 0x7fff7fffu; v.y &= 0x7fff7fffu; v.z &= 0x7fff7fffu; v.w &= 0x7fff7fffu;
+      *reinterpret_cast<uint4 *>(reinterpret_cast<uint8_t *>(S.w4) + kmajor_off(4, kc * 8, HID)) = v;
+    }
+  }
   stage_bias_step(S.bias_b, S.ones_a, p.b, F8 ? p.dq : nullptr, tid, blockDim.x);
   for (int i = tid; i < 4 * HID; i += blockDim.x) S.bias[i / HID][i % HID] = p.b[i / HID][i % HID];
   if (tid < NOUT) S.bias4[tid] = tid < 4 ? p.b[4][tid] : 0.0f;
@@ -905,8 +958,10 @@ int nsvf_field_samples_bf16_dev(int64_t capacity, const int64_t *n_samples_dev,
                                 int64_t n_keys, float voxel_size, const float *centers,
                                 const int32_t *feats, const float *values,
                                 const void *const weights[5], const float *const biases[5],
-                                float *out, int32_t *err, void *stream) {
+                                float *out, int64_t *outliers, int64_t *n_outliers,
+                                int64_t outlier_cap, int32_t *err, void *stream) {
   if (capacity < 0 || !n_samples_dev || n_voxels < 1 || n_keys < 1) return NSVF_ERR_INVALID;
+  if (n_outliers && (outlier_cap < 0 || (outlier_cap > 0 && !outliers))) return NSVF_ERR_INVALID;
   if (capacity == 0) return NSVF_OK;
   MlpParams p = {};
   if (!voxel || !xyz_dist || !centers || !feats || !values || !out ||
@@ -926,6 +981,9 @@ int nsvf_field_samples_bf16_dev(int64_t capacity, const int64_t *n_samples_dev,
   p.ns = capacity;
   p.ns_dev = n_samples_dev;
   p.err = err;
+  p.outl = outliers;
+  p.n_outl = (unsigned long long *)n_outliers;
+  p.outl_cap = outlier_cap;
   return launch_mlp_grid<kSamplesIn>(p, (cudaStream_t)stream, -1);
 }
 
@@ -956,13 +1014,52 @@ int nsvf_prune_scores_bf16(int64_t n_voxels, int bits, int rule, float step, int
   return launch_mlp<kPrune>(p, (cudaStream_t)stream);
 }
 
+int nsvf_prune_screen_bf16(int64_t n_voxels, int bits, int rule, float step, float threshold,
+                           float band, int64_t n_keys, float voxel_size, const float *centers,
+                           const int32_t *feats, const float *values,
+                           const void *const weights[5], const float *const biases[5],
+                           uint32_t *score, uint8_t *keep, int64_t *list, int64_t *n_list,
+                           int64_t list_cap, int32_t *err, void *stream) {
+  if (n_voxels < 0 || bits < 2 || bits > 64 || (rule != 0 && rule != 1) || n_keys < 1 ||
+      list_cap < 0 || !(threshold > 0.0f) || !(band >= 0.0f) || !(threshold < 3.0e38f))
+    return NSVF_ERR_INVALID;
+  if (n_voxels == 0) return NSVF_OK;
+  MlpParams p = {};
+  if (!centers || !feats || !values || !score || !keep || !n_list || (list_cap > 0 && !list) ||
+      !set_weights(p, weights, biases))
+    return NSVF_ERR_INVALID;
+  if ((((uintptr_t)values) | ((uintptr_t)feats)) & 15) return NSVF_ERR_INVALID;
+  p.centers = centers;
+  p.feats = feats;
+  p.values = (const float4 *)values;
+  p.n_vox = n_voxels;
+  p.n_keys = n_keys;
+  p.voxel_size = voxel_size;
+  p.bits = bits;
+  p.rule = rule;
+  p.step = step;
+  p.score = score;
+  p.keep = keep;
+  p.prune_T = threshold;
+  p.prune_c = band;
+  p.plist = list;
+  p.n_plist = (unsigned long long *)n_list;
+  p.plist_cap = list_cap;
+  p.ns = n_voxels * (int64_t)bits * bits * bits;
+  p.err = err;
+  return launch_mlp<kPrune>(p, (cudaStream_t)stream);
+}
+
 int nsvf_field_samples_fp8_dev(int64_t capacity, const int64_t *n_samples_dev,
                                const int32_t *voxel, const float *xyz_dist, int64_t n_voxels,
                                int64_t n_keys, float voxel_size, const float *centers,
                                const int32_t *feats, const float *values,
                                const void *const weights[5], const float *const biases[5],
-                               const float scales[6], float *out, int32_t *err, void *stream) {
+                               const float scales[6], float *out, int64_t *outliers,
+                               int64_t *n_outliers, int64_t outlier_cap, int32_t *err,
+                               void *stream) {
   if (capacity < 0 || !n_samples_dev || n_voxels < 1 || n_keys < 1) return NSVF_ERR_INVALID;
+  if (n_outliers && (outlier_cap < 0 || (outlier_cap > 0 && !outliers))) return NSVF_ERR_INVALID;
   if (capacity == 0) return NSVF_OK;
   MlpParams p = {};
   if (!voxel || !xyz_dist || !centers || !feats || !values || !out ||
@@ -982,6 +1079,9 @@ int nsvf_field_samples_fp8_dev(int64_t capacity, const int64_t *n_samples_dev,
   p.ns = capacity;
   p.ns_dev = n_samples_dev;
   p.err = err;
+  p.outl = outliers;
+  p.n_outl = (unsigned long long *)n_outliers;
+  p.outl_cap = outlier_cap;
   return launch_mlp_grid<kSamplesIn, true>(p, (cudaStream_t)stream, -1);
 }
 

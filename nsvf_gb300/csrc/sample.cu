@@ -593,9 +593,183 @@ __global__ void __launch_bounds__(kBlock) uniform_kernel(
   if (overflow && err) atomicOr(err, 2);
 }
 
+// Parallel uniform sampler: the pure-torch backup sampler of the reference's
+// op set (fairnr/clib/__init__.py:303-349, `_parallel_ray_sampling`), here a
+// warp per ray with its lists in shared memory. Per ray, with the H sorted
+// hit slots (pts_idx, min m_i, max M_i; misses carry MAX_DEPTH):
+//   u_k = m_0 + (k + j_k) * march for k < K (j_k = 0.5, or the clamped
+//       jitter), taking the id of slot #{i : m_i <= u_k} - 1;
+//   the 2H + K depths {M_i} u {m_i} u {u_k}, each with its id, sorted with
+//       ties in that concatenation order (a stable sort): at a face shared
+//       by two voxels the exit comes first, so the segment after it takes
+//       the id of the voxel being entered (the reference's torch.sort leaves
+//       that order unspecified; on the CPU it orders such ties both ways);
+//   segment s between consecutive depths d_s, d_s+1: midpoint .5 (d_s +
+//       d_s+1), length d_s+1 - d_s, the id of d_s; kept when #{i : m_i <=
+//       mid} - 1 == #{i : M_i <= mid}, mid <= max_i M_i (MAX_DEPTH read as
+//       0) and the length is not 0.
+// The kept segments are written in order (count[r] of them), then -1 /
+// MAX_DEPTH / 0 up to out_w. The sort is done as ranks: each boundary's rank
+// among the 2H boundaries counts smaller values and equal values earlier in
+// the concatenation; a boundary's merged position adds the steps strictly
+// below it, a step's adds the boundaries at or below it (both lists are
+// sorted, so binary searches). Shared memory per warp: 4 * (8H + 2N) bytes,
+// N = 2H + K (raw boundaries and ids, sorted boundaries and ids, the merged
+// depths and ids).
+constexpr int kParWarps = 4;
+
+__device__ __forceinline__ float par_step(int k, const float *__restrict__ J, float m0,
+                                          float march) {
+  const float j = J ? J[k] : 0.5f;
+  return __fadd_rn(m0, __fmul_rn(__fadd_rn((float)k, j), march));
+}
+
+__global__ void __launch_bounds__(32 * kParWarps) parallel_sampling_kernel(
+    int64_t rows, int H, int K, float march, const int32_t *__restrict__ pts_idx,
+    const float *__restrict__ min_depth, const float *__restrict__ max_depth,
+    const float *__restrict__ noise, int out_w, int32_t *__restrict__ s_idx,
+    float *__restrict__ s_depth, float *__restrict__ s_dist, int32_t *__restrict__ count) {
+  extern __shared__ float par_smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int N = 2 * H + K;
+  float *bv = par_smem + (size_t)w * (8 * H + 2 * N);
+  int32_t *bi = reinterpret_cast<int32_t *>(bv + 2 * H);
+  float *sv = bv + 4 * H;
+  int32_t *si = reinterpret_cast<int32_t *>(bv + 6 * H);
+  float *mval = bv + 8 * H;
+  int32_t *midx = reinterpret_cast<int32_t *>(bv + 8 * H + N);
+  const int64_t warps = (int64_t)gridDim.x * kParWarps;
+  for (int64_t r = blockIdx.x * (int64_t)kParWarps + w; r < rows; r += warps) {
+    const int32_t *I = pts_idx + r * H;
+    const float *lo = min_depth + r * H, *hi = max_depth + r * H;
+    const float *J = noise ? noise + r * K : nullptr;
+    // bv = [exits M_0..M_H-1, entries m_0..m_H-1]
+    const float *mins = bv + H, *maxs = bv;
+    float mx = 0.0f;
+    for (int i = lane; i < H; i += 32) {
+      const float a = lo[i], b = hi[i];
+      bv[i] = b;
+      bv[H + i] = a;
+      bi[i] = bi[H + i] = I[i];
+      const float bb = b == NSVF_MAX_DEPTH_F ? 0.0f : b;
+      mx = fmaxf(mx, bb);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __syncwarp();
+    const float m0 = mins[0];
+    // stable ranks of the 2H boundaries
+    for (int e = lane; e < 2 * H; e += 32) {
+      const float v = bv[e];
+      int rank = 0;
+      for (int f = 0; f < 2 * H; ++f) {
+        const float u = bv[f];
+        rank += (u < v || (u == v && f < e)) ? 1 : 0;
+      }
+      sv[rank] = v;
+      si[rank] = bi[e];
+    }
+    __syncwarp();
+    // the steps: merged position k + #{boundaries <= u}, id from the slot count
+    for (int k = lane; k < K; k += 32) {
+      const float u = par_step(k, J, m0, march);
+      int a = 0, b = 2 * H;       // first boundary > u
+      while (a < b) {
+        const int m = (a + b) >> 1;
+        if (sv[m] <= u) a = m + 1;
+        else b = m;
+      }
+      int c = 0;
+      for (int i = 0; i < H; ++i) c += (u >= mins[i]) ? 1 : 0;
+      mval[k + a] = u;
+      midx[k + a] = c >= 1 ? bi[H + c - 1] : -1;
+    }
+    // the boundaries: merged position q + #{steps < v}
+    for (int q = lane; q < 2 * H; q += 32) {
+      const float v = sv[q];
+      int a = 0, b = K;           // first step >= v
+      while (a < b) {
+        const int m = (a + b) >> 1;
+        if (par_step(m, J, m0, march) < v) a = m + 1;
+        else b = m;
+      }
+      mval[q + a] = v;
+      midx[q + a] = si[q];
+    }
+    __syncwarp();
+    // segments, kept ones compacted in order
+    int cnt = 0;
+    for (int base = 0; base < N - 1; base += 32) {
+      const int sgm = base + lane;
+      bool keep = false;
+      float mid = 0.0f, len = 0.0f;
+      int32_t id = -1;
+      if (sgm < N - 1) {
+        const float a = mval[sgm], b = mval[sgm + 1];
+        mid = __fmul_rn(0.5f, __fadd_rn(a, b));
+        len = __fsub_rn(b, a);
+        id = midx[sgm];
+        int cmin = 0, cmax = 0;
+        for (int i = 0; i < H; ++i) {
+          cmin += (mid >= mins[i]) ? 1 : 0;
+          cmax += (mid >= maxs[i]) ? 1 : 0;
+        }
+        keep = (cmin - 1 == cmax) && !(mid > mx) && !(len == 0.0f);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+      if (keep && pos < out_w) {
+        s_idx[r * out_w + pos] = id;
+        s_depth[r * out_w + pos] = mid;
+        s_dist[r * out_w + pos] = len;
+      }
+      cnt += __popc(m);
+    }
+    for (int q = cnt + lane; q < out_w; q += 32) {
+      s_idx[r * out_w + q] = -1;
+      s_depth[r * out_w + q] = NSVF_MAX_DEPTH_F;
+      s_dist[r * out_w + q] = 0.0f;
+    }
+    if (lane == 0 && count) count[r] = cnt;
+    __syncwarp();
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int64_t nsvf_parallel_sampling_smem_bytes(int max_hits, int n_steps) {
+  if (max_hits < 1 || n_steps < 0) return -1;
+  const int64_t N = 2 * (int64_t)max_hits + n_steps;
+  return 4 * (8 * (int64_t)max_hits + 2 * N);
+}
+
+int nsvf_parallel_ray_sampling(int64_t rows, int max_hits, int n_steps, float march_size,
+                               const int32_t *pts_idx, const float *min_depth,
+                               const float *max_depth, const float *noise, int out_width,
+                               int32_t *sampled_idx, float *sampled_depth, float *sampled_dists,
+                               int32_t *count, void *stream) {
+  if (rows < 0 || max_hits < 1 || n_steps < 0 || out_width < 0) return NSVF_ERR_INVALID;
+  if (rows == 0) return NSVF_OK;
+  if (!pts_idx || !min_depth || !max_depth || (out_width > 0 && (!sampled_idx || !sampled_depth ||
+      !sampled_dists)))
+    return NSVF_ERR_INVALID;
+  // all kParWarps warps' lists in one block's shared memory (<= 224 KB)
+  const int64_t per_warp = nsvf_parallel_sampling_smem_bytes(max_hits, n_steps);
+  const int64_t smem = per_warp * kParWarps;
+  if (smem > 224 * 1024) return NSVF_ERR_CAPACITY;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(parallel_sampling_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return NSVF_ERR_CUDA;
+  int64_t blocks = (rows + kParWarps - 1) / kParWarps;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  parallel_sampling_kernel<<<(int)blocks, 32 * kParWarps, (size_t)smem, (cudaStream_t)stream>>>(
+      rows, max_hits, n_steps, march_size, pts_idx, min_depth, max_depth, noise, out_width,
+      sampled_idx, sampled_depth, sampled_dists, count);
+  return nsvf_launch_status();
+}
+
 
 int nsvf_inverse_cdf_sampling(int64_t rows, int max_hits, int max_steps, int noise_stride,
                               float fixed_step_size, const int32_t *pts_idx,

@@ -267,10 +267,17 @@ class SparseVoxelEncoder(nn.Module):
 
     # ---------------------------------------------------------- pruning --
     @torch.no_grad()
-    def pruning(self, field_fn, th=0.5, encoder_states=None, train_stats=False):
+    def pruning(self, field_fn, th=0.5, encoder_states=None, train_stats=False, bits=16,
+                use_step=False):
+        """The reference's pruning (fairnr/modules/encoder.py:605-618) with the
+        field in FP32: keep = 1 - min exp(-relu sigma) > th over bits^3 points
+        per voxel (bits 16 as the reference). use_step selects the sigma * step
+        rule: keep = max 1 - exp(-relu(sigma) * step) >= th (the c2 workload
+        uses it with bits 8)."""
         if not train_stats:
-            scores = self.get_scores(field_fn, th=th, bits=16, encoder_states=encoder_states)
-            keep = (1 - scores.min(-1)[0]) > th
+            scores = self.get_scores(field_fn, th=th, bits=bits, encoder_states=encoder_states,
+                                     use_step=use_step)
+            keep = scores.max(-1)[0] >= th if use_step else (1 - scores.min(-1)[0]) > th
         else:
             if dist.is_initialized() and dist.get_world_size() > 1:
                 dist.all_reduce(self.max_voxel_probs, op=dist.ReduceOp.MAX)
@@ -278,9 +285,11 @@ class SparseVoxelEncoder(nn.Module):
         self.keep.masked_scatter_(self.keep.bool(), keep.long())
         logger.info("pruning done. # of voxels before: %d, after: %d", keep.size(0), int(keep.sum()))
 
-    def get_scores(self, field_fn, th=0.5, bits=16, encoder_states=None, chunk_size=64):
+    def get_scores(self, field_fn, th=0.5, bits=16, encoder_states=None, chunk_size=64,
+                   use_step=False):
         """exp(-relu(sigma)) at bits^3 points per voxel: [V, bits^3]
-        (fairnr/modules/encoder.py:620-654)."""
+        (fairnr/modules/encoder.py:620-654); with use_step the alphas
+        1 - exp(-relu(sigma) * step) instead."""
         if encoder_states is None:
             encoder_states = self.precompute(id=None)
         feats = encoder_states['voxel_vertex_idx']
@@ -299,10 +308,32 @@ class SparseVoxelEncoder(nn.Module):
             if encoder_states.get('context', None) is not None:
                 inputs['context'] = encoder_states['context']
             out = field_fn(inputs, outputs=['sigma'])
+            if use_step:
+                return 1 - torch.exp(-torch.relu(out['sigma']).reshape(-1, bits ** 3) * self.step_size)
             return torch.exp(-torch.relu(out['sigma']).reshape(-1, bits ** 3))
 
         return torch.cat([once(feats[i:i + chunk_size], points[i:i + chunk_size])
                           for i in range(0, points.size(0), chunk_size)], 0)
+
+    @torch.no_grad()
+    def pruning_exact(self, mlp, th=0.5, bits=16, use_step=False, apply=True):
+        """pruning() on the GPU with the mask decided exactly: the tensor-core
+        BF16 pass screens every point and the points it cannot decide are
+        evaluated in double-float (TensorCoreMLP.prune_mask). The mask is the
+        reference rule's without rounding error. Returns the keep mask over
+        the currently kept voxels (applied to `keep` unless apply=False)."""
+        states = self.precompute(id=None)
+        centers = states['voxel_center_xyz'].float().contiguous()
+        feats = states['voxel_vertex_idx'].int().contiguous()
+        values = states['voxel_vertex_emb'].detach().float().contiguous()
+        keep, _, n = mlp.prune_mask(centers, feats, values, float(self.voxel_size), th=th,
+                                    bits=bits, rule=1 if use_step else 0,
+                                    step=float(self.step_size))
+        self.last_prune_undecided_points = n
+        if apply:
+            self.keep.masked_scatter_(self.keep.bool(), keep.long())
+            self.clean_runtime_caches()
+        return keep
 
     @torch.no_grad()
     def pruning_fused(self, mlp, th=0.5, bits=8, rule=1, apply=True):

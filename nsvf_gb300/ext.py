@@ -90,6 +90,8 @@ def check_errors(device=None):
             what.append("a voxel or corner id out of range in trilinear interpolation")
         if v & 8:
             what.append("a tensor-core pipeline wait timed out")
+        if v & 16:
+            what.append("more samples far outside their voxel than the outlier list holds")
         raise RuntimeError("nsvf_gb300: " + "; ".join(what))
 
 
@@ -286,6 +288,45 @@ def inverse_cdf_sampling(pts_idx, min_depth, max_depth, uniform_noise, probs, st
         uniform_noise.view(rows, S), probs.view(rows, H), steps.view(rows), fixed_step_size,
         (max(M, 1), max(M, 1), rows, max(B, 1)), S)
     return si.view(B, M, S), sd.view(B, M, S), ss.view(B, M, S)
+
+
+def parallel_ray_sampling_rows(pts_idx, min_depth, max_depth, noise, march_size, n_steps,
+                               sampled_idx, sampled_depth, sampled_dists, count):
+    """nsvf_parallel_ray_sampling over [rows, H] hit lists with n_steps
+    uniform steps per ray (noise [rows, n_steps] or None for 0.5), into
+    [rows, W] outputs and the kept counts [rows] (int32)."""
+    rows, H = pts_idx.shape
+    W = sampled_idx.shape[1] if sampled_idx.dim() == 2 else 0
+    dev = pts_idx.device
+    with _timed("parallel_ray_sampling", dev):
+        check(LIB.nsvf_parallel_ray_sampling(rows, H, int(n_steps), float(march_size),
+                                             _ptr(pts_idx), _ptr(min_depth), _ptr(max_depth),
+                                             _ptr(noise), W, _ptr(sampled_idx),
+                                             _ptr(sampled_depth), _ptr(sampled_dists),
+                                             _ptr(count), ctypes_stream(dev)),
+              "parallel_ray_sampling")
+
+
+def ray_probs(pts_idx, min_depth, max_depth, step_size):
+    """The sampling distribution of NSVFModel.intersecting
+    (fairnr/models/nsvf.py:65-74) on the GPU: [..., H] sorted hit lists ->
+    (probs [..., H], steps [...]). Each ray's segment lengths are summed in
+    slot order (nsvf_ray_probs); the served chain uses the same order."""
+    H = pts_idx.size(-1)
+    idx = pts_idx.reshape(-1, H)
+    if idx.dtype != torch.int32:
+        idx = idx.int()
+    idx = idx.contiguous()
+    lo = min_depth.reshape(-1, H).float().contiguous()
+    hi = max_depth.reshape(-1, H).float().contiguous()
+    rows = idx.shape[0]
+    dev = idx.device
+    probs = torch.empty(rows, H, dtype=torch.float32, device=dev)
+    steps = torch.empty(rows, dtype=torch.float32, device=dev)
+    with _timed("ray_probs", dev):
+        check(LIB.nsvf_ray_probs(rows, H, float(step_size), _ptr(idx), _ptr(lo), _ptr(hi),
+                                 _ptr(probs), _ptr(steps), ctypes_stream(dev)), "ray_probs")
+    return probs.view(pts_idx.shape), steps.view(pts_idx.shape[:-1])
 
 
 def build_octree(center, points, depth):

@@ -4,11 +4,15 @@ TensorCoreMLP(field) snapshots the field's weights as bf16 (row-major
 [out, in]) and biases as FP32 on the field's device; calling it on an FP32
 embedding [N, 32] returns [N, 4] = (sigma, r, g, b) in FP32.
 
+It also keeps the FP32 weights transposed for nsvf_field_exact_dev, the
+double-float re-evaluation of samples far outside their voxel.
+
 enable_fp8(calibration_emb) adds the FP8 option of the fused sample kernel
 (nsvf_field_samples_fp8): the three 128x128 hidden layers in E4M3 with
 per-layer scales, the input layer and the (sigma, rgb) head in BF16.
 """
 import ctypes
+import math
 
 import torch
 
@@ -26,10 +30,39 @@ class TensorCoreMLP:
         self.device = self.w[0].device
         self._wp = (ctypes.c_void_p * 5)(*[t.data_ptr() for t in self.w])
         self._bp = (ctypes.c_void_p * 5)(*[t.data_ptr() for t in self.b])
+        # biases of the BF16 kernels: the field's, until calibrate_bias
+        # corrects them for the BF16 rounding of the weights
+        self.b_tc = [t.clone() for t in self.b]
+        self._bp_tc = (ctypes.c_void_p * 5)(*[t.data_ptr() for t in self.b_tc])
         self.w32 = [lin.weight.detach().float().contiguous() for lin in field.layers]
+        # transposed FP32 copies ([in, out]) for the compensated pass over
+        # samples far outside their voxel (nsvf_field_exact_dev)
+        self.wt32 = [w.t().contiguous() for w in self.w32]
+        self._wtp = (ctypes.c_void_p * 5)(*[t.data_ptr() for t in self.wt32])
         self.fp8 = None
 
     E4M3_MAX = 448.0
+
+    @torch.no_grad()
+    def calibrate_bias(self, calibration_emb):
+        """Bias correction for the BF16 kernels: rounding the weights to bf16
+        shifts each layer's output by (bf16(W) - W) x, an error that is the
+        same for neighbouring samples and so adds up along a ray. Layer by
+        layer, through the BF16 network on `calibration_emb` [N, 32] (FP32
+        embeddings of points inside the scene's voxels), the mean of that
+        shift over the calibration inputs is subtracted from the layer's bias
+        (in float64, stored in FP32). The FP32 and double-float passes keep the
+        field's own biases."""
+        x = calibration_emb.float().to(torch.bfloat16).float()
+        for l in range(5):
+            W32 = self.w32[l].double()
+            dW = self.w[l].double() - W32
+            shift = dW @ x.double().mean(0)
+            self.b_tc[l].copy_((self.b[l].double() - shift).float())
+            x = x @ self.w[l].float().t() + self.b_tc[l]
+            if l < 4:
+                x = torch.relu(x).to(torch.bfloat16).float()
+        return self
 
     def enable_fp8(self, calibration_emb):
         """Per-layer scales for E4M3 hidden layers. Weights: w_scale[l] =
@@ -58,7 +91,7 @@ class TensorCoreMLP:
         if out is None:
             out = torch.empty(n, 4, dtype=torch.float32, device=emb.device)
         with ext._timed("mlp_forward_bf16", emb.device):
-            check(LIB.nsvf_mlp_forward_bf16(n, emb.data_ptr(), self._wp, self._bp, out.data_ptr(),
+            check(LIB.nsvf_mlp_forward_bf16(n, emb.data_ptr(), self._wp, self._bp_tc, out.data_ptr(),
                                             ext.error_word(emb.device).data_ptr(),
                                             ext.ctypes_stream(emb.device)), "mlp_forward_bf16")
         return out
@@ -75,7 +108,7 @@ class TensorCoreMLP:
             check(LIB.nsvf_field_samples_bf16(
                 n, voxel.data_ptr(), xyz_dist.data_ptr(), centers.size(0), values.size(0),
                 float(voxel_size), centers.data_ptr(), feats.data_ptr(), values.data_ptr(),
-                self._wp, self._bp, out.data_ptr(), ext.error_word(dev).data_ptr(),
+                self._wp, self._bp_tc, out.data_ptr(), ext.error_word(dev).data_ptr(),
                 ext.ctypes_stream(dev)), "field_samples_bf16")
         return out
 
@@ -110,10 +143,63 @@ class TensorCoreMLP:
                 "prune_scores_bf16")
         return score.view(torch.float32)
 
+    # Screen band of the exact pruning pass, in units of M = sum_j |W4[0][j]| h_j:
+    # the BF16 error of sigma measured on the workloads' fields stays below
+    # 0.005 M (c2 pruning field, 768k points), so 0.02 leaves a factor 4.
+    PRUNE_BAND = 0.02
+
+    def prune_mask(self, centers, feats, values, voxel_size, th=0.5, bits=8, rule=1, step=0.0,
+                   band=PRUNE_BAND):
+        """Exact pruning mask [V] (bool) for 0 < th < 1: rule 0 (the
+        reference's, fairnr/modules/encoder.py:609-610) keeps voxels with
+        1 - min exp(-relu sigma) > th, rule 1 those with max 1 - exp(-relu(sigma)
+        step) >= th, sigma at bits^3 offset_points positions per voxel. The
+        tensor-core pass screens every point in BF16 and decides all but the
+        points within `band` M of the threshold, which are evaluated in
+        double-float (nsvf_prune_screen_bf16, nsvf_prune_exact_dev). Also
+        returns the BF16 scores (as prune_scores) and the number of points the
+        double-float pass had to examine."""
+        if not 0.0 < th < 1.0:
+            raise ValueError("pruning threshold must lie in (0, 1), got %r" % (th,))
+        if rule == 1 and not step > 0.0:
+            raise ValueError("rule 1 needs a positive step")
+        T = -math.log1p(-th) / (step if rule == 1 else 1.0)
+        V = centers.size(0)
+        dev = centers.device
+        init = 0x7F800000 if rule == 0 else 0
+        score = torch.empty(V, dtype=torch.int32, device=dev)
+        keep = torch.empty(V, dtype=torch.uint8, device=dev)
+        n_list = torch.empty(1, dtype=torch.int64, device=dev)
+        err = ext.error_word(dev)
+        cap = max(65536, V * bits ** 3 // 128)
+        for _ in range(3):
+            lst = torch.empty(cap, dtype=torch.int64, device=dev)
+            score.fill_(init)
+            keep.zero_()
+            n_list.zero_()
+            with ext._timed("prune_screen_bf16", dev):
+                check(LIB.nsvf_prune_screen_bf16(
+                    V, int(bits), int(rule), float(step), float(T), float(band), values.size(0),
+                    float(voxel_size), centers.data_ptr(), feats.data_ptr(), values.data_ptr(),
+                    self._wp, self._bp, score.data_ptr(), keep.data_ptr(), lst.data_ptr(),
+                    n_list.data_ptr(), cap, None, ext.ctypes_stream(dev)), "prune_screen_bf16")
+            n = int(n_list.item())
+            if n <= cap:
+                break
+            cap = n + n // 4
+        with ext._timed("prune_exact", dev):
+            check(LIB.nsvf_prune_exact_dev(
+                V, int(bits), int(rule), float(T), values.size(0), float(voxel_size),
+                centers.data_ptr(), feats.data_ptr(), values.data_ptr(), self._wtp, self._bp,
+                lst.data_ptr(), n_list.data_ptr(), cap, keep.data_ptr(), err.data_ptr(),
+                ext.ctypes_stream(dev)), "prune_exact_dev")
+        return keep.bool(), score.view(torch.float32), n
+
     def reference_bf16(self, emb):
-        """torch emulation of the kernel's rounding: bf16 operands, FP32 sums."""
+        """torch emulation of the kernel's rounding: bf16 operands, FP32 sums
+        (with the BF16 kernels' biases, b_tc)."""
         x = emb.float().to(torch.bfloat16).float()
-        for i, (W, b) in enumerate(zip(self.w, self.b)):
+        for i, (W, b) in enumerate(zip(self.w, self.b_tc)):
             x = x @ W.float().t() + b
             if i < 4:
                 x = torch.relu(x).to(torch.bfloat16).float()

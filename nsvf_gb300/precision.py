@@ -2,11 +2,9 @@
 paths against a float64 render of the same samples.
 
 The float64 render is the validation oracle on the GPU (FP64 is used nowhere
-else). It takes the FP32 geometry of the path it checks: hit lists, sample
-depths, distances and voxel ids. For the drop-in path that geometry is
-bit-identical to the reference's operation sequence; the served path's
-differs only in the order of the per-ray sum that sets its sampling
-distribution, so it gets a float64 render of its own samples. The render
+else). It takes the FP32 geometry both paths share: hit lists, the sampling
+distribution, sample depths, distances and voxel ids (bit-identical between
+the drop-in and served paths, and to the reference's operation sequence). It
 recomputes interpolation, the field MLP and compositing in float64 with
 torch:
 
@@ -16,7 +14,8 @@ torch:
 
 `report()` gives the max and RMS RGB error and the max depth error (hit
 pixels) of each path against it: the served BF16 frame, the served frame with
-E4M3 hidden layers, and the drop-in FP32 frame.
+E4M3 hidden layers, the served chain with the FP32 field, and the drop-in FP32
+frame.
 
 Samples far outside their voxel. The reference's inverse-CDF kernel can give
 a sample the voxel id of the next row (its tail loop, which this library
@@ -24,9 +23,11 @@ reproduces bit for bit: fairnr/clib/src/sample_gpu.cu:188-201). Such a
 sample's position lies voxels away from that voxel, and the trilinear weights
 extrapolate (by 1e5x at the c2 frame), so field outputs there are orders of
 magnitude larger than elsewhere. A relative MLP error then becomes a large
-absolute colour error on those pixels. The report counts these samples (a
-coordinate more than half a voxel outside the voxel) and gives the errors
-over all pixels and over the pixels that have none.
+absolute colour error on those pixels; the served chain therefore evaluates
+those samples again in double-float arithmetic (nsvf_field_exact_dev). The
+report counts these samples (a coordinate more than half a voxel outside the
+voxel) and gives the errors over all pixels and over the pixels that have
+none.
 """
 import torch
 
@@ -36,35 +37,12 @@ from .renderer import render_rays
 from .served import SceneState, render_frame
 
 
-def _served_rows(inter, pix, step_size):
-    """The hit rows of rays `pix` with the served path's sampling
-    distribution (nsvf_gather_probs: the per-ray sum in its fixed warp
-    order)."""
-    idx = inter['intersected_voxel_idx']
-    H = idx.size(-1)
-    dev = idx.device
-    idx = idx.reshape(-1, H).int().contiguous()
-    lo = inter['min_depth'].reshape(-1, H).float().contiguous()
-    hi = inter['max_depth'].reshape(-1, H).float().contiguous()
-    n = pix.numel()
-    n_dev = torch.tensor([n], dtype=torch.int64, device=dev)
-    I = torch.empty(n, H, dtype=torch.int32, device=dev)
-    L, U, probs = (torch.empty(n, H, device=dev) for _ in range(3))
-    steps = torch.empty(n, device=dev)
-    check(LIB.nsvf_gather_probs(n, n_dev.data_ptr(), H, float(step_size), pix.data_ptr(),
-                                idx.data_ptr(), lo.data_ptr(), hi.data_ptr(), I.data_ptr(),
-                                L.data_ptr(), U.data_ptr(), probs.data_ptr(), steps.data_ptr(),
-                                ext.ctypes_stream(dev)), "gather_probs")
-    return {'intersected_voxel_idx': I, 'min_depth': L, 'max_depth': U, 'probs': probs,
-            'steps': steps}
-
-
 @torch.no_grad()
-def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768, served=False):
+def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768):
     """Float64 colours [R, 3] and depths [R] of the rays (ray_start [3],
-    ray_dir [R, 3] on the encoder's device). served: sample with the served
-    path's distribution (its per-ray sum order) instead of the drop-in
-    path's, so that the samples are the served frame's own."""
+    ray_dir [R, 3] on the encoder's device), on the samples both the drop-in
+    and the served paths evaluate (the FP32 geometry: intersection, the
+    sampling distribution of nsvf_ray_probs, inverse-CDF placement)."""
     dev = ray_dir.device
     R = ray_dir.shape[0]
     st = encoder.precompute(id=None)
@@ -74,14 +52,11 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768, served=False):
                                                          for k, v in st.items()})
     hits = hits.reshape(-1)
     pix = hits.nonzero().squeeze(1)
-    if served:
-        sub = _served_rows(inter, pix, encoder.step_size)
-    else:
-        d = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
-        inter['probs'] = d / d.sum(-1, keepdim=True)
-        inter['steps'] = d.sum(-1) / encoder.step_size
-        sub = {k: v.reshape(-1, v.shape[-1])[pix] for k, v in inter.items() if k != 'steps'}
-        sub['steps'] = inter['steps'].reshape(-1)[pix]
+    inter['probs'], inter['steps'] = ext.ray_probs(inter['intersected_voxel_idx'],
+                                                   inter['min_depth'], inter['max_depth'],
+                                                   encoder.step_size)
+    sub = {k: v.reshape(-1, v.shape[-1])[pix] for k, v in inter.items() if k != 'steps'}
+    sub['steps'] = inter['steps'].reshape(-1)[pix]
     samples = encoder.ray_sample(sub)
     centers = st['voxel_center_xyz'].double()
     feats = st['voxel_vertex_idx']
@@ -133,22 +108,25 @@ def fp64_render(encoder, field, ray_start, ray_dir, chunk=32768, served=False):
 
 
 def report(encoder, field, renderer, ray_start, ray_dir):
-    """Errors of the served BF16 and FP8 frames and of the drop-in FP32 frame,
-    each against a float64 render of its own samples."""
+    """Errors against the float64 render of the served BF16 and FP8 frames,
+    the served chain with the FP32 field (all three with the double-float
+    pass over samples far outside their voxel), and the drop-in FP32 frame
+    (the reference's module structure, no such pass)."""
     ref_c, ref_d, hits, foreign, n_foreign = fp64_render(encoder, field, ray_start, ray_dir)
-    srv_c, srv_d, _, srv_foreign, _ = fp64_render(encoder, field, ray_start, ray_dir, served=True)
     scene = SceneState(encoder, field)
     served = render_frame(scene, ray_start, ray_dir)
     served8 = render_frame(scene, ray_start, ray_dir, mlp="tc_fp8")
+    chain32 = render_frame(scene, ray_start, ray_dir, mlp="fp32")
     with torch.no_grad():
         plain = render_rays(encoder, field, renderer, ray_start.reshape(1, 1, 1, 3),
                             ray_dir.reshape(1, 1, -1, 3))
     out = {}
-    for name, c, d, rc, rdp, fr in [
-            ("served_bf16", served["colors"], served["depths"], srv_c, srv_d, srv_foreign),
-            ("served_fp8", served8["colors"], served8["depths"], srv_c, srv_d, srv_foreign),
-            ("plain_fp32", plain["colors"].reshape(-1, 3), plain["depths"].reshape(-1), ref_c, ref_d,
-             foreign)]:
+    for name, c, d in [
+            ("served_bf16", served["colors"], served["depths"]),
+            ("served_fp8", served8["colors"], served8["depths"]),
+            ("served_fp32", chain32["colors"], chain32["depths"]),
+            ("plain_fp32", plain["colors"].reshape(-1, 3), plain["depths"].reshape(-1))]:
+        rc, rdp, fr = ref_c, ref_d, foreign
         e = (c.double() - rc).abs()
         de = (d.double() - rdp).abs()[hits]
         clean = e[~fr]
@@ -158,5 +136,6 @@ def report(encoder, field, renderer, ray_start, ray_dir):
                      "rms_rgb_err_clean_pixels": float(clean.pow(2).mean().sqrt()) if clean.numel() else 0.0}
     out["hit_pixels"] = int(hits.sum())
     out["samples_outside_their_voxel"] = n_foreign
+    out["samples_reevaluated_in_double_float"] = int(served["n_far_outside"])
     out["pixels_with_such_samples"] = int(foreign.sum())
     return out

@@ -14,6 +14,7 @@ from collections import defaultdict
 
 import torch
 
+from .ext import ray_probs
 from .functional import composite
 from .geometry import fill_in, ray
 
@@ -174,13 +175,14 @@ def render_rays(encoder, field, renderer, ray_start, ray_dir, encoder_states=Non
         encoder_states = encoder.precompute(id=None)
     rs, rd, inter, hits = encoder.ray_intersect(ray_start, ray_dir, {
         k: (v.unsqueeze(0) if v is not None else None) for k, v in encoder_states.items()})
-    # probs / steps (fairnr/models/nsvf.py:65-74)
-    dists = (inter['max_depth'] - inter['min_depth']).masked_fill(inter['intersected_voxel_idx'].eq(-1), 0)
-    inter['probs'] = dists / dists.sum(dim=-1, keepdim=True)
+    # probs / steps (fairnr/models/nsvf.py:65-74), each ray's sum in slot
+    # order (nsvf_ray_probs; the served chain's order too)
+    inter['probs'], steps = ray_probs(inter['intersected_voxel_idx'], inter['min_depth'],
+                                      inter['max_depth'], encoder.step_size)
     if fixed_num_samples > 0:
         inter['steps'] = inter['min_depth'].new_ones(*inter['min_depth'].size()[:-1], 1) * fixed_num_samples
     else:
-        inter['steps'] = dists.sum(-1) / encoder.step_size
+        inter['steps'] = steps
     rs0, rd0 = rs.reshape(-1, 3), rd.reshape(-1, 3)
     all_results = defaultdict(lambda: None)
     if hits.sum() > 0:

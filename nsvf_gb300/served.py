@@ -21,6 +21,13 @@ rays, samples), so the host enqueues the frame while the traversal runs and
 reads the counts once, at the end. The sample buffers keep a capacity across
 frames; a frame that needs more is composited again with room for it.
 
+Samples far outside their voxel (the reference's inverse-CDF tail can give a
+sample the voxel id of the next hit slot, fairnr/clib/src/sample_gpu.cu:
+188-201) are listed by the MLP's loaders and their field is evaluated again in
+double-float arithmetic (nsvf_field_exact_dev) before compositing: their
+extrapolated trilinear weights would turn BF16 rounding into colour errors of
+units.
+
 Geometry (slab distances, sample depths and positions) is FP32 and comes from
 the drop-in path's kernels. The one difference from the drop-in path is the
 order of the per-ray sum of segment lengths in step 3 (a fixed warp order
@@ -56,25 +63,32 @@ class SceneState:
         self.feats = states['voxel_vertex_idx'].int().contiguous()
         self.values = states['voxel_vertex_emb'].detach().float().contiguous()
         self.field = field
+        self.device = self.centers.device
         self.mlp = TensorCoreMLP(field)
+        # BF16 bias correction, calibrated once per scene
+        self.mlp.calibrate_bias(self.calibration_emb())
         bg = field.bg_color.bg_color.detach().float().cpu()
         self.bg = (ctypes.c_float * 3)(*bg.tolist())
         self.bg_depth = float(field.bg_color.depth)
-        self.device = self.centers.device
+
+    def calibration_emb(self, n=65536, seed=0):
+        """FP32 embeddings of `n` points drawn uniformly inside random voxels
+        of this scene (seeded): the calibration set of the BF16 bias
+        correction and of the FP8 activation scales."""
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        V = self.centers.size(0)
+        vox = torch.randint(0, V, (n,), generator=g).to(self.device)
+        off = (torch.rand(n, 3, generator=g) - 0.5).to(self.device) * self.voxel_size
+        xyz = self.centers[vox] + off
+        return trilinear_embed(vox.int(), xyz, self.centers, self.feats, self.values,
+                               self.voxel_size)
 
     def mlp_fp8(self, n_calibration=65536, seed=0):
         """The tensor-core MLP with E4M3 hidden layers, its activation scales
         calibrated once on `n_calibration` points drawn uniformly inside
         random voxels of this scene (FP32 interpolation + FP32 MLP)."""
         if self.mlp.fp8 is None:
-            g = torch.Generator(device="cpu").manual_seed(seed)
-            V = self.centers.size(0)
-            vox = torch.randint(0, V, (n_calibration,), generator=g).to(self.device)
-            off = (torch.rand(n_calibration, 3, generator=g) - 0.5).to(self.device) * self.voxel_size
-            xyz = self.centers[vox] + off
-            emb = trilinear_embed(vox.int(), xyz, self.centers, self.feats, self.values,
-                                  self.voxel_size)
-            self.mlp.enable_fp8(emb)
+            self.mlp.enable_fp8(self.calibration_emb(n_calibration, seed))
         return self.mlp
 
     def bytes(self):
@@ -112,8 +126,10 @@ def _frame_buffers(scene, R, stream):
          "ws": ext._svo_workspace(1, scene.octree_centers.shape[0], dev),
          "bg": torch.tensor(list(scene.bg), dtype=torch.float32, device=dev),
          "err": torch.zeros(1, dtype=i32, device=dev),
-         "counts_host": torch.zeros(2, dtype=i64).pin_memory(),
-         "err_host": torch.zeros(1, dtype=i32).pin_memory(), "cap": 0}
+         "counts_host": torch.zeros(4, dtype=i64).pin_memory(),
+         "err_host": torch.zeros(1, dtype=i32).pin_memory(), "cap": 0,
+         "n_outl": torch.zeros(1, dtype=i64, device=dev), "outl": None, "outl_cap": 0,
+         "n_refine": torch.zeros(1, dtype=i64, device=dev)}
     frames[stream] = b
     return b
 
@@ -134,6 +150,56 @@ def _sample_buffers(b, cap):
     return b["vox"], b["xyzd"], b["depth"], b["field"]
 
 
+# Initial capacity of the list of samples far outside their voxel (about
+# 1.2k per c2 frame, 2.3k per c4 frame); it grows when a frame needs more.
+INITIAL_OUTLIERS = 16384
+
+
+# A ray whose far-outside sample has a colour magnitude above this gets its
+# other samples evaluated in FP32 (nsvf_field_refine_fp32_dev): the BF16 error
+# of the transmittance in front of that sample, about 1e-6 with the bias
+# correction on the c4 frame, times the colour stays below ~1e-3 elsewhere.
+REFINE_ABOVE = 1000.0
+
+
+def _outlier_list(b, cap):
+    if cap > b["outl_cap"]:
+        b["outl"] = None
+        b["outl"] = torch.empty(2 * cap, dtype=torch.int64, device=b["ro"].device)
+        b["outl_cap"] = cap
+    return b["outl"], b["outl_cap"]
+
+
+def _exact_pass(scene, b, R, ro, rd, vox, xyzd, depth, field, err, stream, cap, refine=True):
+    """nsvf_field_exact_dev over the frame's outlier list: the listed samples'
+    field in double-float, written over `field`; then the rays whose listed
+    sample's colour exceeds REFINE_ABOVE get their other samples in FP32
+    (nsvf_field_refine_fp32_dev). The second half of the outlier buffer holds
+    those rays."""
+    m = scene.mlp
+    ocap = b["outl_cap"]
+    rows = b["outl"][ocap:]
+    b["n_refine"].zero_()
+    with ext._timed("field_exact", scene.device):
+        check(LIB.nsvf_field_exact_dev(R, _p(b["n_hit"]), _p(b["offset"]), _p(b["pix"]), _p(ro), 3,
+                                       _p(rd), _p(depth), _p(vox), scene.centers.size(0),
+                                       scene.values.size(0), scene.voxel_size, _p(scene.centers),
+                                       _p(scene.feats), _p(scene.values), m._wtp, m._bp,
+                                       _p(b["outl"]), _p(b["n_outl"]), ocap, _p(field),
+                                       REFINE_ABOVE, _p(rows) if refine else None,
+                                       _p(b["n_refine"]) if refine else None, ocap, err,
+                                       stream), "field_exact_dev")
+    if not refine:
+        return
+    with ext._timed("field_refine_fp32", scene.device):
+        check(LIB.nsvf_field_refine_fp32_dev(_p(rows), _p(b["n_refine"]), ocap, R, _p(b["n_hit"]),
+                                             _p(b["offset"]), cap, _p(vox), _p(xyzd),
+                                             scene.centers.size(0), scene.values.size(0),
+                                             scene.voxel_size, _p(scene.centers), _p(scene.feats),
+                                             _p(scene.values), m._wtp, m._bp, _p(field), stream),
+              "field_refine_fp32_dev")
+
+
 def _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, err, stream):
     dev = scene.device
     with ext._timed("sample_compact", dev):
@@ -143,20 +209,26 @@ def _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, err, stream):
                                           _p(xyzd), _p(depth), err, stream), "sample_compact_dev")
 
 
-def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, stream):
+def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, exact, stream):
     """Steps 4-6 with the hit-ray and sample counts on the device only: the
     sample buffers have the frame buffers' capacity (INITIAL_SAMPLES_PER_RAY at
     first), and the host reads the counts and the error bits once, at the
-    end. A frame with more samples than the capacity (error bit 1) is
+    end. A frame with more samples than the capacity (error bit 1), or more
+    samples far outside their voxel than the outlier list holds (bit 4), is
     composited again with room for all of them."""
     dev = scene.device
     err = b["err"]
     counts, err_h = b["counts_host"], b["err_host"]
     cap = max(b["cap"], INITIAL_SAMPLES_PER_RAY * R)
-    for _ in range(2):
+    ocap = max(b["outl_cap"], INITIAL_OUTLIERS)
+    for _ in range(3):
         vox, xyzd, depth, field = _sample_buffers(b, cap)
         cap = b["cap"]
+        outl, ocap = _outlier_list(b, ocap) if exact else (None, 0)
+        n_outl = b["n_outl"] if exact else None
         err.zero_()
+        if exact:
+            n_outl.zero_()
         _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, _p(err), stream)
         ns_dev = _p(b["offset"][R:])
         common = (_p(vox), _p(xyzd), scene.centers.size(0), scene.values.size(0), scene.voxel_size,
@@ -164,14 +236,18 @@ def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, stream):
         if mlp == "tc":
             m = scene.mlp
             with ext._timed("field_samples_bf16", dev):
-                check(LIB.nsvf_field_samples_bf16_dev(cap, ns_dev, *common, m._wp, m._bp, _p(field),
+                check(LIB.nsvf_field_samples_bf16_dev(cap, ns_dev, *common, m._wp, m._bp_tc,
+                                                      _p(field), _p(outl), _p(n_outl), ocap,
                                                       _p(err), stream), "field_samples_bf16_dev")
         else:
             m = scene.mlp_fp8()
             with ext._timed("field_samples_fp8", dev):
                 check(LIB.nsvf_field_samples_fp8_dev(cap, ns_dev, *common, m.fp8["wp"], m._bp,
-                                                     m.fp8["scales"], _p(field), _p(err), stream),
+                                                     m.fp8["scales"], _p(field), _p(outl),
+                                                     _p(n_outl), ocap, _p(err), stream),
                       "field_samples_fp8_dev")
+        if exact:
+            _exact_pass(scene, b, R, ro, rd, vox, xyzd, depth, field, _p(err), stream, cap)
         with ext._timed("composite_segments", dev):
             check(LIB.nsvf_composite_segments_dev(
                 R, _p(b["n_hit"]), _p(b["offset"]), cap, _p(field), _p(xyzd), _p(depth), _p(b["pix"]),
@@ -179,22 +255,35 @@ def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, stream):
                 _p(out["missed"]), int(bool(kahan)), stream), "composite_segments_dev")
         counts[0:1].copy_(b["n_hit"], non_blocking=True)
         counts[1:2].copy_(b["offset"][R:], non_blocking=True)
+        if exact:
+            counts[2:3].copy_(n_outl, non_blocking=True)
+            counts[3:4].copy_(b["n_refine"], non_blocking=True)
         err_h.copy_(err, non_blocking=True)
         torch.cuda.current_stream(dev).synchronize()
         n, ns, e = int(counts[0]), int(counts[1]), int(err_h[0])
-        if not (e & 2):
+        n_far = int(counts[2]) if exact else 0
+        n_ref = int(counts[3]) if exact else 0
+        if not (e & (2 | 16)):
             break
-        cap = ns
-    if e & ~2:
+        if e & 2:
+            cap = ns
+        if e & 16:
+            ocap = max(n_far, n_ref) + max(n_far, n_ref) // 4
+    if e & ~(2 | 16):
         ext.error_word(dev).bitwise_or_(err)
-    out["n_hit_rays"], out["n_samples"] = n, ns
+    out["n_hit_rays"], out["n_samples"], out["n_far_outside"] = n, ns, n_far
+    out["n_rays_refined_fp32"] = n_ref
     return out
 
 
-def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
+def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exact=True):
     """ray_start [3] (shared origin) or [R, 3], ray_dir [R, 3] (FP32, on the
     scene's device) -> dict(colors [R, 3], depths [R], missed [R],
-    n_hit_rays, n_samples).
+    n_hit_rays, n_samples, n_far_outside).
+    exact: samples far outside their voxel (a trilinear coordinate outside
+    [-0.5, 1.5]; the reference's sampling tail gives about one per thousand
+    hit rays) get their field evaluated again in double-float arithmetic
+    (nsvf_field_exact_dev) before compositing, whatever `mlp` computed.
     mlp: "tc" (interpolation fused into the tcgen05 BF16 MLP), "tc_fp8" (the
     same with E4M3 hidden layers), "tc_unfused" (interpolation kernel, then
     the MLP kernel), "bf16_emulated" / "fp8_emulated" (torch emulations of
@@ -207,7 +296,7 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     if out is None:
         out = {"colors": torch.empty(R, 3, device=dev), "depths": torch.empty(R, device=dev),
                "missed": torch.empty(R, device=dev)}
-    out["n_hit_rays"] = out["n_samples"] = 0
+    out["n_hit_rays"] = out["n_samples"] = out["n_far_outside"] = out["n_rays_refined_fp32"] = 0
     if R == 0:
         return out
     H = scene.max_hits
@@ -244,7 +333,7 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     out["depths"].fill_(scene.bg_depth)
     out["missed"].fill_(1.0)
     if mlp in ("tc", "tc_fp8"):
-        return _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, stream)
+        return _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, exact, stream)
     counts = b["counts_host"]
     counts[0:1].copy_(b["n_hit"], non_blocking=True)
     counts[1:2].copy_(offset[R:], non_blocking=True)
@@ -261,6 +350,7 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
     if mlp == "tc_unfused":
         field = scene.mlp(emb)
     elif mlp == "bf16_emulated":
+        # (the emulation uses the BF16 kernels' corrected biases)
         field = scene.mlp.reference_bf16(emb).contiguous()
     elif mlp == "fp8_emulated":
         field = scene.mlp_fp8().reference_fp8(emb).contiguous()
@@ -268,6 +358,23 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc"):
         field = scene.field.mlp(emb).float().contiguous()
     else:
         raise ValueError("unknown mlp mode %r" % (mlp,))
+    if exact:
+        ocap = max(b["outl_cap"], INITIAL_OUTLIERS)
+        for _ in range(2):
+            outl, ocap = _outlier_list(b, ocap)
+            b["n_outl"].zero_()
+            with ext._timed("flag_outliers", dev):
+                check(LIB.nsvf_flag_outliers(ns, None, _p(vox), _p(xyzd), scene.centers.size(0),
+                                             scene.voxel_size, _p(scene.centers), _p(outl),
+                                             _p(b["n_outl"]), ocap, None, stream), "flag_outliers")
+            n_far = int(b["n_outl"].item())
+            if n_far <= ocap:
+                break
+            ocap = n_far + n_far // 4
+        _exact_pass(scene, b, R, ro, rd, vox, xyzd, depth, field, err, stream, ns,
+                    refine=mlp != "fp32")
+        out["n_far_outside"] = n_far
+        out["n_rays_refined_fp32"] = int(b["n_refine"].item())
     with ext._timed("composite_segments", dev):
         check(LIB.nsvf_composite_segments(
             n, _p(offset), _p(field), _p(xyzd), _p(depth), _p(b["pix"]), 7.0, scene.bg,

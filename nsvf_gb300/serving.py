@@ -11,7 +11,10 @@ Pieces:
   5. inverse-CDF sample count, offsets (torch cumsum) and compaction (`nsvf_sample_count_dev`,
      `nsvf_sample_compact_dev`), with the reference wrapper's launch layout taken from the device-side hit
      count;
-  6. interpolation + tcgen05 BF16 MLP on the device-side sample count (`nsvf_field_samples_bf16_dev`);
+  6. interpolation + tcgen05 BF16 MLP on the device-side sample count (`nsvf_field_samples_bf16_dev`),
+     then the double-float re-evaluation of the samples far outside their voxel (`nsvf_field_exact_dev`)
+     and the FP32 re-evaluation of the rays where such a sample's colour is large
+     (`nsvf_field_refine_fp32_dev`);
   7. compensated compositing + background into the chunk's output (`nsvf_composite_segments_dev`).
 
   It is captured once into a CUDA graph and replayed per chunk. The only per-chunk input is 18 camera
@@ -27,7 +30,7 @@ Pieces:
     is completion minus arrival.
 
 A pipeline holds at most `chunk_rays * samples_per_ray` samples. A chunk that needs more sets bit 1 of its
-error word; the server then renders that chunk again with the synchronising served path (`render_frame`),
+error word (bit 4 for more far-outside samples than its list holds); the server then renders that chunk again with the synchronising served path (`render_frame`),
 so results never depend on the capacity.
 """
 import math
@@ -39,7 +42,7 @@ import torch
 
 from . import scenes
 from ._lib import LIB, check
-from .served import SceneState, render_frame
+from .served import REFINE_ABOVE, SceneState, render_frame
 
 
 def _p(t):
@@ -96,6 +99,13 @@ class ChunkPipeline:
         self.field = z(self.cap, 4)
         self.colors, self.depths, self.missed = z(C, 3), z(C), z(C)
         self.err = z(1, dtype=i32)
+        # samples far outside their voxel, re-evaluated in double-float
+        self.outl_cap = max(4096, self.cap // 1024)
+        self.outl = z(self.outl_cap, dtype=i64)
+        self.n_outl = z(1, dtype=i64)
+        # rays re-evaluated in FP32 (their far-outside sample's colour is large)
+        self.refine_rows = z(self.outl_cap, dtype=i64)
+        self.n_refine = z(1, dtype=i64)
         n_nodes = scene.octree_centers.shape[0]
         self.ws = torch.empty(max(16, int(LIB.nsvf_svo_workspace_bytes(1, n_nodes))), dtype=u8,
                               device=dev)
@@ -127,11 +137,28 @@ class ChunkPipeline:
                                           _p(self.vox), _p(self.xyzd), _p(self.sdepth),
                                           _p(self.err), s), "sample_compact_dev")
         m = sc.mlp
+        self.n_outl.zero_()
+        self.n_refine.zero_()
         check(LIB.nsvf_field_samples_bf16_dev(self.cap, _p(self.offset[C:]), _p(self.vox),
                                               _p(self.xyzd), sc.centers.size(0), sc.values.size(0),
                                               sc.voxel_size, _p(sc.centers), _p(sc.feats),
-                                              _p(sc.values), m._wp, m._bp, _p(self.field),
+                                              _p(sc.values), m._wp, m._bp_tc, _p(self.field),
+                                              _p(self.outl), _p(self.n_outl), self.outl_cap,
                                               _p(self.err), s), "field_samples_bf16_dev")
+        check(LIB.nsvf_field_exact_dev(C, _p(self.n_hit), _p(self.offset), _p(self.pix),
+                                       _p(self.ro), 3, _p(self.rd), _p(self.sdepth), _p(self.vox),
+                                       sc.centers.size(0), sc.values.size(0), sc.voxel_size,
+                                       _p(sc.centers), _p(sc.feats), _p(sc.values), m._wtp, m._bp,
+                                       _p(self.outl), _p(self.n_outl), self.outl_cap,
+                                       _p(self.field), REFINE_ABOVE, _p(self.refine_rows),
+                                       _p(self.n_refine), self.outl_cap, _p(self.err), s),
+              "field_exact_dev")
+        check(LIB.nsvf_field_refine_fp32_dev(_p(self.refine_rows), _p(self.n_refine),
+                                             self.outl_cap, C, _p(self.n_hit), _p(self.offset),
+                                             self.cap, _p(self.vox), _p(self.xyzd),
+                                             sc.centers.size(0), sc.values.size(0), sc.voxel_size,
+                                             _p(sc.centers), _p(sc.feats), _p(sc.values), m._wtp,
+                                             m._bp, _p(self.field), s), "field_refine_fp32_dev")
         self.colors.copy_(self.bg.expand(C, 3))
         self.depths.fill_(sc.bg_depth)
         self.missed.fill_(1.0)
@@ -305,7 +332,7 @@ class Server:
                     busy[s] = None
                     progressed = True
                     r.done_chunks += 1
-                    if int(r.err[k]) & 2:
+                    if int(r.err[k]) & (2 | 16):
                         r.redo.append(k)
                     if r.done_chunks == r.n_chunks:
                         for kk in r.redo:

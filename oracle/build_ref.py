@@ -26,7 +26,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("NSVF_REFERENCE_ROOT", "/root/reference")
+# Where this recipe reads the reference checkout: NSVF_REFERENCE_ROOT, else
+# the checkout's location in the container that builds the fixtures (the
+# only place in the repository that names it; oracle.ref_import uses REF).
+REF = os.environ.get("NSVF_REFERENCE_ROOT") or "/root/reference"
 OUT = os.path.join(HERE, "_ref")
 CLIB = os.path.join(REF, "fairnr", "clib")
 

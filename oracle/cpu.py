@@ -176,8 +176,10 @@ def discretize_points(points, voxel_size):
     mn = points.min(0, keepdims=True)
     q = (points - mn) / np.float32(voxel_size)
     idx = np.round(q).astype(np.int64)   # torch.round_ = round half to even, like np.round
+    # the mean accumulated in float64 (a float32 running sum over 500k
+    # voxels drifts by 1e-2; torch's float32 mean is accurate here)
     residual = (points - idx.astype(np.float32) * np.float32(voxel_size)).mean(0, keepdims=True,
-                                                                                  dtype=np.float32)
+                                                                                  dtype=np.float64)
     return idx, residual.astype(np.float32)
 
 
@@ -217,6 +219,72 @@ def inverse_cdf_op(pts_idx, min_depth, max_depth, probs, steps, noise_rows, fixe
     return si[:, :L], sd[:, :L], ss[:, :L]
 
 
+def parallel_ray_sampling(march, pts_idx, min_depth, max_depth, noise=None):
+    """The back-up parallel uniform sampler (fairnr/clib/__init__.py:303-349)
+    on one chunk of [R, H] sorted hit lists, in float32 numpy. noise [R, K]
+    is the clamped jitter (None: 0.5). The depth sort is stable in the
+    concatenation order exits, entries, steps (the reference's torch.sort
+    leaves ties unspecified; at a face shared by two voxels this puts the
+    exit first, so the next segment takes the entered voxel's id). Returns
+    (idx, depth, dists) truncated to the largest kept count."""
+    f32 = np.float32
+    pts_idx = np.asarray(pts_idx)
+    lo = np.asarray(min_depth, f32)
+    hi = np.asarray(max_depth, f32)
+    R, H = pts_idx.shape
+    first = lo.min(1)
+    last = np.where(hi == f32(MAX_DEPTH), f32(0), hi).max(1).astype(f32)
+    K = int(f32(f32((last - first).max()) / f32(march))) if R else 0
+    k = np.arange(K, dtype=f32)[None, :]
+    jit = f32(0.5) if noise is None else np.asarray(noise, f32)[:, :K]
+    delta = ((k + jit).astype(f32) * f32(march)).astype(f32)
+    u = (lo[:, :1] + delta).astype(f32)
+    cnt = (u[:, :, None] >= lo[:, None, :]).sum(-1) - 1
+    uid = np.take_along_axis(pts_idx, cnt, 1)
+    d = np.concatenate([hi, lo, u], 1)
+    ids = np.concatenate([pts_idx, pts_idx, uid], 1)
+    order = np.argsort(d, axis=1, kind="stable")
+    d = np.take_along_axis(d, order, 1)
+    ids = np.take_along_axis(ids, order, 1)
+    dist = (d[:, 1:] - d[:, :-1]).astype(f32)
+    mid = (f32(0.5) * (d[:, 1:] + d[:, :-1]).astype(f32)).astype(f32)
+    min_ids = (mid[:, :, None] >= lo[:, None, :]).sum(-1) - 1
+    max_ids = (mid[:, :, None] >= hi[:, None, :]).sum(-1)
+    bad = (max_ids != min_ids) | (mid > last[:, None]) | (dist == 0)
+    mid = np.where(bad, f32(MAX_DEPTH), mid)
+    order = np.argsort(mid, axis=1, kind="stable")
+    mid = np.take_along_axis(mid, order, 1)
+    dist = np.where(bad, f32(0), dist)
+    dist = np.take_along_axis(dist, order, 1)
+    ids = np.take_along_axis(np.where(bad, -1, ids[:, :-1]), order, 1)
+    n = int((~np.take_along_axis(bad, order, 1)).sum(-1).max()) if R else 0
+    return ids[:, :n], mid[:, :n], dist[:, :n]
+
+
+def shared_face_ids_agree(idx, ref_idx, depth, dists, pts_idx, min_depth, max_depth):
+    """Checker for parallel_ray_sampling outputs against the reference's:
+    ids equal everywhere except segments that start at a face shared by two
+    consecutive hit voxels (one's exit equals the next one's entry), where
+    the reference's torch.sort picks either voxel; there the two ids must be
+    those two voxels. Returns the number of such segments."""
+    n = 0
+    for r, c in zip(*np.nonzero(idx != ref_idx)):
+        left = np.float64(depth[r, c]) - np.float64(dists[r, c]) / 2
+        ok = False
+        for j in range(pts_idx.shape[1] - 1):
+            if pts_idx[r, j + 1] == -1:
+                break
+            if max_depth[r, j] == min_depth[r, j + 1] and abs(left - max_depth[r, j]) <= 1e-5 and \
+                    {int(idx[r, c]), int(ref_idx[r, c])} == {int(pts_idx[r, j]), int(pts_idx[r, j + 1])}:
+                ok = True
+                break
+        if not ok:
+            raise AssertionError("segment %d of row %d: id %d vs %d away from a shared face"
+                                 % (c, r, idx[r, c], ref_idx[r, c]))
+        n += 1
+    return n
+
+
 def sort_hits(idx, lo, hi):
     """Encoder post-processing (fairnr/modules/encoder.py:518-523): misses to
     MAX_DEPTH, stable sort by min_depth, gather."""
@@ -228,9 +296,13 @@ def sort_hits(idx, lo, hi):
 
 
 def probs_steps(idx, lo, hi, step_size):
-    """fairnr/models/nsvf.py:65-74 in float32."""
+    """fairnr/models/nsvf.py:65-74 in float32, the per-ray sum taken one slot
+    at a time in slot order (np.add.accumulate is a sequential loop)."""
     d = np.where(idx == -1, np.float32(0), (hi - lo).astype(np.float32)).astype(np.float32)
-    tot = d.sum(-1, keepdims=True, dtype=np.float32)
+    if d.shape[-1] == 0:
+        tot = np.zeros(d.shape[:-1] + (1,), np.float32)
+    else:
+        tot = np.add.accumulate(d, axis=-1, dtype=np.float32)[..., -1:]
     with np.errstate(invalid="ignore", divide="ignore"):
         probs = (d / tot).astype(np.float32)
     steps = (tot[..., 0] / np.float32(step_size)).astype(np.float32)

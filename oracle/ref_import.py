@@ -24,7 +24,7 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("NSVF_REFERENCE_ROOT", "/root/reference")
+from .build_ref import REF  # noqa: E402  (the reference checkout's location)
 _STUBS = ["cv2", "pandas", "pylab", "skimage", "skimage.metrics", "imageio", "plyfile", "open3d",
           "fairseq", "fairseq.models", "fairseq.utils", "fairseq.modules", "fairseq.meters",
           "fairseq.distributed_utils", "fairseq.logging", "fairseq.logging.progress_bar",
@@ -74,6 +74,13 @@ class CpuExt:
         return tuple(cls._t(o) for o in out)
 
     @classmethod
+    def ball_intersect(cls, ray_start, ray_dir, points, radius, n_max):
+        from oracle import ref_clib
+        out = ref_clib.ball_intersect(ray_start.numpy(), ray_dir.numpy(), points.numpy(),
+                                      float(radius), int(n_max))
+        return tuple(cls._t(o) for o in out)
+
+    @classmethod
     def triangle_intersect(cls, ray_start, ray_dir, face_points, cagesize, blur, n_max):
         from oracle import ref_clib
         out = ref_clib.triangle_intersect(ray_start.numpy(), ray_dir.numpy(), face_points.numpy(),
@@ -117,7 +124,7 @@ def load():
     R = os.path.join(REF, "fairnr")
     ext = types.ModuleType("fairnr.clib._ext")
     for name in ["aabb_intersect", "svo_intersect", "uniform_ray_sampling",
-                 "inverse_cdf_sampling", "build_octree", "triangle_intersect"]:
+                 "inverse_cdf_sampling", "build_octree", "triangle_intersect", "ball_intersect"]:
         setattr(ext, name, getattr(CpuExt, name))
     sys.modules["fairnr.clib._ext"] = ext
     ns = types.SimpleNamespace()

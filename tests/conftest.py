@@ -41,6 +41,16 @@ def golden_next():
 
 
 @pytest.fixture(scope="session")
+def golden_ops():
+    return dict(np.load(os.path.join(GOLDEN, "golden_ops.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_train():
+    return dict(np.load(os.path.join(GOLDEN, "golden_train.npz")))
+
+
+@pytest.fixture(scope="session")
 def cuda():
     import torch
     if not torch.cuda.is_available():
