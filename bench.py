@@ -313,7 +313,7 @@ def train_bench(dev, steps=5, warmup=2):
         enc.values.weight.copy_(scenes.voxel_embeddings(v0.shape[0], 32, 0.01, seed=7).to(dev))
         target = train.render_batch(enc, field, ro, rd, states=st)
         enc.values.weight.copy_(v0)
-    opt = torch.optim.Adam(list(enc.parameters()) + list(field.parameters()), lr=1e-3)
+    opt = torch.optim.Adam(list(enc.parameters()) + list(field.parameters()), lr=1e-4)
     for _ in range(warmup):
         train.train_step(enc, field, ro, rd, target, optimizer=opt, states=st)
     torch.cuda.synchronize(dev)

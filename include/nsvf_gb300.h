@@ -312,6 +312,21 @@ int nsvf_composite_segments(int64_t rays, const int64_t *offset, const float *fi
 int nsvf_pinhole_rays(int64_t n, const float *cam, float *ray_start, float *ray_dir,
                       void *stream);
 
+/* pinhole_rays_multi: one serving chunk of n rays made of several pixel
+ * ranges, possibly of different frames: segment s < min(*n_seg, max_seg)
+ * (n_seg on the device) is cams[s] (18 floats as nsvf_pinhole_rays, its
+ * first pixel and pixel count included) and takes the next cams[s][17] rays
+ * of the chunk; rays past the last segment point away from the scene. */
+int nsvf_pinhole_rays_multi(int64_t n, int max_seg, const int32_t *n_seg, const float *cams,
+                            float *ray_start, float *ray_dir, void *stream);
+
+/* piece_rows: the hit-row range of every segment of such a chunk, for the
+ * piece-aware sampling entry points: with scan (int32 [n]) the inclusive
+ * prefix sum of the chunk's hit flags, piece_rows[s + 1] = hit rows of
+ * segments 0..s (max_seg + 1 entries, int64; segments past *n_seg empty). */
+int nsvf_piece_rows(int max_seg, const int32_t *n_seg, const float *cams, int64_t n,
+                    const int32_t *scan, int64_t *piece_rows, void *stream);
+
 /* camera_rays: n rays in the reference's camera convention, the eval path of
  * ImageReader (fairnr/modules/reader.py:92-119) with get_uv
  * (fairnr/data/data_utils.py:57-65) and get_ray_direction
@@ -338,7 +353,7 @@ int nsvf_compact_hits(int64_t n, const uint8_t *hits, const int32_t *scan, int64
  * loop; torch's reduction order is unspecified and differs between builds
  * and devices); probs [rows, max_hits] = d / tot; steps [rows] = tot /
  * step_size. Rows without hits get 0 / 0 = NaN probs and 0 steps, as the
- * reference's division does. max_hits <= 128. */
+ * reference's division does. Any max_hits. */
 int nsvf_ray_probs(int64_t rows, int max_hits, float step_size, const int32_t *idx,
                    const float *min_depth, const float *max_depth, float *probs, float *steps,
                    void *stream);
@@ -346,7 +361,7 @@ int nsvf_ray_probs(int64_t rows, int max_hits, float step_size, const int32_t *i
 /* gather_probs: for rows i < *n_hit, copies the sorted hit list of ray pix[i]
  * ([., max_hits] idx/min/max) and builds its sampling distribution exactly as
  * nsvf_ray_probs does (same sum order, same roundings), so the served chain
- * samples exactly the drop-in path's samples. max_hits <= 128. */
+ * samples exactly the drop-in path's samples. */
 int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
                       const int64_t *pix, const int32_t *idx, const float *min_depth,
                       const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
@@ -367,6 +382,27 @@ int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max
                             const float *ray_dir, const int64_t *ray_index,
                             const int64_t *offset, int64_t sample_cap, int32_t *voxel,
                             float *xyz_dist, float *depth, int32_t *err, void *stream);
+
+/* sample_count_pieces / sample_compact_pieces: nsvf_sample_count_dev /
+ * nsvf_sample_compact_dev for rows made of independent pieces: piece p
+ * owns rows [piece_rows[p], piece_rows[p + 1]) (max_pieces + 1 ascending
+ * entries, device memory; rows past the last entry belong to the last
+ * piece), and each piece gets the reference wrapper's launch layout for its
+ * own row count, so a piece's samples are the same whatever else shares the
+ * launch. max_pieces 0: one piece (the _dev behaviour). */
+int nsvf_sample_count_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                             const int32_t *pts_idx, const float *min_depth,
+                             const float *max_depth, const float *probs, const float *steps,
+                             const int64_t *piece_rows, int max_pieces, int32_t *count,
+                             void *stream);
+int nsvf_sample_compact_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                               const int32_t *pts_idx, const float *min_depth,
+                               const float *max_depth, const float *probs, const float *steps,
+                               const int64_t *piece_rows, int max_pieces,
+                               const float *ray_start, int64_t ray_start_stride,
+                               const float *ray_dir, const int64_t *ray_index,
+                               const int64_t *offset, int64_t sample_cap, int32_t *voxel,
+                               float *xyz_dist, float *depth, int32_t *err, void *stream);
 
 /* composite_segments_dev: nsvf_composite_segments over *n_rays_dev rays,
  * each ray's segment [offset[r], offset[r + 1]) clamped to the sample

@@ -55,6 +55,11 @@ def _load():
         "nsvf_compact_hits": ([i64, P, P, P, P, P], i32),
         "nsvf_gather_probs": ([i64, P, i32, f32, P, P, P, P, P, P, P, P, P, P], i32),
         "nsvf_ray_probs": ([i64, i32, f32, P, P, P, P, P, P], i32),
+        "nsvf_pinhole_rays_multi": ([i64, i32, P, P, P, P, P], i32),
+        "nsvf_piece_rows": ([i32, P, P, i64, P, P, P], i32),
+        "nsvf_sample_count_pieces": ([i64, P, i32, P, P, P, P, P, P, i32, P, P], i32),
+        "nsvf_sample_compact_pieces": ([i64, P, i32, P, P, P, P, P, P, i32, P, i64, P, P, P, i64,
+                                        P, P, P, P, P], i32),
         "nsvf_parallel_ray_sampling": ([i64, i32, i32, f32, P, P, P, P, i32, P, P, P, P, P], i32),
         "nsvf_parallel_sampling_smem_bytes": ([i32, i32], i64),
         "nsvf_prune_screen_bf16": ([i64, i32, i32, f32, f32, f32, i64, f32, P, P, P, P, P, P, P,
@@ -111,5 +116,6 @@ def exported_symbols():
         "nsvf_wait_timeout_selftest", "nsvf_flag_outliers", "nsvf_field_exact_dev",
         "nsvf_ray_probs", "nsvf_prune_screen_bf16", "nsvf_prune_exact_dev",
         "nsvf_field_refine_fp32_dev", "nsvf_parallel_ray_sampling",
-        "nsvf_parallel_sampling_smem_bytes",
+        "nsvf_parallel_sampling_smem_bytes", "nsvf_pinhole_rays_multi", "nsvf_piece_rows",
+        "nsvf_sample_count_pieces", "nsvf_sample_compact_pieces",
     ]

@@ -17,12 +17,13 @@ constexpr int kBlock = 256;
 // any frame. Ray t is pixel first + t (row-major) and looks along
 // normalize(R ((j + .5 - cx) / f, (i + .5 - cy) / f, 1)); rays t >= count
 // repeat the last pixel with the direction reversed, away from the scene.
-__global__ void pinhole_kernel(int64_t n, const float *__restrict__ cam, float *__restrict__ ro,
-                               float *__restrict__ rd) {
-  int64_t t = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (t >= n) return;
+// Ray t of a camera's pixel range: local index t (t >= count repeats the last
+// pixel, pointing away from the scene), written to slot `out`.
+__device__ __forceinline__ void pinhole_ray(const float *__restrict__ cam, int64_t t, int64_t out,
+                                            float *__restrict__ ro, float *__restrict__ rd) {
   float f = cam[12], cx = cam[13], cy = cam[14];
   int64_t W = (int64_t)cam[15];
+  if (W < 1) W = 1;
   int64_t first = (int64_t)cam[16], count = (int64_t)cam[17];
   if (count < 1) count = 1;
   int64_t pix = first + (t < count ? t : count - 1);
@@ -33,8 +34,62 @@ __global__ void pinhole_kernel(int64_t n, const float *__restrict__ cam, float *
   float z = cam[9] * a + cam[10] * b + cam[11];
   float inv = rsqrtf(x * x + y * y + z * z);
   if (t >= count) inv = -inv;
-  ro[t * 3 + 0] = cam[0]; ro[t * 3 + 1] = cam[1]; ro[t * 3 + 2] = cam[2];
-  rd[t * 3 + 0] = x * inv; rd[t * 3 + 1] = y * inv; rd[t * 3 + 2] = z * inv;
+  ro[out * 3 + 0] = cam[0]; ro[out * 3 + 1] = cam[1]; ro[out * 3 + 2] = cam[2];
+  rd[out * 3 + 0] = x * inv; rd[out * 3 + 1] = y * inv; rd[out * 3 + 2] = z * inv;
+}
+
+__global__ void pinhole_kernel(int64_t n, const float *__restrict__ cam, float *__restrict__ ro,
+                               float *__restrict__ rd) {
+  int64_t t = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (t >= n) return;
+  pinhole_ray(cam, t, t, ro, rd);
+}
+
+// A chunk of several pixel ranges (of different frames): segment s (s <
+// min(*n_seg, max_seg)) holds cams[s][17] rays, in order; rays past the last
+// segment repeat its last pixel pointing away from the scene.
+__global__ void pinhole_multi_kernel(int64_t n, int max_seg, const int32_t *__restrict__ n_seg,
+                                     const float *__restrict__ cams, float *__restrict__ ro,
+                                     float *__restrict__ rd) {
+  int64_t t = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (t >= n) return;
+  int ns = *n_seg < max_seg ? *n_seg : max_seg;
+  if (ns < 1) ns = 1;
+  int64_t acc = 0;
+  int s = 0;
+  for (; s < ns; ++s) {
+    int64_t c = (int64_t)cams[s * 18 + 17];
+    if (c < 0) c = 0;
+    if (t < acc + c) break;
+    acc += c;
+  }
+  if (s == ns) {
+    // past the last segment: its last pixel, pointing away
+    pinhole_ray(cams + (ns - 1) * 18, (int64_t)1 << 40, t, ro, rd);
+    return;
+  }
+  pinhole_ray(cams + s * 18, t - acc, t, ro, rd);
+}
+
+// The hit-row range of every segment of a multi-segment chunk: with scan the
+// inclusive prefix sum of the chunk's hit flags, segment s owns hit rows
+// [piece_rows[s], piece_rows[s + 1]); segments past *n_seg are empty.
+__global__ void piece_rows_kernel(int max_seg, const int32_t *__restrict__ n_seg,
+                                  const float *__restrict__ cams, int64_t n,
+                                  const int32_t *__restrict__ scan,
+                                  int64_t *__restrict__ piece_rows) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int ns = *n_seg < max_seg ? *n_seg : max_seg;
+  int64_t acc = 0;
+  piece_rows[0] = 0;
+  for (int s = 0; s < max_seg; ++s) {
+    if (s < ns) {
+      int64_t c = (int64_t)cams[s * 18 + 17];
+      acc += c > 0 ? c : 0;
+      if (acc > n) acc = n;
+    }
+    piece_rows[s + 1] = acc > 0 ? (int64_t)scan[acc - 1] : 0;
+  }
 }
 
 // Rays in the reference's camera convention: ImageReader's eval path
@@ -86,25 +141,28 @@ __global__ void compact_hits_kernel(int64_t n, const uint8_t *__restrict__ hits,
 // max_k - min_k where slot k is a hit (0 elsewhere), tot = d_0 + d_1 + ... +
 // d_{H-1} added one slot at a time in slot order (FP32, the order of a
 // plain loop), probs_k = d_k / tot, steps = tot / step. One warp per row:
-// lane l holds slots l, l + 32, ...; every lane adds the row's values in slot
-// order from shuffles, so all lanes hold the same total. Rows are coalesced.
-// Both the drop-in path (nsvf_ray_probs) and the served chain
-// (nsvf_gather_probs) use it, so their samples are identical.
-template <int kMaxChunks>
-__device__ __forceinline__ float row_total(const float (&d)[kMaxChunks], int H, int lane) {
-  float tot = 0.0f;
-#pragma unroll
-  for (int c = 0; c < kMaxChunks; ++c) {
-    const int base = 32 * c;
-    if (base >= H) break;
-    const int n = H - base < 32 ? H - base : 32;
-    for (int j = 0; j < n; ++j) tot = __fadd_rn(tot, __shfl_sync(0xffffffffu, d[c], j));
-  }
-  (void)lane;
-  return tot;
+// the row is read 32 slots at a time (coalesced) and every lane adds the 32
+// values in slot order from shuffles, so all lanes hold the same total; a
+// second sweep writes the probabilities. Both the drop-in path
+// (nsvf_ray_probs) and the served chain (nsvf_gather_probs) use it, so their
+// samples are identical.
+__device__ __forceinline__ float slot_d(const int32_t *__restrict__ ir,
+                                        const float *__restrict__ lr,
+                                        const float *__restrict__ hr, int k) {
+  return ir[k] == -1 ? 0.0f : __fsub_rn(hr[k], lr[k]);
 }
 
-constexpr int kProbChunks = 4;  // rows of up to 128 slots
+__device__ __forceinline__ float row_total(const int32_t *__restrict__ ir,
+                                           const float *__restrict__ lr,
+                                           const float *__restrict__ hr, int H, int lane) {
+  float tot = 0.0f;
+  for (int base = 0; base < H; base += 32) {
+    const float dv = base + lane < H ? slot_d(ir, lr, hr, base + lane) : 0.0f;
+    const int n = H - base < 32 ? H - base : 32;
+    for (int j = 0; j < n; ++j) tot = __fadd_rn(tot, __shfl_sync(0xffffffffu, dv, j));
+  }
+  return tot;
+}
 
 __global__ void __launch_bounds__(kBlock) ray_probs_kernel(
     int64_t rows, int H, float step, const int32_t *__restrict__ idx,
@@ -113,19 +171,10 @@ __global__ void __launch_bounds__(kBlock) ray_probs_kernel(
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (kBlock / 32);
   for (int64_t r = (blockIdx.x * (int64_t)kBlock + threadIdx.x) >> 5; r < rows; r += warps) {
-    float d[kProbChunks];
-#pragma unroll
-    for (int c = 0; c < kProbChunks; ++c) {
-      const int k = 32 * c + lane;
-      d[c] = 0.0f;
-      if (k < H && idx[r * H + k] != -1) d[c] = __fsub_rn(hi[r * H + k], lo[r * H + k]);
-    }
-    const float tot = row_total(d, H, lane);
-#pragma unroll
-    for (int c = 0; c < kProbChunks; ++c) {
-      const int k = 32 * c + lane;
-      if (k < H) probs[r * H + k] = __fdiv_rn(d[c], tot);
-    }
+    const int32_t *ir = idx + r * H;
+    const float *lr = lo + r * H, *hr = hi + r * H;
+    const float tot = row_total(ir, lr, hr, H, lane);
+    for (int k = lane; k < H; k += 32) probs[r * H + k] = __fdiv_rn(slot_d(ir, lr, hr, k), tot);
     if (lane == 0) steps[r] = __fdiv_rn(tot, step);
   }
 }
@@ -145,25 +194,12 @@ __global__ void __launch_bounds__(kBlock) gather_probs_kernel(
     const int64_t r = pix[i];
     const int32_t *ir = idx + r * H;
     const float *lr = lo + r * H, *hr = hi + r * H;
-    float d[kProbChunks];
-#pragma unroll
-    for (int c = 0; c < kProbChunks; ++c) {
-      const int k = 32 * c + lane;
-      d[c] = 0.0f;
-      if (k < H) {
-        const int32_t id = ir[k];
-        const float a = lr[k], b = hr[k];
-        I[i * H + k] = id;
-        L[i * H + k] = a;
-        U[i * H + k] = b;
-        if (id != -1) d[c] = __fsub_rn(b, a);
-      }
-    }
-    const float tot = row_total(d, H, lane);
-#pragma unroll
-    for (int c = 0; c < kProbChunks; ++c) {
-      const int k = 32 * c + lane;
-      if (k < H) probs[i * H + k] = __fdiv_rn(d[c], tot);
+    const float tot = row_total(ir, lr, hr, H, lane);
+    for (int k = lane; k < H; k += 32) {
+      I[i * H + k] = ir[k];
+      L[i * H + k] = lr[k];
+      U[i * H + k] = hr[k];
+      probs[i * H + k] = __fdiv_rn(slot_d(ir, lr, hr, k), tot);
     }
     if (lane == 0) steps[i] = __fdiv_rn(tot, step);
   }
@@ -180,6 +216,23 @@ int nsvf_pinhole_rays(int64_t n, const float *cam, float *ray_start, float *ray_
   if (!ray_start || !ray_dir) return NSVF_ERR_INVALID;
   pinhole_kernel<<<nsvf_grid(n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(n, cam, ray_start,
                                                                           ray_dir);
+  return nsvf_launch_status();
+}
+
+int nsvf_pinhole_rays_multi(int64_t n, int max_seg, const int32_t *n_seg, const float *cams,
+                            float *ray_start, float *ray_dir, void *stream) {
+  if (n < 0 || max_seg < 1 || !n_seg || !cams) return NSVF_ERR_INVALID;
+  if (n == 0) return NSVF_OK;
+  if (!ray_start || !ray_dir) return NSVF_ERR_INVALID;
+  pinhole_multi_kernel<<<nsvf_grid(n, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      n, max_seg, n_seg, cams, ray_start, ray_dir);
+  return nsvf_launch_status();
+}
+
+int nsvf_piece_rows(int max_seg, const int32_t *n_seg, const float *cams, int64_t n,
+                    const int32_t *scan, int64_t *piece_rows, void *stream) {
+  if (max_seg < 1 || n < 1 || !n_seg || !cams || !scan || !piece_rows) return NSVF_ERR_INVALID;
+  piece_rows_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(max_seg, n_seg, cams, n, scan, piece_rows);
   return nsvf_launch_status();
 }
 
@@ -204,7 +257,7 @@ int nsvf_camera_rays(int64_t n, const float *cam, float *ray_start, float *ray_d
 int nsvf_ray_probs(int64_t rows, int max_hits, float step_size, const int32_t *idx,
                    const float *min_depth, const float *max_depth, float *probs, float *steps,
                    void *stream) {
-  if (rows < 0 || max_hits < 1 || max_hits > 32 * kProbChunks) return NSVF_ERR_INVALID;
+  if (rows < 0 || max_hits < 1) return NSVF_ERR_INVALID;
   if (rows == 0) return NSVF_OK;
   if (!idx || !min_depth || !max_depth || !probs || !steps) return NSVF_ERR_INVALID;
   int blocks = nsvf_grid(rows, kBlock / 32);
@@ -218,7 +271,7 @@ int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float ste
                       const int64_t *pix, const int32_t *idx, const float *min_depth,
                       const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,
                       float *probs, float *steps, void *stream) {
-  if (cap < 0 || max_hits < 1 || max_hits > 32 * kProbChunks || !n_hit) return NSVF_ERR_INVALID;
+  if (cap < 0 || max_hits < 1 || !n_hit) return NSVF_ERR_INVALID;
   if (cap == 0) return NSVF_OK;
   if (!pix || !idx || !min_depth || !max_depth || !out_idx || !out_min || !out_max || !probs ||
       !steps)

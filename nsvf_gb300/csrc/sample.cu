@@ -158,18 +158,52 @@ __device__ __forceinline__ bool dyn_rows(const int64_t *n_dev, int64_t cap, int6
   return true;
 }
 
+// With a piece table, the hit rows are the concatenation of independent
+// pieces (pixel ranges of different frames packed into one serving chunk):
+// piece p owns rows [piece_rows[p], piece_rows[p + 1]) (max_pieces + 1
+// ascending entries; rows past the last entry belong to the last piece), and
+// each piece gets the reference wrapper's layout for its own row count, as if
+// it had been launched alone. A piece's results then do not depend on what
+// else shares the chunk.
+__device__ __forceinline__ void piece_rows_of(int64_t r, const int64_t *__restrict__ piece_rows,
+                                              int max_pieces, int64_t &tail, int64_t &nxt) {
+  int lo = 0, hi = max_pieces;   // piece_rows[lo] <= r; find the last such lo < max_pieces
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (piece_rows[mid] <= r) lo = mid;
+    else hi = mid;
+  }
+  const int64_t base = piece_rows[lo];
+  int64_t end = piece_rows[lo + 1];
+  if (end <= r) end = r + 1;
+  const int64_t N = end - base, G = 200;
+  int64_t K = (N + G - 1) / G;
+  if (K < 1) K = 1;
+  icdf_rows(r - base, K, 800, N, G, tail, nxt);
+  tail += base;
+  if (nxt >= 0) nxt += base;
+}
+
+__device__ __forceinline__ void row_layout(int64_t r, int64_t K, int64_t C, int64_t N, int64_t G,
+                                           const int64_t *__restrict__ piece_rows, int max_pieces,
+                                           int64_t &tail, int64_t &nxt) {
+  if (piece_rows) piece_rows_of(r, piece_rows, max_pieces, tail, nxt);
+  else icdf_rows(r, K, C, N, G, tail, nxt);
+}
+
 __global__ void __launch_bounds__(kBlock) icdf_count_kernel(
     int64_t rows, int H, const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
     const float *__restrict__ max_depth, const float *__restrict__ probs,
     const float *__restrict__ steps, int64_t K, int64_t C, int64_t N, int64_t G,
-    const int64_t *__restrict__ n_dev, int32_t *__restrict__ count) {
+    const int64_t *__restrict__ n_dev, int32_t *__restrict__ count,
+    const int64_t *__restrict__ piece_rows, int max_pieces) {
   int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   int64_t cap = rows;
   dyn_rows(n_dev, cap, rows, K, C, N, G);
   if (r >= cap) return;
   if (r >= rows) { count[r] = 0; return; }
   int64_t tail, nxt;
-  icdf_rows(r, K, C, N, G, tail, nxt);
+  row_layout(r, K, C, N, G, piece_rows, max_pieces, tail, nxt);
   CountEmit em{0};
   icdf_walk(H, pts_idx + r * H, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H,
             max_depth + r * H, probs + r * H, steps[r], nullptr, 0, -1.0f, em);
@@ -205,13 +239,14 @@ __global__ void __launch_bounds__(kBlock) icdf_compact_kernel(
     int64_t ray_start_stride, const float *__restrict__ ray_dir,
     const int64_t *__restrict__ ray_index, const int64_t *__restrict__ offset,
     int64_t sample_cap, int32_t *__restrict__ vox, float4 *__restrict__ xyzd,
-    float *__restrict__ depth, int32_t *__restrict__ err) {
+    float *__restrict__ depth, int32_t *__restrict__ err, const int64_t *__restrict__ piece_rows,
+    int max_pieces) {
   int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   int64_t cap = rows;
   dyn_rows(n_dev, cap, rows, K, C, N, G);
   if (r >= rows) return;
   int64_t tail, nxt;
-  icdf_rows(r, K, C, N, G, tail, nxt);
+  row_layout(r, K, C, N, G, piece_rows, max_pieces, tail, nxt);
   // the ray's origin/direction: row r of the ray arrays, or row ray_index[r]
   int64_t rr = ray_index ? ray_index[r] : r;
   const float *o = ray_start + rr * ray_start_stride;
@@ -430,7 +465,8 @@ __global__ void __launch_bounds__(32 * kWarpRays) icdf_warp_kernel(
     const float *__restrict__ ray_start, int64_t ray_start_stride,
     const float *__restrict__ ray_dir, const int64_t *__restrict__ ray_index,
     const int64_t *__restrict__ offset, int64_t sample_cap, int32_t *__restrict__ vox,
-    float4 *__restrict__ xyzd, float *__restrict__ depth, int32_t *__restrict__ err) {
+    float4 *__restrict__ xyzd, float *__restrict__ depth, int32_t *__restrict__ err,
+    const int64_t *__restrict__ piece_rows, int max_pieces) {
   __shared__ RayTab tabs[kWarpRays];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   RayTab &T = tabs[wib];
@@ -443,7 +479,7 @@ __global__ void __launch_bounds__(32 * kWarpRays) icdf_warp_kernel(
       continue;
     }
     int64_t tail, nxt;
-    icdf_rows(r, K, C, N, G, tail, nxt);
+    row_layout(r, K, C, N, G, piece_rows, max_pieces, tail, nxt);
     const int32_t *I = pts_idx + r * H;
     WarpRay w = build_tab(T, H, I, min_depth + r * H, max_depth + r * H, probs + r * H,
                           steps[r], lane);
@@ -801,10 +837,11 @@ int nsvf_sample_count(int64_t rows, int max_hits, const int32_t *pts_idx, const 
   if (max_hits <= kMaxH)
     icdf_warp_kernel<false><<<warp_grid(rows), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
         rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count,
-        nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr);
+        nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0);
   else
     icdf_count_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-        rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count);
+        rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, count,
+        nullptr, 0);
   return nsvf_launch_status();
 }
 
@@ -826,29 +863,72 @@ int nsvf_sample_compact(int64_t rows, int max_hits, const int32_t *pts_idx,
     icdf_warp_kernel<true><<<warp_grid(rows), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
         rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, nullptr,
         ray_start, ray_start_stride, ray_dir, nullptr, offset, INT64_MAX, voxel,
-        (float4 *)xyz_dist, depth, err);
+        (float4 *)xyz_dist, depth, err, nullptr, 0);
   else
     icdf_compact_kernel<<<nsvf_grid(rows, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
         rows, max_hits, pts_idx, min_depth, max_depth, probs, steps, K, C, N, G, nullptr, ray_start,
         ray_start_stride, ray_dir, nullptr, offset, INT64_MAX, voxel, (float4 *)xyz_dist, depth,
-        err);
+        err, nullptr, 0);
+  return nsvf_launch_status();
+}
+
+int nsvf_sample_count_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                             const int32_t *pts_idx, const float *min_depth,
+                             const float *max_depth, const float *probs, const float *steps,
+                             const int64_t *piece_rows, int max_pieces, int32_t *count,
+                             void *stream) {
+  if (rows_cap < 0 || max_hits < 1 || !n_rows_dev || max_pieces < 0 ||
+      (max_pieces > 0 && !piece_rows))
+    return NSVF_ERR_INVALID;
+  if (rows_cap == 0) return NSVF_OK;
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !count) return NSVF_ERR_INVALID;
+  const int64_t *pr = max_pieces > 0 ? piece_rows : nullptr;
+  if (max_hits <= kMaxH)
+    icdf_warp_kernel<false><<<warp_grid(rows_cap), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+        count, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, pr,
+        max_pieces);
+  else
+    icdf_count_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
+        count, pr, max_pieces);
   return nsvf_launch_status();
 }
 
 int nsvf_sample_count_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
                           const int32_t *pts_idx, const float *min_depth, const float *max_depth,
                           const float *probs, const float *steps, int32_t *count, void *stream) {
-  if (rows_cap < 0 || max_hits < 1 || !n_rows_dev) return NSVF_ERR_INVALID;
+  return nsvf_sample_count_pieces(rows_cap, n_rows_dev, max_hits, pts_idx, min_depth, max_depth,
+                                  probs, steps, nullptr, 0, count, stream);
+}
+
+int nsvf_sample_compact_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                               const int32_t *pts_idx, const float *min_depth,
+                               const float *max_depth, const float *probs, const float *steps,
+                               const int64_t *piece_rows, int max_pieces,
+                               const float *ray_start, int64_t ray_start_stride,
+                               const float *ray_dir, const int64_t *ray_index,
+                               const int64_t *offset, int64_t sample_cap, int32_t *voxel,
+                               float *xyz_dist, float *depth, int32_t *err, void *stream) {
+  if (rows_cap < 0 || max_hits < 1 || !n_rows_dev || sample_cap < 0 ||
+      (ray_start_stride != 0 && ray_start_stride != 3) || max_pieces < 0 ||
+      (max_pieces > 0 && !piece_rows))
+    return NSVF_ERR_INVALID;
   if (rows_cap == 0) return NSVF_OK;
-  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !count) return NSVF_ERR_INVALID;
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !ray_start || !ray_dir ||
+      !offset || !voxel || !xyz_dist || !depth || (((uintptr_t)xyz_dist) & 15))
+    return NSVF_ERR_INVALID;
+  const int64_t *pr = max_pieces > 0 ? piece_rows : nullptr;
   if (max_hits <= kMaxH)
-    icdf_warp_kernel<false><<<warp_grid(rows_cap), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+    icdf_warp_kernel<true><<<warp_grid(rows_cap), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
         rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
-        count, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr);
+        nullptr, ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
+        (float4 *)xyz_dist, depth, err, pr, max_pieces);
   else
-    icdf_count_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+    icdf_compact_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
         rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
-        count);
+        ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
+        (float4 *)xyz_dist, depth, err, pr, max_pieces);
   return nsvf_launch_status();
 }
 
@@ -859,24 +939,10 @@ int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max
                             const float *ray_dir, const int64_t *ray_index,
                             const int64_t *offset, int64_t sample_cap, int32_t *voxel,
                             float *xyz_dist, float *depth, int32_t *err, void *stream) {
-  if (rows_cap < 0 || max_hits < 1 || !n_rows_dev || sample_cap < 0 ||
-      (ray_start_stride != 0 && ray_start_stride != 3))
-    return NSVF_ERR_INVALID;
-  if (rows_cap == 0) return NSVF_OK;
-  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !ray_start || !ray_dir ||
-      !offset || !voxel || !xyz_dist || !depth || (((uintptr_t)xyz_dist) & 15))
-    return NSVF_ERR_INVALID;
-  if (max_hits <= kMaxH)
-    icdf_warp_kernel<true><<<warp_grid(rows_cap), 32 * kWarpRays, 0, (cudaStream_t)stream>>>(
-        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
-        nullptr, ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
-        (float4 *)xyz_dist, depth, err);
-  else
-    icdf_compact_kernel<<<nsvf_grid(rows_cap, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-        rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, 1, 1, 1, 1, n_rows_dev,
-        ray_start, ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel,
-        (float4 *)xyz_dist, depth, err);
-  return nsvf_launch_status();
+  return nsvf_sample_compact_pieces(rows_cap, n_rows_dev, max_hits, pts_idx, min_depth,
+                                    max_depth, probs, steps, nullptr, 0, ray_start,
+                                    ray_start_stride, ray_dir, ray_index, offset, sample_cap,
+                                    voxel, xyz_dist, depth, err, stream);
 }
 
 int nsvf_uniform_ray_sampling(int b, int m, int max_hits, int max_steps, float step_size,

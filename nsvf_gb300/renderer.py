@@ -163,13 +163,59 @@ class VolumeRenderer(torch.nn.Module):
         return results
 
 
+def normalize_rows(x):
+    """x / x.sum(-1) with each row summed one slot at a time in slot order
+    (nsvf_ray_probs on intervals [0, x]), the order the sampling
+    distributions of this library use."""
+    H = x.size(-1)
+    idx = torch.zeros(x.shape, dtype=torch.int32, device=x.device)
+    p, tot = ray_probs(idx, torch.zeros_like(x, dtype=torch.float32), x.float(), 1.0)
+    return p, tot
+
+
+def prepare_hierarchical_sampling(intersection_outputs, samples, all_results,
+                                  fixed_fine_num_samples=0, reduce_fine_for_missed=False,
+                                  fine_num_sample_ratio=0):
+    """Hierarchical resampling (fairnr/models/nerf.py:64-79; NSVFModel's
+    fine_num_sample_ratio, fairnr/models/nsvf.py:83-87): every coarse sample
+    becomes an interval [t - d/2, t + d/2] with its voxel id; the
+    distribution is the coarse render's per-sample probs plus 1e-5,
+    normalised per ray (slot-order sum); steps are 1 per ray times
+    fixed_fine_num_samples (if set), times the ray's summed probs with
+    reduce_fine_for_missed, or fine_num_sample_ratio times the ray's number
+    of coarse samples (if set, NSVF's rule). The inverse-CDF op then places
+    the fine samples."""
+    depth = samples.get('original_point_depth', samples['sampled_point_depth'])
+    dists = samples.get('original_point_distance', samples['sampled_point_distance'])
+    out = dict(intersection_outputs)
+    out['min_depth'] = depth - dists * .5
+    out['max_depth'] = depth + dists * .5
+    out['intersected_voxel_idx'] = samples['sampled_point_voxel_idx'].contiguous()
+    safe = all_results['probs'] + 1e-5
+    out['probs'], total = normalize_rows(safe)
+    out['steps'] = safe.new_ones(*safe.size()[:-1])
+    if fixed_fine_num_samples > 0:
+        out['steps'] = out['steps'] * fixed_fine_num_samples
+    if reduce_fine_for_missed:
+        out['steps'] = out['steps'] * total
+    if fine_num_sample_ratio > 0:
+        out['steps'] = samples['sampled_point_voxel_idx'].ne(-1).sum(-1).float() * fine_num_sample_ratio
+    return out
+
+
 def render_rays(encoder, field, renderer, ray_start, ray_dir, encoder_states=None,
-                fixed_num_samples=0):
+                fixed_num_samples=0, hierarchical=False, field_fine=None,
+                fixed_fine_num_samples=0, fine_num_sample_ratio=0,
+                reduce_fine_for_missed=False):
     """One frame of rays through the NSVF model glue: intersect, keep the hit
     rays, build the sampling distribution, sample, render, fill the missed
     rays with the background. ray_start [S, V, P, 3] (or [S, 1, 1, 3]
     broadcast), ray_dir [S, V, P, 3]; returns the reference's output dict
-    (colors [S, V, P, 3], depths, missed, ...)."""
+    (colors [S, V, P, 3], depths, missed, ...).
+    hierarchical: a second, fine pass on samples placed by the coarse pass's
+    probabilities (prepare_hierarchical_sampling), rendered with field_fine
+    (or `field`); the coarse results are under 'coarse'
+    (fairnr/models/fairnr_model.py:142-186)."""
     S, V, P, _ = ray_dir.size()
     if encoder_states is None:
         encoder_states = encoder.precompute(id=None)
@@ -185,13 +231,30 @@ def render_rays(encoder, field, renderer, ray_start, ray_dir, encoder_states=Non
         inter['steps'] = steps
     rs0, rd0 = rs.reshape(-1, 3), rd.reshape(-1, 3)
     all_results = defaultdict(lambda: None)
+    coarse = None
     if hits.sum() > 0:
         sub = {name: outs[hits] for name, outs in inter.items()}
         rsh, rdh = rs[hits], rd[hits]
         samples = encoder.ray_sample(sub)
         all_results = renderer(encoder, field.forward, rsh, rdh, samples, encoder_states)
         all_results['voxel_depth'] = samples['sampled_point_depth'][:, 0]
+        if hierarchical:
+            sub = prepare_hierarchical_sampling(sub, samples, all_results, fixed_fine_num_samples,
+                                                reduce_fine_for_missed, fine_num_sample_ratio)
+            coarse = dict(all_results)
+            samples = encoder.ray_sample(sub)
+            fine = field_fine if field_fine is not None else field
+            all_results = renderer(encoder, fine.forward, rsh, rdh, samples, encoder_states)
+            all_results['voxel_depth'] = samples['sampled_point_depth'][:, 0]
     hits = hits.reshape(-1)
+    out = _postprocess(all_results, hits, field, rs0, S, V, P)
+    if coarse is not None:
+        out['coarse'] = _postprocess(coarse, hits, field, rs0, S, V, P)
+    return out
+
+
+def _postprocess(all_results, hits, field, rs0, S, V, P):
+    """fill_in + background (fairnr/models/nsvf.py:89-110)."""
     full = S * V * P
     out = dict(all_results)
     if all_results['missed'] is None:

@@ -285,6 +285,28 @@ def shared_face_ids_agree(idx, ref_idx, depth, dists, pts_idx, min_depth, max_de
     return n
 
 
+def prepare_hierarchical(depth, dists, voxel_idx, probs, fixed_fine_num_samples=0,
+                         fine_num_sample_ratio=0):
+    """Hierarchical resampling's fine-pass inputs (fairnr/models/nerf.py:
+    64-79, fairnr/models/nsvf.py:83-87) in float32: intervals [t - d/2,
+    t + d/2], the coarse probs plus 1e-5 normalised per ray (sequential
+    slot-order sum), steps = fixed_fine_num_samples or the coarse count times
+    fine_num_sample_ratio."""
+    f32 = np.float32
+    depth, dists = np.asarray(depth, f32), np.asarray(dists, f32)
+    lo = (depth - dists * f32(0.5)).astype(f32)
+    hi = (depth + dists * f32(0.5)).astype(f32)
+    safe = (np.asarray(probs, f32) + f32(1e-5)).astype(f32)
+    tot = np.add.accumulate(safe, axis=-1, dtype=f32)[..., -1:]
+    pr = (safe / tot).astype(f32)
+    steps = np.ones(safe.shape[:-1], f32)
+    if fixed_fine_num_samples > 0:
+        steps = (steps * f32(fixed_fine_num_samples)).astype(f32)
+    if fine_num_sample_ratio > 0:
+        steps = ((voxel_idx != -1).sum(-1).astype(f32) * f32(fine_num_sample_ratio)).astype(f32)
+    return lo, hi, np.asarray(voxel_idx), pr, steps
+
+
 def sort_hits(idx, lo, hi):
     """Encoder post-processing (fairnr/modules/encoder.py:518-523): misses to
     MAX_DEPTH, stable sort by min_depth, gather."""

@@ -51,6 +51,11 @@ def golden_train():
 
 
 @pytest.fixture(scope="session")
+def golden_hier():
+    return dict(np.load(os.path.join(GOLDEN, "golden_hier.npz")))
+
+
+@pytest.fixture(scope="session")
 def cuda():
     import torch
     if not torch.cuda.is_available():

@@ -7,7 +7,9 @@ Workload: the 125,476-voxel c2 shell with N(0, 0.01^2) corner embeddings
 (seed 1), the 4 x 128 field with its density row scaled 30x and bias 0.5 (an
 opaque field, so that compositing gradients matter), a batch of 4 views
 (cameras 0, 25, 50, 75 of the 100 on the radius-4 sphere, 800x800) x 2,048
-pixels drawn (seed 21) among the pixels whose ray hits a voxel, and targets
+pixels drawn (seed 21) among the pixels whose ray hits a voxel and enters no
+two voxels at the same depth (where the reference's unstable depth sort is
+free to order them either way), and targets
 rendered from a second embedding set (seed 7). Both sides sample with the
 slot-order sampling distribution (oracle.cpu.probs_steps), so they evaluate
 the same samples.
@@ -45,15 +47,21 @@ SIGMA_SCALE, SIGMA_BIAS = 30.0, 0.5
 
 
 def batch_pixels(sc):
-    """(view, pixel) pairs: 2,048 hit pixels per view, seeded."""
+    """(view, pixel) pairs: 2,048 hit pixels per view, seeded, among the rays
+    that enter no two voxels at the same depth (for those the reference's
+    unstable torch.sort may order the hits either way, and the samples with
+    them)."""
     cen, chi = sc["octree"]
     rng = np.random.RandomState(21)
     out = []
     for v in VIEWS:
         rs, rd = workload.frame(v)
-        idx, _, _ = cpu.svo_intersect(np.broadcast_to(rs, (rd.shape[0], 3))[None], rd[None],
-                                      cen[None], chi[None], sc["voxel_size"], 64)
-        hit = np.nonzero((idx[0] != -1).any(-1))[0]
+        idx, lo, _ = cpu.sort_hits(*cpu.svo_intersect(np.broadcast_to(rs, (rd.shape[0], 3))[None],
+                                                      rd[None], cen[None], chi[None],
+                                                      sc["voxel_size"], 64))
+        idx, lo = idx[0], lo[0]
+        tie = ((lo[:, 1:] == lo[:, :-1]) & (idx[:, 1:] != -1)).any(-1)
+        hit = np.nonzero((idx != -1).any(-1) & ~tie)[0]
         out.append(np.sort(rng.choice(hit, RAYS_PER_VIEW, replace=False)))
     return np.stack(out)
 

@@ -101,3 +101,33 @@ def test_c2_subset(golden_ops):
     m = ref_si != -1
     assert np.array_equal(sd[m], go["c2_det_sampled_point_depth"][m])
     assert np.array_equal(np.maximum(ss[m], 0), go["c2_det_sampled_point_distance"][m])
+
+
+def test_hierarchical_resampling(golden, golden_hier):
+    """The oracle's fine-pass inputs and fine samples against the reference's
+    (golden_hier.npz): bit for bit, except the normalised probabilities
+    (torch's pairwise sum, ~1e-6 relative); fine samples from the reference's
+    inputs."""
+    g, gh = golden, golden_hier
+    for tag, kw in [("nerf64", dict(fixed_fine_num_samples=64)),
+                    ("nsvf2", dict(fine_num_sample_ratio=2.0))]:
+        lo, hi, vid, pr, st = cpu.prepare_hierarchical(
+            g["svo_det_sampled_point_depth"], g["svo_det_sampled_point_distance"],
+            g["svo_det_sampled_point_voxel_idx"], g["render_probs"], **kw)
+        assert np.array_equal(lo, gh["%s_min_depth" % tag])
+        assert np.array_equal(hi, gh["%s_max_depth" % tag])
+        assert np.array_equal(vid, gh["%s_intersected_voxel_idx" % tag])
+        assert np.array_equal(st, gh["%s_steps" % tag])
+        # a sequential sum adds the ~1e-5 padding terms onto ~1 one by one; torch's
+        # pairwise sum keeps them apart: ~1e-6 relative
+        np.testing.assert_allclose(pr, gh["%s_probs" % tag], rtol=5e-6, atol=0)
+        I, L, U = (gh["%s_%s" % (tag, k)] for k in ["intersected_voxel_idx", "min_depth", "max_depth"])
+        P, S = gh["%s_probs" % tag], gh["%s_steps" % tag]
+        N, Hh = I.shape
+        M = int(np.ceil(S).max()) + Hh
+        si, sd, ss = cpu.inverse_cdf_op(I, L, U, P, S, np.full((N, M), 0.5, np.float32))
+        ref = gh["%s_fine_sampled_point_voxel_idx" % tag]
+        assert np.array_equal(si, ref)
+        m = ref != -1
+        assert np.array_equal(sd[m], gh["%s_fine_sampled_point_depth" % tag][m])
+        assert np.array_equal(np.maximum(ss[m], 0), gh["%s_fine_sampled_point_distance" % tag][m])

@@ -1,8 +1,10 @@
 """Serving: continuous batching of ray chunks of several resident scenes
-under CUDA graphs. Each frame's result is the same rendered alone and in a
-mix of concurrent requests (bit for bit: the same captured kernels run on
-the same chunks), with and without graphs, and close to the synchronising
-full-frame served path."""
+under CUDA graphs, chunks packing pixel ranges (pieces) of several frames of
+a scene. Each frame's result is the same rendered alone and in a mix of
+concurrent requests -- bit for bit: every piece gets its own launch layout,
+so what shares its chunk does not matter -- with and without graphs, under
+an HBM budget that forces pipelines to be released, and close to the
+synchronising full-frame served path."""
 import argparse
 
 import numpy as np
@@ -43,22 +45,46 @@ def test_same_alone_and_in_the_mix(cuda):
     from nsvf_gb300 import ext
     from nsvf_gb300.serving import Server
     store = _store(cuda)
-    server = Server(store, chunk_rays=16384, slots=3, max_inflight=4)
-    mix = server.run(_requests(), real_time=True)
+    server = Server(store, chunk_rays=65536, slots=3, max_inflight=6)
+    mix = server.run(_requests(), real_time=False)
+    assert server.stats["max_frames_per_chunk"] >= 2      # frames shared chunks
     alone = []
     for r in _requests():
         r.arrival = 0.0
         alone += server.run([r], real_time=False)
     ext.check_errors(cuda)
-    assert any(r.n_chunks > 1 for r in mix)
+    assert any(len(r.pieces) > 1 for r in mix)
     for a, b in zip(sorted(mix, key=lambda r: r.rid), sorted(alone, key=lambda r: r.rid)):
         assert torch.equal(a.colors, b.colors), a.rid
         assert torch.equal(a.depths, b.depths), a.rid
         assert a.latency() > 0
-    # the same without CUDA graphs
-    eager = Server(store, chunk_rays=16384, slots=2, max_inflight=4, use_graph=False)
-    for r, a in zip(eager.run(_requests(), real_time=False), sorted(mix, key=lambda r: r.rid)):
+    # the same in real time, and without CUDA graphs
+    rt = Server(store, chunk_rays=65536, slots=3, max_inflight=4)
+    for r, a in zip(sorted(rt.run(_requests(), real_time=True), key=lambda r: r.rid),
+                    sorted(mix, key=lambda r: r.rid)):
         assert torch.equal(r.colors, a.colors)
+    eager = Server(store, chunk_rays=65536, slots=2, max_inflight=4, use_graph=False)
+    for r, a in zip(sorted(eager.run(_requests(), real_time=False), key=lambda r: r.rid),
+                    sorted(mix, key=lambda r: r.rid)):
+        assert torch.equal(r.colors, a.colors)
+
+
+def test_hbm_budget_releases_pipelines(cuda):
+    """A budget with room for the scenes and one pipeline: slots take turns,
+    idle pipelines are released to make room, and the frames are the same as
+    with room for all."""
+    from nsvf_gb300.serving import ChunkPipeline, Server
+    store = _store(cuda)
+    big = max(ChunkPipeline.estimate_bytes(sc, 65536, 128) for sc in store.scenes.values())
+    tight = Server(store, chunk_rays=65536, slots=3, max_inflight=6,
+                   hbm_budget_bytes=store.used + big + (1 << 20))
+    roomy = Server(store, chunk_rays=65536, slots=3, max_inflight=6)
+    a = sorted(tight.run(_requests(seed=5), real_time=False), key=lambda r: r.rid)
+    b = sorted(roomy.run(_requests(seed=5), real_time=False), key=lambda r: r.rid)
+    assert tight.stats["pipelines_released"] > 0
+    assert tight.device_bytes() <= tight.hbm_budget
+    for x, y in zip(a, b):
+        assert torch.equal(x.colors, y.colors) and torch.equal(x.depths, y.depths)
 
 
 def test_served_chunks_match_full_frame(cuda):

@@ -54,6 +54,8 @@ def test_training_step_matches_reference_autograd(golden_train, cuda):
     target = torch.from_numpy(go["target"]).to(cuda)
     samples = train.sample_rays(enc, ro, rd)
     assert bool(samples[0].all())
+    # the same samples (the batch holds no ray that enters two voxels at the
+    # same depth, where the reference's unstable sort is free to differ)
     assert int(samples[1].ne(-1).sum()) == int(go["n_samples"])
     torch.cuda.reset_peak_memory_stats(cuda)
     base = torch.cuda.memory_allocated(cuda)
