@@ -74,6 +74,59 @@ int nsvf_svo_intersect(int b, int b_pts, int n, int m, float voxelsize, int n_ma
                        const int32_t *children, int32_t *idx, float *min_depth,
                        float *max_depth, int32_t *err, void *workspace, void *stream);
 
+/* svo_pack: writes the packed copy of ONE octree (points [n, 3], children
+ * [n, 9]) that the sorted traversal reads into `workspace`
+ * (nsvf_svo_workspace_bytes(1, n) bytes, 16-byte aligned), so that
+ * nsvf_svo_intersect_grid can reuse it across calls. The packing step of
+ * fairnr/clib/__init__.py:101-111 (the reference copies the octree once per
+ * ray block on every call). */
+int nsvf_svo_pack(int n, float voxelsize, const float *points, const int32_t *children,
+                  void *workspace, void *stream);
+
+/* svo_grid_build: HOST function (host pointers, no GPU needed). Builds the
+ * leaf-grid form of ONE octree (points [n, 3], children [n, 9], both host
+ * memory) for nsvf_svo_intersect_grid: the leaves' FP32 centres as per-axis
+ * grid lines, a 4x4x4-brick occupancy bitmap with prefix counts, each leaf's
+ * rank in the depth-first visiting order of
+ * fairnr/clib/src/intersect_gpu.cu:200-235, and a flag on leaves whose
+ * ancestors' FP32 faces do not all enclose their own. Writes the blob into
+ * `grid` (`capacity` bytes); `*bytes` (may be NULL) gets its size. Returns
+ * NSVF_ERR_CAPACITY with `*bytes` set when `grid` is NULL or too small (call
+ * once to size, once to fill), and NSVF_ERR_OCTREE when the tree is not in
+ * leaf-grid form: a child id >= n, a node reached twice, a node deeper than
+ * 15 levels, a size < 1, two different centres on one grid line, two leaves
+ * in one cell, or more than 65,536 grid lines on an axis. Such trees go
+ * through nsvf_svo_intersect_sorted, which reports the malformed ones. Copy
+ * the blob to device memory (16-byte aligned) for the intersection. */
+int nsvf_svo_grid_build(int n, float voxelsize, const float *points, const int32_t *children,
+                        void *grid, int64_t capacity, int64_t *bytes);
+/* out[6] = grid lines x, y, z, leaves, flagged leaves, nodes of a HOST copy
+ * of a blob. */
+int nsvf_svo_grid_info(const void *grid_host, int32_t *out);
+/* Device bytes of the ray list nsvf_svo_intersect_grid needs for `rays`. */
+int64_t nsvf_svo_grid_list_bytes(int64_t rays);
+
+/* svo_intersect_grid: the outputs of nsvf_svo_intersect_sorted (b = 1, one
+ * octree: rays [rays, 3]; idx/min_depth/max_depth [rays, n_max], hits
+ * [rays]), bit for bit, replacing svo_intersect + the encoder's sort
+ * (fairnr/clib/src/intersect_gpu.cu:170-237, fairnr/modules/encoder.py:
+ * 518-524) by a sweep of each ray across the grid of leaf cells, one thread
+ * per ray, in order of depth. `grid` is the device copy of the
+ * nsvf_svo_grid_build blob, `info` (HOST int32[6]) its nsvf_svo_grid_info,
+ * `packed` the nsvf_svo_pack workspace of the
+ * same octree, `list_ws` nsvf_svo_grid_list_bytes(rays) bytes of device
+ * scratch (16-byte aligned). Rays the sweep leaves to the depth-first search
+ * are listed there and traversed by it in a second launch: rays with a zero
+ * direction component or with a hit beyond depth 10000. Rays with more than
+ * n_max hits keep, like the search, the first n_max leaves in visiting
+ * order. n_max <= 128. Calls that share `list_ws` must not overlap on the
+ * GPU. */
+int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
+                            const float *ray_start, const float *ray_dir, const float *points,
+                            const int32_t *children, const void *grid, const int32_t *info,
+                            const void *packed, void *list_ws, int32_t *idx, float *min_depth,
+                            float *max_depth, uint8_t *hits, int32_t *err, void *stream);
+
 /* svo_intersect_noalloc: has no counterpart in the reference. The same
  * computation and outputs as nsvf_svo_intersect, for callers that cannot
  * allocate device memory on the call path (a real-time render loop, or a host

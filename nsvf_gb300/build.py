@@ -5,9 +5,10 @@ every source of nsvf_gb300/csrc/ with nvcc, one process per file in
 parallel, into nsvf_gb300/_build/, and links
 nsvf_gb300/_build/libnsvf_gb300.so. Only sm_103a code is generated.
 
-Geometry kernels (intersection, sampling) are compiled with -fmad=false:
-they spell out every fused multiply-add the reference's default nvcc build
-contracts, so their FP32 results are reproducible on a CPU.
+Geometry kernels (intersection, sampling) are compiled with -fmad=false
+(and their host code with -ffp-contract=off): they spell out every fused
+multiply-add the reference's default nvcc build contracts, so their FP32
+results are reproducible on a CPU, x86 or Arm.
 """
 import os
 import subprocess
@@ -22,7 +23,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "-I", os.path.join(HERE, "..", "include")]
-EXACT_FP = {"intersect.cu", "sample.cu", "chunk.cu", "exact.cu"}
+EXACT_FP = {"intersect.cu", "sample.cu", "chunk.cu", "exact.cu", "svo_grid.cu"}
 
 
 def sources():
@@ -39,7 +40,7 @@ def _compile(src):
     obj = os.path.join(BUILD, src + ".o")
     cmd = [NVCC] + ARCH + COMMON
     if src in EXACT_FP:
-        cmd += ["-fmad=false"]
+        cmd += ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
     if src.endswith(".cpp"):
         cmd += ["-x", "c++"]
     cmd += ["-c", os.path.join(CSRC, src), "-o", obj]

@@ -277,7 +277,8 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
     int64_t rays, int m, int b_pts, int n, int n_max, const float *__restrict__ ray_start,
     const float *__restrict__ ray_dir, const float4 *__restrict__ cbox_all,
     const int32_t *__restrict__ kids_all, int32_t *__restrict__ idx, float *__restrict__ min_depth,
-    float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err) {
+    float *__restrict__ max_depth, uint8_t *__restrict__ hits, int32_t *__restrict__ err,
+    const int32_t *__restrict__ ray_list, const int32_t *__restrict__ n_list) {
   // per ray and stack level: the expanded node's 8 child ids (lane j writes
   // children j + P c) and the node's id
   __shared__ int s_child[kSvoLevels * kRaysPerBlock * 8];
@@ -288,8 +289,17 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   const int g0 = lane - j;                           // the group's first lane
   const uint32_t gshift = (uint32_t)(kLanesPerRay * grp);
   const int slot = warp * kRaysPerWarp + grp;        // ray slot in the block
-  const int64_t r = (int64_t)blockIdx.x * kRaysPerBlock + slot;
-  const bool live = r < rays;
+  // Ray-list mode (ray_list != NULL): slot q of the launch takes ray
+  // ray_list[q] for q < *n_list; blocks past the list return at once (the
+  // test is the same for the whole block).
+  int64_t r = (int64_t)blockIdx.x * kRaysPerBlock + slot;
+  bool live = r < rays;
+  if (ray_list) {
+    const int64_t nl = *n_list;
+    if ((int64_t)blockIdx.x * kRaysPerBlock >= nl) return;
+    live = r < nl;
+    r = live ? (int64_t)ray_list[r] : 0;
+  }
   bool bad = false;
   int cnt = 0;
 
@@ -483,8 +493,8 @@ __global__ void __launch_bounds__(kRayBlock) svo_kernel(
   for (int q = 0; q < kRaysPerWarp; ++q) {
     int cq = __shfl_sync(0xffffffffu, cnt, q * kLanesPerRay);
     bool lq = __shfl_sync(0xffffffffu, (int)live, q * kLanesPerRay) != 0;
+    const int64_t rq = __shfl_sync(0xffffffffu, (long long)r, q * kLanesPerRay);
     if (!lq) continue;
-    int64_t rq = (int64_t)blockIdx.x * kRaysPerBlock + warp * kRaysPerWarp + q;
     int32_t *Iq = idx + rq * n_max;
     float *Lq = min_depth + rq * n_max, *Hq = max_depth + rq * n_max;
     if (SORTED && cq > 0) {
@@ -724,11 +734,11 @@ static int svo_launch(bool sorted, int b, int b_pts, int n, int m, float voxelsi
   if (sorted)
     svo_kernel<true><<<nsvf_grid(rays, kRaysPerBlock), kRayBlock, 0, s>>>(
         rays, m, b_pts, n, n_max, ray_start, ray_dir, cbox, kids, idx, min_depth, max_depth, hits,
-        err);
+        err, nullptr, nullptr);
   else
     svo_kernel<false><<<nsvf_grid(rays, kRaysPerBlock), kRayBlock, 0, s>>>(
         rays, m, b_pts, n, n_max, ray_start, ray_dir, cbox, kids, idx, min_depth, max_depth, hits,
-        err);
+        err, nullptr, nullptr);
   return nsvf_launch_status();
 }
 
@@ -748,6 +758,39 @@ int nsvf_svo_intersect_sorted(int b, int b_pts, int n, int m, float voxelsize, i
   return svo_launch(true, b, b_pts, n, m, voxelsize, n_max, ray_start, ray_dir, points, children,
                     idx, min_depth, max_depth, hits, err, workspace, stream);
 }
+
+int nsvf_svo_pack(int n, float voxelsize, const float *points, const int32_t *children,
+                  void *workspace, void *stream) {
+  if (n < 1 || !points || !children || !workspace || (((uintptr_t)workspace) & 15))
+    return NSVF_ERR_INVALID;
+  float4 *cbox = (float4 *)workspace;
+  int32_t *kids = (int32_t *)(cbox + ((int64_t)n * 8 + 1));
+  pack_octree_kernel<<<nsvf_grid((int64_t)n * 8, 256), 256, 0, (cudaStream_t)stream>>>(
+      n, n, voxelsize * 0.5f, points, children, cbox, kids);
+  return nsvf_launch_status();
+}
+
+}  // extern "C"
+
+// The sorted traversal over a device-side list of rays (one octree, packed
+// by nsvf_svo_pack into `packed`): the leaf-grid intersection's fallback for
+// the rays it leaves to the depth-first search. The launch covers `cap` list
+// slots; blocks past the list's device-side length return at once.
+int nsvf_svo_sorted_list_launch(int64_t rays, int64_t cap, int n, int n_max,
+                                const float *ray_start, const float *ray_dir, const void *packed,
+                                const int32_t *ray_list, const int32_t *n_list, int32_t *idx,
+                                float *min_depth, float *max_depth, uint8_t *hits, int32_t *err,
+                                cudaStream_t stream) {
+  if (cap <= 0) return NSVF_OK;
+  const float4 *cbox = (const float4 *)packed;
+  const int32_t *kids = (const int32_t *)(cbox + ((int64_t)n * 8 + 1));
+  svo_kernel<true><<<nsvf_grid(cap, kRaysPerBlock), kRayBlock, 0, stream>>>(
+      rays, (int)(rays > 0x7fffffff ? 0x7fffffff : rays), 1, n, n_max, ray_start, ray_dir, cbox,
+      kids, idx, min_depth, max_depth, hits, err, ray_list, n_list);
+  return nsvf_launch_status();
+}
+
+extern "C" {
 
 // ------------------------------------------------------------------------
 // SVO intersection without any device allocation.

@@ -1,0 +1,673 @@
+// Sparse-voxel-octree intersection in leaf-grid form: the same sorted hit
+// lists as the depth-first traversal (nsvf_svo_intersect_sorted), bit for
+// bit, from a sweep along the ray over the grid of leaf voxels.
+//
+// What the depth-first search computes (fairnr/clib/src/intersect_gpu.cu:
+// 170-237, then the encoder's stable depth sort, fairnr/modules/encoder.py:
+// 518-524): the leaves whose slab test hits and whose every ancestor's slab
+// test hits, the first n_max of them in visiting order (children 7..0), then
+// ordered by (min_depth, visiting order).
+//
+// The leaf-grid form replaces the tree walk by three facts checked once per
+// octree on the host (nsvf_svo_grid_build):
+//
+// 1. Leaves sit on a grid of cells: along each axis, every leaf with grid
+//    index i has the same FP32 centre coordinate tab[i], and tab increases
+//    with i. A leaf's slab test then splits per axis: along axis a the ray is
+//    inside cell i for t in [E_a(i), F_a(i)], with exactly the products the
+//    slab test takes, and the leaf (i, j, k) is hit iff
+//    max(0, E_x(i), E_y(j), E_z(k)) <= min(1e5, F_x(i), F_y(j), F_z(k)).
+//    In travel order along an axis both E and F are non-decreasing (rounding
+//    is monotone), so at each t the cells "active" on an axis form a range.
+// 2. Ancestors: where every ancestor's FP32 faces (c - h, c + h) enclose the
+//    leaf's, a leaf hit implies every ancestor hit (the slab arithmetic is
+//    monotone in the face coordinate). Leaves without that property are
+//    flagged, and their ancestors' slab tests run explicitly on a hit.
+// 3. Order: each leaf's rank in the depth-first visiting order is stored, to
+//    order hits with equal min_depth.
+//
+// The sweep (one thread per ray) processes the cell-entry events of the
+// three axes in t order. At an event t, the cells entered at t are new; every
+// hit triple with a new member is "born" at t, which is exactly its
+// min_depth. Triples are produced in non-decreasing min_depth, each once;
+// equal-t triples are ordered by visiting rank. A 4x4x4 brick bitmap with
+// prefix counts maps an occupied cell to its leaf. Steps per ray are the grid
+// cells the ray crosses (44 on average on the c2 frame), against the
+// hundreds of node expansions of the tree walk.
+//
+// Rays with more than n_max hits: the search stops after the first n_max
+// leaves in visiting order. The sweep keeps, of the hits met so far, the
+// n_max with the smallest visiting ranks (a smaller rank replaces the row's
+// largest), so the row ends as that set in (min_depth, rank) order.
+//
+// Rays the sweep does not take go to the depth-first kernel, through a list:
+// rays with a zero direction component (the slab test's non-finite branch)
+// and rays with a hit beyond depth 10000 (the sort puts those after the
+// misses).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+int nsvf_svo_sorted_list_launch(int64_t rays, int64_t cap, int n, int n_max,
+                                const float *ray_start, const float *ray_dir, const void *packed,
+                                const int32_t *ray_list, const int32_t *n_list, int32_t *idx,
+                                float *min_depth, float *max_depth, uint8_t *hits, int32_t *err,
+                                cudaStream_t stream);
+
+namespace {
+
+constexpr int32_t kGridMagic = 0x3147534e;   // "NSG1"
+constexpr int kGridMaxAxis = 1 << 16;
+constexpr int64_t kGridMaxBricks = (int64_t)1 << 27;
+constexpr int kGridMaxLevels = 16;            // the depth-first kernel's stack levels
+
+// Blob layout: header, per-axis centre tables (x, y, z), bricks (occupancy
+// bits of 4x4x4 cells + exclusive prefix count of leaves), leaves in brick
+// order (node id, visiting rank | flag << 31), visiting rank per node,
+// parent per node. Every section starts on a 16-byte boundary.
+struct GridHeader {
+  int32_t magic;
+  int32_t n[3];
+  int32_t nb[3];
+  int32_t n_leaves;
+  int32_t n_nodes;
+  int32_t n_flagged;
+  float hv;
+  int32_t pad[5];
+};
+static_assert(sizeof(GridHeader) == 64, "64-byte header");
+
+struct GridLayout {
+  int64_t tab, brick, leaf, rank, parent, bytes;
+};
+
+__host__ __device__ inline int64_t al16(int64_t x) { return (x + 15) & ~(int64_t)15; }
+
+__host__ __device__ inline GridLayout grid_layout(const int32_t n[3], const int32_t nb[3],
+                                                  int32_t n_leaves, int32_t n_nodes) {
+  GridLayout L;
+  L.tab = (int64_t)sizeof(GridHeader);
+  L.brick = al16(L.tab + 4 * ((int64_t)n[0] + n[1] + n[2]));
+  L.leaf = L.brick + 16 * (int64_t)nb[0] * nb[1] * nb[2];
+  L.rank = al16(L.leaf + 8 * (int64_t)n_leaves);
+  L.parent = al16(L.rank + 4 * (int64_t)n_nodes);
+  L.bytes = al16(L.parent + 4 * (int64_t)n_nodes);
+  return L;
+}
+
+// ------------------------------------------------------------ host build --
+
+struct GridPlan {
+  GridHeader h;
+  std::vector<float> tab[3];
+  std::vector<uint64_t> bits;
+  std::vector<int32_t> prefix;
+  std::vector<int32_t> leaf_id, leaf_rank;
+  std::vector<int32_t> rank, parent;
+};
+
+// Analyses an octree: NSVF_OK and a plan, NSVF_ERR_OCTREE when the tree is
+// not in leaf-grid form (the caller then uses the depth-first kernel, which
+// also reports malformed trees).
+int grid_plan(int n, float voxelsize, const float *P, const int32_t *C, GridPlan &G) {
+  if (n < 1 || !P || !C || !(voxelsize > 0.0f)) return NSVF_ERR_INVALID;
+  const float hv = voxelsize * 0.5f;
+  G.rank.assign(n, -1);
+  G.parent.assign(n, -1);
+  std::vector<uint8_t> flag(n, 0);
+  std::vector<int32_t> leaves;
+  struct Item {
+    int32_t k, depth;
+    float lo[3], hi[3];   // tightest ancestor faces
+  };
+  std::vector<Item> stack;
+  Item root;
+  root.k = n - 1;
+  root.depth = 0;
+  for (int a = 0; a < 3; ++a) {
+    root.lo[a] = -INFINITY;
+    root.hi[a] = INFINITY;
+  }
+  stack.push_back(root);
+  int32_t visited = 0;
+  while (!stack.empty()) {
+    Item it = stack.back();
+    stack.pop_back();
+    const int32_t k = it.k;
+    if (G.rank[k] >= 0 || it.depth >= kGridMaxLevels) return NSVF_ERR_OCTREE;
+    G.rank[k] = visited++;
+    const int32_t size = C[(int64_t)k * 9 + 8];
+    if (size < 1) return NSVF_ERR_OCTREE;
+    const float h = hv * (float)size;     // as the packed octree computes it
+    float flo[3], fhi[3];
+    bool inside = true;
+    for (int a = 0; a < 3; ++a) {
+      const float c = P[(int64_t)k * 3 + a];
+      if (!std::isfinite(c)) return NSVF_ERR_OCTREE;
+      flo[a] = c - h;
+      fhi[a] = c + h;
+      if (flo[a] < it.lo[a] || fhi[a] > it.hi[a]) inside = false;
+    }
+    if (size == 1) {
+      flag[k] = !inside;
+      leaves.push_back(k);
+      continue;
+    }
+    for (int u = 0; u < 8; ++u) {
+      const int32_t ch = C[(int64_t)k * 9 + u];
+      if (ch >= n) return NSVF_ERR_OCTREE;
+      if (ch > -1) {
+        Item c;
+        c.k = ch;
+        c.depth = it.depth + 1;
+        for (int a = 0; a < 3; ++a) {
+          c.lo[a] = std::max(it.lo[a], flo[a]);
+          c.hi[a] = std::min(it.hi[a], fhi[a]);
+        }
+        G.parent[ch] = k;
+        stack.push_back(c);
+      }
+    }
+  }
+  if (leaves.empty()) return NSVF_ERR_OCTREE;
+  const size_t L = leaves.size();
+  std::vector<int32_t> cell[3];
+  for (int a = 0; a < 3; ++a) {
+    double mn = INFINITY, mx = -INFINITY;
+    for (int32_t k : leaves) {
+      mn = std::min(mn, (double)P[(int64_t)k * 3 + a]);
+      mx = std::max(mx, (double)P[(int64_t)k * 3 + a]);
+    }
+    const double cells = std::floor((mx - mn) / (double)voxelsize + 0.5) + 1.0;
+    if (!(cells >= 1.0 && cells <= (double)kGridMaxAxis)) return NSVF_ERR_OCTREE;
+    const int32_t na = (int32_t)cells;
+    std::vector<float> &t = G.tab[a];
+    t.assign(na, NAN);
+    cell[a].resize(L);
+    for (size_t q = 0; q < L; ++q) {
+      const float c = P[(int64_t)leaves[q] * 3 + a];
+      const int64_t i = (int64_t)std::floor(((double)c - mn) / (double)voxelsize + 0.5);
+      if (i < 0 || i >= na) return NSVF_ERR_OCTREE;
+      if (std::isnan(t[i])) t[i] = c;
+      else if (t[i] != c) return NSVF_ERR_OCTREE;   // two centres on one grid line
+      cell[a][q] = (int32_t)i;
+    }
+    // grid lines without a leaf: any non-decreasing value keeps the sweep
+    // exact (no leaf sits on them)
+    float prev = -INFINITY;
+    for (int32_t i = 0; i < na; ++i) {
+      if (std::isnan(t[i])) t[i] = std::max(prev, (float)(mn + (double)i * (double)voxelsize));
+      else if (!(t[i] > prev)) return NSVF_ERR_OCTREE;
+      prev = t[i];
+    }
+    G.h.n[a] = na;
+    G.h.nb[a] = (na + 3) / 4;
+  }
+  const int64_t nbricks = (int64_t)G.h.nb[0] * G.h.nb[1] * G.h.nb[2];
+  if (nbricks > kGridMaxBricks) return NSVF_ERR_OCTREE;
+  G.bits.assign(nbricks, 0);
+  auto brick_of = [&](size_t q, int64_t &w, int &b) {
+    const int32_t i = cell[0][q], j = cell[1][q], k = cell[2][q];
+    w = ((int64_t)(k >> 2) * G.h.nb[1] + (j >> 2)) * G.h.nb[0] + (i >> 2);
+    b = ((k & 3) * 4 + (j & 3)) * 4 + (i & 3);
+  };
+  for (size_t q = 0; q < L; ++q) {
+    int64_t w;
+    int b;
+    brick_of(q, w, b);
+    if ((G.bits[w] >> b) & 1u) return NSVF_ERR_OCTREE;   // two leaves in one cell
+    G.bits[w] |= (uint64_t)1 << b;
+  }
+  G.prefix.assign(nbricks, 0);
+  int64_t acc = 0;
+  for (int64_t w = 0; w < nbricks; ++w) {
+    G.prefix[w] = (int32_t)acc;
+    acc += __builtin_popcountll(G.bits[w]);
+  }
+  G.leaf_id.assign(L, -1);
+  G.leaf_rank.assign(L, 0);
+  int32_t n_flagged = 0;
+  for (size_t q = 0; q < L; ++q) {
+    int64_t w;
+    int b;
+    brick_of(q, w, b);
+    const int64_t rk = G.prefix[w] + __builtin_popcountll(G.bits[w] & (((uint64_t)1 << b) - 1));
+    const int32_t k = leaves[q];
+    G.leaf_id[rk] = k;
+    G.leaf_rank[rk] = G.rank[k] | (flag[k] ? (int32_t)0x80000000u : 0);
+    n_flagged += flag[k];
+  }
+  G.h.magic = kGridMagic;
+  G.h.n_leaves = (int32_t)L;
+  G.h.n_nodes = n;
+  G.h.n_flagged = n_flagged;
+  G.h.hv = hv;
+  for (int q = 0; q < 5; ++q) G.h.pad[q] = 0;
+  return NSVF_OK;
+}
+
+// ----------------------------------------------------------- the sweep ----
+
+constexpr int kGridBlock = 128;
+
+// The grid as the kernel sees it: pointers into the device blob and its
+// dimensions, passed by value (kernel parameters live in the constant bank,
+// not in per-thread registers).
+struct GridView {
+  const float *tab[3];            // grid-line centres per axis
+  const ulonglong2 *bricks;       // (occupancy bits, prefix count)
+  const int2 *leaf;               // (node id, visiting rank | flag << 31)
+  const int32_t *rank_of;         // visiting rank per node
+  const int32_t *parent;          // parent per node
+  const float *points;            // octree node centres [n, 3]
+  const int32_t *children;        // [n, 9]
+  int32_t n[3], nb[3];
+  float hv;
+};
+
+// Per ray: origin, reciprocal direction, and the signed half size (the sign
+// of the direction: travel order along the axis).
+struct Sweep {
+  float o[3], inv[3], sh[3];
+};
+
+// Entry (clamped at 0, as the slab test's running max) and exit of the ray
+// along axis a through the cell at travel position u.
+__device__ __forceinline__ float cell_centre(const GridView &G, const Sweep &S, int a, int u) {
+  return __ldg(G.tab[a] + (S.sh[a] > 0.0f ? u : G.n[a] - 1 - u));
+}
+__device__ __forceinline__ float entry_t(const GridView &G, const Sweep &S, int a, int u) {
+  const float c = cell_centre(G, S, a, u);
+  const float l = __fmul_rn(__fsub_rn(__fsub_rn(c, S.sh[a]), S.o[a]), S.inv[a]);
+  return fmaxf(0.0f, __fadd_rn(l, 0.0f));
+}
+__device__ __forceinline__ float exit_t(const GridView &G, const Sweep &S, int a, int u) {
+  const float c = cell_centre(G, S, a, u);
+  return __fmul_rn(__fsub_rn(__fadd_rn(c, S.sh[a]), S.o[a]), S.inv[a]);
+}
+
+// The rare paths of the sweep, kept out of its loop.
+// Every ancestor of `leaf` passes its slab test (the depth-first kernel's
+// test, on the ancestor's box).
+__device__ __noinline__ bool ancestors_hit(const GridView G, float ox, float oy, float oz,
+                                           float ix, float iy, float iz, int32_t leaf) {
+  const float sx = ix >= 0.0f ? 1.0f : -1.0f, sy = iy >= 0.0f ? 1.0f : -1.0f,
+              sz = iz >= 0.0f ? 1.0f : -1.0f;
+  int p = __ldg(G.parent + leaf);
+  for (int lv = 0; lv < kGridMaxLevels && p >= 0; ++lv) {
+    const float hp = fabsf(__fmul_rn(G.hv, (float)__ldg(G.children + (int64_t)p * 9 + 8)));
+    float a0, a1;
+    if (!nsvf_slab_fast(ox, oy, oz, ix, iy, iz, sx, sy, sz, __ldg(G.points + (int64_t)p * 3 + 0),
+                        __ldg(G.points + (int64_t)p * 3 + 1),
+                        __ldg(G.points + (int64_t)p * 3 + 2), hp, a0, a1))
+      return false;
+    p = __ldg(G.parent + p);
+  }
+  return true;
+}
+
+// Largest visiting rank in a full row, and its slot.
+// (returned as rank << 8 | slot; n_max <= 128)
+__device__ __noinline__ int64_t row_largest_rank(const int32_t *I, int n_max,
+                                                 const int32_t *__restrict__ rank_of) {
+  int32_t best = -1;
+  int pos = 0;
+  for (int q = 0; q < n_max; ++q) {
+    const int32_t rq = __ldg(rank_of + I[q]);
+    if (rq > best) { best = rq; pos = q; }
+  }
+  return ((int64_t)best << 8) | pos;
+}
+
+// Removes slot `pos` of a full row; the rest keeps its order.
+__device__ __noinline__ void row_remove(int32_t *I, float *LO, float *HI, int n_max, int pos) {
+  for (int q = pos; q + 1 < n_max; ++q) {
+    I[q] = I[q + 1];
+    LO[q] = LO[q + 1];
+    HI[q] = HI[q + 1];
+  }
+}
+
+// (No minimum of resident blocks: capping the registers at 80 or 64 spills
+// and was 12 % / 26 % slower on the c2 frame.)
+__global__ void __launch_bounds__(kGridBlock) svo_grid_kernel(
+    int64_t rays, int n_max, const float *__restrict__ ray_start,
+    const float *__restrict__ ray_dir, const GridView G, int32_t *__restrict__ idx,
+    float *__restrict__ min_depth, float *__restrict__ max_depth, uint8_t *__restrict__ hits,
+    int32_t *__restrict__ list, int32_t *__restrict__ n_list) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = r < rays;
+  const int64_t rr = live ? r : 0;
+  Sweep S;
+  bool fast = true;
+  float dir[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S.o[a] = ray_start[rr * 3 + a];
+    dir[a] = ray_dir[rr * 3 + a];
+    S.inv[a] = nsvf_rcp(dir[a]);
+    fast = fast && isfinite(S.inv[a]);
+    S.sh[a] = S.inv[a] >= 0.0f ? G.hv : -G.hv;
+  }
+  int32_t *I = idx + rr * n_max;
+  float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
+  int cnt = 0;
+  bool to_list = live && !fast;
+
+  if (live && fast) {
+    // the first time inside the grid's slab on every axis, and the cells
+    // active then: the first cell (in travel order) not yet left, and the
+    // first not yet entered
+    float t = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) t = fmaxf(t, entry_t(G, S, a, 0));
+    bool dead = !(t <= 100000.0f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dead = dead || exit_t(G, S, a, G.n[a] - 1) < t;
+    int old[3], nxt[3], ns[3];
+    float f_old[3], e_nxt[3], f_new[3];   // exits of the first and last active cells
+    if (!dead) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        // estimate, then correct with the exact exits
+        const float c0 = __ldg(G.tab[a]);
+        const float x = dir[a] * t + S.o[a];
+        float fi = floorf((x - (c0 - G.hv)) / (2.0f * G.hv));
+        fi = fminf(fmaxf(fi, 0.0f), (float)(G.n[a] - 1));
+        int u = S.sh[a] > 0.0f ? (int)fi : G.n[a] - 1 - (int)fi;
+        while (u > 0 && exit_t(G, S, a, u - 1) >= t) --u;
+        while (exit_t(G, S, a, u) < t) ++u;            // ends: the last cell's exit >= t
+        old[a] = u;
+        f_old[a] = exit_t(G, S, a, u);
+        int v = u;
+        float e = entry_t(G, S, a, v);
+        while (e <= t) {
+          ++v;
+          if (v >= G.n[a]) { e = INFINITY; break; }
+          e = entry_t(G, S, a, v);
+        }
+        nxt[a] = v;
+        e_nxt[a] = e;
+        f_new[a] = v > u ? exit_t(G, S, a, v - 1) : f_old[a];
+        ns[a] = u;                                   // the first event: every active cell is new
+      }
+    }
+    int64_t cached = -1;
+    ulonglong2 brick = make_ulonglong2(0, 0);
+    int64_t row_max = -1;   // a full row's largest rank << 8 | its slot (-1: not known)
+    // Visits the cell at travel positions (ux, uy, uz), born at t, with the
+    // exits fx, fy, fz: emits its leaf if there is one.
+    auto visit = [&](int ux, int uy, int uz, float fx, float fy, float fz) {
+      const int gi = S.sh[0] > 0.0f ? ux : G.n[0] - 1 - ux;
+      const int gj = S.sh[1] > 0.0f ? uy : G.n[1] - 1 - uy;
+      const int gk = S.sh[2] > 0.0f ? uz : G.n[2] - 1 - uz;
+      const int64_t w = ((int64_t)(gk >> 2) * G.nb[1] + (gj >> 2)) * G.nb[0] + (gi >> 2);
+      const int bit = ((gk & 3) * 4 + (gj & 3)) * 4 + (gi & 3);
+      if (w != cached) {
+        brick = __ldg(G.bricks + w);
+        cached = w;
+      }
+      if (!((brick.x >> bit) & 1ull)) return;
+      const int64_t rk = (int64_t)brick.y + __popcll(brick.x & ((1ull << bit) - 1ull));
+      const int2 lf = __ldg(G.leaf + rk);
+      float hi = 100000.0f;
+      hi = (fx < hi) ? fx : hi;
+      hi = (fy < hi) ? fy : hi;
+      hi = (fz < hi) ? fz : hi;
+      // a flagged leaf: its ancestors' faces do not all enclose its own
+      if (lf.y < 0 && !ancestors_hit(G, S.o[0], S.o[1], S.o[2], S.inv[0], S.inv[1], S.inv[2],
+                                    lf.x))
+        return;
+      if (t > NSVF_MAX_DEPTH_F) {
+        to_list = true;
+        return;
+      }
+      const int32_t my = lf.y & 0x7fffffff;
+      if (cnt >= n_max) {
+        // The search keeps the first n_max leaves in visiting order: the row
+        // holds the n_max smallest ranks met so far; a smaller rank replaces
+        // the largest (the rest of the row keeps its order).
+        if (row_max < 0) row_max = row_largest_rank(I, n_max, G.rank_of);
+        if (my > (int32_t)(row_max >> 8)) return;
+        row_remove(I, LO, HI, n_max, (int)(row_max & 0xff));
+        cnt = n_max - 1;
+        row_max = -1;                      // rescanned at the next full row
+      }
+      // equal min_depth: visiting order
+      int pos = cnt;
+      while (pos > 0 && LO[pos - 1] == t && __ldg(G.rank_of + I[pos - 1]) > my) {
+        I[pos] = I[pos - 1];
+        LO[pos] = LO[pos - 1];
+        HI[pos] = HI[pos - 1];
+        --pos;
+      }
+      I[pos] = lf.x;
+      LO[pos] = t;
+      HI[pos] = hi;
+      ++cnt;
+    };
+    // each event enters at least one cell (a skip enters the cells at t_j)
+    const int64_t max_events = (int64_t)G.n[0] + G.n[1] + G.n[2] + 2;
+    for (int64_t ev = 0; !dead && !to_list && ev < max_events; ++ev) {
+      if (old[0] < nxt[0] && old[1] < nxt[1] && old[2] < nxt[2]) {
+        // The common event: one axis enters one cell and the other two have
+        // one active cell each: one new triple. (On a dyadic grid a cell's
+        // exit equals the next cell's entry, so the entering axis's previous
+        // cell is still active at t; its triples were born earlier.)
+        const int e0 = nxt[0] - ns[0], e1 = nxt[1] - ns[1], e2 = nxt[2] - ns[2];
+        const int w0 = nxt[0] - old[0], w1 = nxt[1] - old[1], w2 = nxt[2] - old[2];
+        const bool one = (e0 + e1 + e2 == 1) && ((e0 == 1) ? (w1 == 1 && w2 == 1)
+                                                 : (e1 == 1) ? (w0 == 1 && w2 == 1)
+                                                             : (w0 == 1 && w1 == 1));
+        if (one) {
+          visit(e0 ? nxt[0] - 1 : old[0], e1 ? nxt[1] - 1 : old[1], e2 ? nxt[2] - 1 : old[2],
+                e0 ? f_new[0] : f_old[0], e1 ? f_new[1] : f_old[1], e2 ? f_new[2] : f_old[2]);
+        } else {
+          for (int ux = old[0]; ux < nxt[0] && !to_list; ++ux) {
+            const float fx = exit_t(G, S, 0, ux);
+            for (int uy = old[1]; uy < nxt[1] && !to_list; ++uy) {
+              const float fy = exit_t(G, S, 1, uy);
+              for (int uz = old[2]; uz < nxt[2] && !to_list; ++uz) {
+                if (ux < ns[0] && uy < ns[1] && uz < ns[2]) continue;   // born earlier
+                visit(ux, uy, uz, fx, fy, exit_t(G, S, 2, uz));
+              }
+            }
+          }
+        }
+      }
+      if (to_list) break;
+      // Brick skip. After t, an axis's cells that can still form triples are
+      // the active ones with exit > t and the ones not yet entered. When
+      // that is one cell per axis (c) and c's 4x4x4 brick is empty, every
+      // triple born before t_j -- the first entry, on any axis, of a cell
+      // past the brick -- lies in the brick: those events are taken
+      // silently and the sweep resumes at the event t_j.
+      float tn = INFINITY;
+      bool skip = true;
+      int c[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const int wdt = nxt[a] - old[a];
+        c[a] = (wdt == 1) ? old[a] : old[a] + 1;
+        skip = skip && (wdt == 1 || (wdt == 2 && f_old[a] <= t));
+      }
+      if (skip) {
+        const int gi = S.sh[0] > 0.0f ? c[0] : G.n[0] - 1 - c[0];
+        const int gj = S.sh[1] > 0.0f ? c[1] : G.n[1] - 1 - c[1];
+        const int gk = S.sh[2] > 0.0f ? c[2] : G.n[2] - 1 - c[2];
+        const int64_t w = ((int64_t)(gk >> 2) * G.nb[1] + (gj >> 2)) * G.nb[0] + (gi >> 2);
+        if (w != cached) {
+          brick = __ldg(G.bricks + w);
+          cached = w;
+        }
+        skip = brick.x == 0ull;
+        if (skip) {
+          const int g3[3] = {gi, gj, gk};
+          int lim[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const int rem = S.sh[a] > 0.0f ? 4 - (g3[a] & 3) : (g3[a] & 3) + 1;
+            lim[a] = min(G.n[a], c[a] + rem);
+            if (lim[a] < G.n[a]) tn = fminf(tn, entry_t(G, S, a, lim[a]));
+          }
+          if (!(tn <= 100000.0f)) break;          // nothing past this empty brick
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            while (nxt[a] < lim[a] && e_nxt[a] < tn) {
+              f_new[a] = exit_t(G, S, a, nxt[a]);
+              if (old[a] == nxt[a]) f_old[a] = f_new[a];
+              ++nxt[a];
+              e_nxt[a] = nxt[a] < G.n[a] ? entry_t(G, S, a, nxt[a]) : INFINITY;
+            }
+          }
+        }
+      }
+      // the next entry event
+      if (!skip) {
+        tn = fminf(e_nxt[0], fminf(e_nxt[1], e_nxt[2]));
+        if (!(tn <= 100000.0f)) break;
+      }
+      t = tn;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        while (old[a] < nxt[a] && f_old[a] < t) {
+          ++old[a];
+          f_old[a] = old[a] == nxt[a] - 1 ? f_new[a]
+                     : (old[a] < G.n[a] ? exit_t(G, S, a, old[a]) : 0.0f);
+        }
+        dead = dead || old[a] >= G.n[a];
+        ns[a] = nxt[a];
+        while (e_nxt[a] == t) {
+          f_new[a] = exit_t(G, S, a, nxt[a]);
+          if (old[a] == nxt[a]) f_old[a] = f_new[a];
+          ++nxt[a];
+          e_nxt[a] = nxt[a] < G.n[a] ? entry_t(G, S, a, nxt[a]) : INFINITY;
+        }
+      }
+    }
+  }
+  if (to_list) {
+    const int32_t q = atomicAdd(n_list, 1);
+    list[q] = (int32_t)r;
+  } else if (live) {
+    hits[r] = cnt > 0;
+  }
+  // pad the rows (misses: id -1, depths 10000), a warp per row
+  const int lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  const bool pad = live && !to_list;
+  const int64_t r0 = r - lane;
+  for (int q = 0; q < 32; ++q) {
+    const int cq = __shfl_sync(full, cnt, q);
+    if (!__shfl_sync(full, (int)pad, q)) continue;
+    const int64_t rq = r0 + q;
+    for (int l = cq + lane; l < n_max; l += 32) {
+      idx[rq * n_max + l] = -1;
+      min_depth[rq * n_max + l] = NSVF_MAX_DEPTH_F;
+      max_depth[rq * n_max + l] = NSVF_MAX_DEPTH_F;
+    }
+  }
+}
+
+__global__ void zero_kernel(int32_t *p) { *p = 0; }
+
+}  // namespace
+
+extern "C" {
+
+int nsvf_svo_grid_build(int n, float voxelsize, const float *points, const int32_t *children,
+                        void *grid, int64_t capacity, int64_t *bytes) {
+  GridPlan G;
+  const int st = grid_plan(n, voxelsize, points, children, G);
+  if (st != NSVF_OK) return st;
+  const GridLayout L = grid_layout(G.h.n, G.h.nb, G.h.n_leaves, G.h.n_nodes);
+  if (bytes) *bytes = L.bytes;
+  if (!grid || capacity < L.bytes) return NSVF_ERR_CAPACITY;
+  unsigned char *B = static_cast<unsigned char *>(grid);
+  std::fill(B, B + L.bytes, (unsigned char)0);
+  std::copy(reinterpret_cast<const unsigned char *>(&G.h),
+            reinterpret_cast<const unsigned char *>(&G.h) + sizeof(GridHeader), B);
+  float *tab = reinterpret_cast<float *>(B + L.tab);
+  for (int a = 0; a < 3; ++a) {
+    std::copy(G.tab[a].begin(), G.tab[a].end(), tab);
+    tab += G.h.n[a];
+  }
+  uint64_t *br = reinterpret_cast<uint64_t *>(B + L.brick);
+  for (size_t w = 0; w < G.bits.size(); ++w) {
+    br[2 * w] = G.bits[w];
+    br[2 * w + 1] = (uint64_t)(uint32_t)G.prefix[w];
+  }
+  int32_t *lf = reinterpret_cast<int32_t *>(B + L.leaf);
+  for (size_t q = 0; q < G.leaf_id.size(); ++q) {
+    lf[2 * q] = G.leaf_id[q];
+    lf[2 * q + 1] = G.leaf_rank[q];
+  }
+  std::copy(G.rank.begin(), G.rank.end(), reinterpret_cast<int32_t *>(B + L.rank));
+  std::copy(G.parent.begin(), G.parent.end(), reinterpret_cast<int32_t *>(B + L.parent));
+  return NSVF_OK;
+}
+
+int nsvf_svo_grid_info(const void *grid_host, int32_t *out) {
+  if (!grid_host || !out) return NSVF_ERR_INVALID;
+  const GridHeader *h = static_cast<const GridHeader *>(grid_host);
+  if (h->magic != kGridMagic) return NSVF_ERR_INVALID;
+  out[0] = h->n[0];
+  out[1] = h->n[1];
+  out[2] = h->n[2];
+  out[3] = h->n_leaves;
+  out[4] = h->n_flagged;
+  out[5] = h->n_nodes;
+  return NSVF_OK;
+}
+
+int64_t nsvf_svo_grid_list_bytes(int64_t rays) { return 16 + 4 * (rays > 0 ? rays : 0); }
+
+int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
+                            const float *ray_start, const float *ray_dir, const float *points,
+                            const int32_t *children, const void *grid, const int32_t *info,
+                            const void *packed, void *list_ws, int32_t *idx, float *min_depth,
+                            float *max_depth, uint8_t *hits, int32_t *err, void *stream) {
+  if (!info || info[5] != n || info[0] < 1 || info[1] < 1 || info[2] < 1 || info[3] < 1)
+    return NSVF_ERR_INVALID;
+  if (rays < 0 || n < 1 || n_max < 1 || !points || !children || !grid || !packed || !list_ws ||
+      (((uintptr_t)grid) & 15) || (((uintptr_t)packed) & 15) || (((uintptr_t)list_ws) & 15))
+    return NSVF_ERR_INVALID;
+  if (rays == 0) return NSVF_OK;
+  if (!ray_start || !ray_dir || !idx || !min_depth || !max_depth || !hits || n_max > 128 ||
+      rays > 0x7fffffff)
+    return NSVF_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t *n_list = static_cast<int32_t *>(list_ws);
+  int32_t *list = n_list + 4;
+  zero_kernel<<<1, 1, 0, s>>>(n_list);
+  int st = nsvf_launch_status();
+  if (st != NSVF_OK) return st;
+  const unsigned char *B = static_cast<const unsigned char *>(grid);
+  GridView G;
+  int32_t nb[3];
+  for (int a = 0; a < 3; ++a) {
+    G.n[a] = info[a];
+    G.nb[a] = nb[a] = (info[a] + 3) / 4;
+  }
+  const GridLayout L = grid_layout(G.n, nb, info[3], info[5]);
+  G.tab[0] = reinterpret_cast<const float *>(B + L.tab);
+  G.tab[1] = G.tab[0] + G.n[0];
+  G.tab[2] = G.tab[1] + G.n[1];
+  G.bricks = reinterpret_cast<const ulonglong2 *>(B + L.brick);
+  G.leaf = reinterpret_cast<const int2 *>(B + L.leaf);
+  G.rank_of = reinterpret_cast<const int32_t *>(B + L.rank);
+  G.parent = reinterpret_cast<const int32_t *>(B + L.parent);
+  G.points = points;
+  G.children = children;
+  G.hv = voxelsize * 0.5f;
+  svo_grid_kernel<<<nsvf_grid(rays, kGridBlock), kGridBlock, 0, s>>>(
+      rays, n_max, ray_start, ray_dir, G, idx, min_depth, max_depth, hits, list, n_list);
+  st = nsvf_launch_status();
+  if (st != NSVF_OK) return st;
+  return nsvf_svo_sorted_list_launch(rays, rays, n, n_max, ray_start, ray_dir, packed, list,
+                                     n_list, idx, min_depth, max_depth, hits, err, s);
+}
+
+}  // extern "C"

@@ -4,8 +4,10 @@ Same constructor, buffers (points, keys, feats, num_keys, keep, voxel_size,
 step_size, max_hits; fairnr/modules/encoder.py:285-293), `values` embedding
 and methods. The hot methods run on the sm_103a kernels:
 
-* ray_intersect: SVO traversal with the depth sort fused into the kernel
-  (nsvf_svo_intersect_sorted), or the brute-force AABB kernel + sort;
+* ray_intersect: the octree's sorted hit lists from the leaf-grid sweep
+  (nsvf_svo_intersect_grid, one octree), or the SVO traversal with the depth
+  sort fused into the kernel (nsvf_svo_intersect_sorted), or the brute-force
+  AABB kernel + sort;
 * ray_sample:    inverse-CDF sampling kernel (nsvf_gb300.clib);
 * forward:       trilinear interpolation kernel with a hand-written backward;
 * octree build:  native host builder (about 150x faster than the reference's
@@ -93,7 +95,7 @@ class SparseVoxelEncoder(nn.Module):
         self.use_octree = getattr(args, "use_octree", False)
         self.track_max_probs = getattr(args, "track_max_probs", False)
         self._runtime_caches = {"flatten_centers": None, "flatten_children": None,
-                                "max_voxel_probs": None}
+                                "max_voxel_probs": None, "svo_grid": None}
         if shared_values is None and self.embed_dim and self.embed_dim > 0:
             self.values = Embedding(int(num_keys), self.embed_dim, None)
         else:
@@ -141,6 +143,7 @@ class SparseVoxelEncoder(nn.Module):
             centers, children = build_easy_octree(points, self.voxel_size / 2.0)
             self._runtime_caches['flatten_centers'] = centers
             self._runtime_caches['flatten_children'] = children
+            self._runtime_caches['svo_grid'] = None
         if self.track_max_probs:
             self._runtime_caches['max_voxel_probs'] = self.points.new_zeros(self.points.size(0))
 
@@ -159,6 +162,26 @@ class SparseVoxelEncoder(nn.Module):
         if self._runtime_caches['flatten_children'] is None:
             self.reset_runtime_caches()
         return self._runtime_caches['flatten_children']
+
+    def svo_grid(self, centers, children):
+        """The leaf-grid form (ext.SvoGrid) of the octree `centers` [N, 3],
+        `children` [N, 9] of this encoder's states, built once per octree on
+        the first intersection and kept with the runtime caches; None when
+        the states' octree is not this encoder's (checked by value) or not in
+        leaf-grid form."""
+        fc, fch = self.flatten_centers, self.flatten_children
+        if fc is None or centers.shape != fc.shape or children.shape != fch.shape:
+            return None
+        g = self._runtime_caches.get('svo_grid')
+        if g is None or g.centers.device != centers.device:
+            g = ext.SvoGrid(fc.to(centers.device).float().contiguous(),
+                            fch.to(centers.device).int().contiguous(), float(self.voxel_size))
+            self._runtime_caches['svo_grid'] = g
+        if not g.ok or g.voxel_size != float(self.voxel_size):
+            return None
+        if not (torch.equal(centers, g.centers) and torch.equal(children, g.children)):
+            return None
+        return g
 
     @property
     def max_voxel_probs(self):
@@ -203,11 +226,19 @@ class SparseVoxelEncoder(nn.Module):
         ray_start = ray_start.expand_as(ray_dir).contiguous().view(S, V * P, 3).contiguous()
         ray_dir = ray_dir.reshape(S, V * P, 3).contiguous()
         n_max = int(self.max_hits)
+        grid = None
         if self.use_octree and n_max <= 128 and ray_start.dtype == torch.float32:
+            oc = encoder_states['voxel_octree_center_xyz'].float().contiguous()
+            och = encoder_states['voxel_octree_children_idx'].int().contiguous()
+            if S == 1 and oc.dim() == 3 and ray_start.is_cuda:
+                grid = self.svo_grid(oc[0], och[0])
+        if grid is not None:
+            # the leaf-grid sweep: the same sorted lists as the traversal + sort
+            pts_idx, min_depth, max_depth, hits = ext.svo_intersect_grid(
+                grid, ray_start, ray_dir, n_max)
+        elif self.use_octree and n_max <= 128 and ray_start.dtype == torch.float32:
             pts_idx, min_depth, max_depth, hits = ext.svo_intersect_sorted(
-                ray_start, ray_dir, encoder_states['voxel_octree_center_xyz'].float().contiguous(),
-                encoder_states['voxel_octree_children_idx'].int().contiguous(),
-                float(self.voxel_size), n_max)
+                ray_start, ray_dir, oc, och, float(self.voxel_size), n_max)
         else:
             if self.use_octree:
                 pts_idx, min_depth, max_depth = clib.svo_ray_intersect(

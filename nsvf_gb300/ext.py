@@ -14,10 +14,15 @@ The sampling wrappers of nsvf_gb300.clib, which synchronise anyway for their
 output width, check it on every call.
 """
 import contextlib
+import ctypes
 
+import numpy as np
 import torch
 
 from ._lib import LIB, check
+
+NSVF_ERR_OCTREE = -3
+NSVF_ERR_CAPACITY = -4
 
 _err_words = {}
 
@@ -191,6 +196,98 @@ def svo_intersect_sorted(ray_start, ray_dir, points, children, voxelsize, n_max)
                                             _ptr(children), _ptr(idx), _ptr(lo), _ptr(hi),
                                             _ptr(hits), _ptr(error_word(dev)), _ptr(ws),
                                             _stream(ray_start)), "svo_intersect_sorted")
+    return idx, lo, hi, hits.bool()
+
+
+class SvoGrid:
+    """Leaf-grid form of ONE octree on its device, for nsvf_svo_intersect_grid:
+    the blob of nsvf_svo_grid_build (built on the host from a copy of the
+    octree) and the packed octree of nsvf_svo_pack, both kept for the
+    octree's lifetime. `ok` is False when the tree is not in leaf-grid form;
+    callers then use the depth-first kernel (svo_intersect_sorted)."""
+
+    def __init__(self, centers, children, voxel_size):
+        _check_float("centers", centers)
+        _check_int("children", children)
+        _need(centers.dim() == 2 and centers.size(1) == 3 and children.dim() == 2 and
+              children.size(1) == 9 and children.size(0) == centers.size(0),
+              "one octree: centers [N, 3], children [N, 9]")
+        dev = centers.device
+        self.n = int(centers.size(0))
+        self.voxel_size = float(voxel_size)
+        self.centers = centers.contiguous()
+        self.children = children.contiguous()
+        c = self.centers.detach().cpu().numpy()
+        ch = self.children.detach().cpu().numpy()
+        nbytes = ctypes.c_int64(0)
+        st = LIB.nsvf_svo_grid_build(self.n, self.voxel_size, c.ctypes.data, ch.ctypes.data, None,
+                                     0, ctypes.byref(nbytes))
+        self.ok = st == NSVF_ERR_CAPACITY
+        if not self.ok:
+            if st != NSVF_ERR_OCTREE:
+                check(st, "svo_grid_build")
+            return
+        blob = np.zeros(int(nbytes.value), np.uint8)
+        check(LIB.nsvf_svo_grid_build(self.n, self.voxel_size, c.ctypes.data, ch.ctypes.data,
+                                      blob.ctypes.data, blob.size, None), "svo_grid_build")
+        info = np.zeros(6, np.int32)
+        check(LIB.nsvf_svo_grid_info(blob.ctypes.data, info.ctypes.data), "svo_grid_info")
+        self.info = info                     # host int32[6], passed to every call
+        self.lines = tuple(int(v) for v in info[:3])
+        self.n_leaves, self.n_flagged = int(info[3]), int(info[4])
+        self.grid = torch.from_numpy(blob).to(dev)
+        self.packed = _svo_workspace(1, self.n, dev)
+        check(LIB.nsvf_svo_pack(self.n, self.voxel_size, _ptr(self.centers), _ptr(self.children),
+                                _ptr(self.packed), _stream(self.centers)), "svo_pack")
+        self._lists = {}
+
+    def bytes(self):
+        return self.grid.numel() + self.packed.numel() if self.ok else 0
+
+    def list_workspace(self, rays, dev):
+        """The ray-list scratch for calls of `rays` rays on the current stream
+        (kept per stream: calls on one stream run in order)."""
+        key = _stream(self.grid)
+        ws = self._lists.get(key)
+        need = int(LIB.nsvf_svo_grid_list_bytes(rays))
+        if ws is None or ws.numel() < need:
+            ws = torch.empty(need, dtype=torch.uint8, device=dev)
+            self._lists[key] = ws
+        return ws
+
+    def intersect_into(self, R, n_max, ro, rd, idx, lo, hi, hits, stream, list_ws=None,
+                       err=None):
+        """nsvf_svo_intersect_grid on raw device pointers (R rays); `err` (a
+        device int32 tensor) defaults to the device's error word."""
+        ws = list_ws if list_ws is not None else self.list_workspace(R, self.grid.device)
+        if err is None:
+            err = error_word(self.grid.device)
+        check(LIB.nsvf_svo_intersect_grid(
+            R, self.n, self.voxel_size, int(n_max), ro, rd, _ptr(self.centers),
+            _ptr(self.children), _ptr(self.grid), self.info.ctypes.data, _ptr(self.packed),
+            _ptr(ws), idx, lo, hi, hits,
+            _ptr(err), stream), "svo_intersect_grid")
+
+
+def svo_intersect_grid(grid, ray_start, ray_dir, n_max):
+    """Sorted SVO intersection through a SvoGrid: ray_start, ray_dir [R, 3]
+    (or [1, R, 3]) -> the outputs of svo_intersect_sorted with B = 1."""
+    _need(grid.ok, "the octree is not in leaf-grid form")
+    _need(n_max <= 128, "sorted SVO intersection supports n_max <= 128")
+    for n, t in (("ray_start", ray_start), ("ray_dir", ray_dir)):
+        _check_float(n, t)
+    rs = ray_start.reshape(-1, 3).contiguous()
+    rd = ray_dir.reshape(-1, 3).contiguous()
+    _need(rs.shape == rd.shape, "one origin per ray")
+    R = rd.size(0)
+    dev = rd.device
+    idx = torch.empty(1, R, n_max, dtype=torch.int32, device=dev)
+    lo = torch.empty(1, R, n_max, dtype=torch.float32, device=dev)
+    hi = torch.empty(1, R, n_max, dtype=torch.float32, device=dev)
+    hits = torch.empty(1, R, dtype=torch.uint8, device=dev)
+    with _timed("svo_intersect_grid", dev):
+        grid.intersect_into(R, n_max, _ptr(rs), _ptr(rd), _ptr(idx), _ptr(lo), _ptr(hi),
+                            _ptr(hits), _stream(rd))
     return idx, lo, hi, hits.bool()
 
 

@@ -26,10 +26,16 @@ def ray(ray_start, ray_dir, depths):
 
 def discretize_points(voxel_points, voxel_size):
     """Voxel centres/corners -> integer grid coordinates (rounded, relative to
-    the minimum point) and the mean residual."""
+    the minimum point) and the mean residual (fairnr/data/geometry.py:
+    discretize_points). The residuals are the reference's FP32 values; their
+    mean is taken in float64 and rounded once, so it is the same on every
+    device: torch's FP32 mean is not (on CUDA it multiplies the sum by 1/N,
+    one ulp off the exact mean of the c2 shell's identical residuals, and every
+    octree centre, slab distance and sample would inherit that ulp)."""
     minimal = voxel_points.min(dim=0, keepdim=True)[0]
     coords = ((voxel_points - minimal) / voxel_size).round_().long()
-    residual = (voxel_points - coords.type_as(voxel_points) * voxel_size).mean(0, keepdim=True)
+    res = voxel_points - coords.type_as(voxel_points) * voxel_size
+    residual = res.double().mean(0, keepdim=True).to(voxel_points.dtype)
     return coords, residual
 
 

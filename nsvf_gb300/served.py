@@ -2,7 +2,9 @@
 
 For one frame of rays of a resident scene:
 
-1. nsvf_svo_intersect_sorted  -- octree traversal + depth sort (FP32, exact)
+1. nsvf_svo_intersect_grid    -- the octree's hit lists in depth order from a
+   sweep over the leaf grid (FP32, exact; nsvf_svo_intersect_sorted, the
+   depth-first traversal + sort, for trees not in leaf-grid form)
 2. nsvf_compact_hits          -- order-preserving compaction of the hit rays
    (on a torch prefix sum of the hit flags)
 3. nsvf_gather_probs          -- the hit rays' lists and their sampling
@@ -59,6 +61,9 @@ class SceneState:
         self.max_hits = int(encoder.max_hits if max_hits is None else max_hits)
         self.octree_centers = states['voxel_octree_center_xyz'].float().contiguous()
         self.octree_children = states['voxel_octree_children_idx'].int().contiguous()
+        # the leaf-grid form of the octree (host-built once per scene); trees
+        # not in that form go through the depth-first kernel
+        self.svo_grid = ext.SvoGrid(self.octree_centers, self.octree_children, self.voxel_size)
         self.centers = states['voxel_center_xyz'].float().contiguous()
         self.feats = states['voxel_vertex_idx'].int().contiguous()
         self.values = states['voxel_vertex_emb'].detach().float().contiguous()
@@ -94,7 +99,7 @@ class SceneState:
     def bytes(self):
         ts = [self.octree_centers, self.octree_children, self.centers, self.feats, self.values]
         ts += self.mlp.w + self.mlp.b
-        return sum(t.numel() * t.element_size() for t in ts)
+        return sum(t.numel() * t.element_size() for t in ts) + self.svo_grid.bytes()
 
 
 # Sample capacity of a frame's first render, per ray; a frame that needs more
@@ -276,7 +281,8 @@ def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, exact, stream):
     return out
 
 
-def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exact=True):
+def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exact=True,
+                 traversal="grid"):
     """ray_start [3] (shared origin) or [R, 3], ray_dir [R, 3] (FP32, on the
     scene's device) -> dict(colors [R, 3], depths [R], missed [R],
     n_hit_rays, n_samples, n_far_outside).
@@ -290,7 +296,10 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
     the kernels' rounding) or "fp32" (the field's FP32 torch forward). The
     two tensor-core modes run on device-side counts with one host read at
     the end of the frame; the others read the sample count mid-frame to size
-    their torch tensors."""
+    their torch tensors.
+    traversal: "grid" (the leaf-grid sweep, nsvf_svo_intersect_grid, where the
+    scene's octree is in leaf-grid form) or "dfs" (the depth-first kernel,
+    nsvf_svo_intersect_sorted); both give the same hit lists bit for bit."""
     dev = scene.device
     R = ray_dir.shape[0]
     if out is None:
@@ -310,11 +319,17 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
         ro = ray_start.float().contiguous()
     err = _p(ext.error_word(dev))
     n_nodes = scene.octree_centers.shape[0]
-    with ext._timed("svo_intersect_sorted", dev):
-        check(LIB.nsvf_svo_intersect_sorted(1, 1, n_nodes, R, scene.voxel_size, H, _p(ro), _p(rd),
-                                            _p(scene.octree_centers), _p(scene.octree_children),
-                                            _p(b["idx"]), _p(b["lo"]), _p(b["hi"]), _p(b["hits"]),
-                                            err, _p(b["ws"]), stream), "svo_intersect_sorted")
+    if traversal == "grid" and scene.svo_grid.ok:
+        with ext._timed("svo_intersect_grid", dev):
+            scene.svo_grid.intersect_into(R, H, _p(ro), _p(rd), _p(b["idx"]), _p(b["lo"]),
+                                          _p(b["hi"]), _p(b["hits"]), stream)
+    else:
+        with ext._timed("svo_intersect_sorted", dev):
+            check(LIB.nsvf_svo_intersect_sorted(1, 1, n_nodes, R, scene.voxel_size, H, _p(ro),
+                                                _p(rd), _p(scene.octree_centers),
+                                                _p(scene.octree_children), _p(b["idx"]),
+                                                _p(b["lo"]), _p(b["hi"]), _p(b["hits"]), err,
+                                                _p(b["ws"]), stream), "svo_intersect_sorted")
     with ext._timed("hit_rows", dev):
         torch.cumsum(b["hits"], 0, dtype=torch.int32, out=b["scan"])
         check(LIB.nsvf_compact_hits(R, _p(b["hits"]), _p(b["scan"]), _p(b["pix"]), _p(b["n_hit"]),

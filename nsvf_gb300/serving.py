@@ -10,7 +10,8 @@ launches with each other and with the tails of large ones.
   fixed device buffers and with no host synchronisation:
   1. pinhole rays of every piece from a table of camera parameters in device
      memory (`nsvf_pinhole_rays_multi`);
-  2. SVO intersection + depth sort (`nsvf_svo_intersect_sorted`);
+  2. SVO intersection in depth order (`nsvf_svo_intersect_grid`, the leaf-grid sweep;
+     `nsvf_svo_intersect_sorted` for trees not in leaf-grid form);
   3. order-preserving hit compaction (torch cumsum + `nsvf_compact_hits`) and
      each piece's hit-row range (`nsvf_piece_rows`);
   4. the hit rays' lists and sampling distribution (`nsvf_gather_probs`);
@@ -130,9 +131,7 @@ class ChunkPipeline:
         self.n_outl = z(1, dtype=i64)
         self.refine_rows = z(self.outl_cap, dtype=i64)
         self.n_refine = z(1, dtype=i64)
-        n_nodes = scene.octree_centers.shape[0]
-        self.ws = torch.empty(max(16, int(LIB.nsvf_svo_workspace_bytes(1, n_nodes))), dtype=u8,
-                              device=dev)
+        self.ws = torch.empty(self._ws_bytes(scene, C), dtype=u8, device=dev)
         self.bg = torch.tensor(list(scene.bg), device=dev)
         self.graph = None
         self.use_graph = use_graph
@@ -144,8 +143,17 @@ class ChunkPipeline:
         cap = C * int(samples_per_ray)
         outl = max(4096, cap // 1024)
         per_ray = 24 + 12 * H + 1 + 4 + 8 + 16 * H + 4 + 4 + 8 + 20
-        ws = max(16, int(LIB.nsvf_svo_workspace_bytes(1, scene.octree_centers.shape[0])))
-        return C * per_ray + cap * 40 + outl * 16 + ws + MAX_PIECES * 80 + 64
+        return C * per_ray + cap * 40 + outl * 16 + ChunkPipeline._ws_bytes(scene, C) + \
+            MAX_PIECES * 80 + 64
+
+    @staticmethod
+    def _ws_bytes(scene, C):
+        """Traversal scratch: the leaf-grid sweep's ray list (the scene holds
+        the grid and its packed octree), else the depth-first kernel's packed
+        octree."""
+        if scene.svo_grid.ok:
+            return max(16, int(LIB.nsvf_svo_grid_list_bytes(C)))
+        return max(16, int(LIB.nsvf_svo_workspace_bytes(1, scene.octree_centers.shape[0])))
 
     def bytes(self):
         ts = [v for v in vars(self).values() if isinstance(v, torch.Tensor) and v.is_cuda]
@@ -155,11 +163,17 @@ class ChunkPipeline:
         sc, C, H, s = self.scene, self.C, self.scene.max_hits, self.stream.cuda_stream
         check(LIB.nsvf_pinhole_rays_multi(C, MAX_PIECES, _p(self.n_seg), _p(self.cams), _p(self.ro),
                                           _p(self.rd), s), "pinhole_rays_multi")
-        check(LIB.nsvf_svo_intersect_sorted(1, 1, sc.octree_centers.shape[0], C, sc.voxel_size, H,
-                                            _p(self.ro), _p(self.rd), _p(sc.octree_centers),
-                                            _p(sc.octree_children), _p(self.idx), _p(self.lo),
-                                            _p(self.hi), _p(self.hits), _p(self.err), _p(self.ws),
-                                            s), "svo_intersect_sorted")
+        if sc.svo_grid.ok:
+            sc.svo_grid.intersect_into(C, H, _p(self.ro), _p(self.rd), _p(self.idx), _p(self.lo),
+                                       _p(self.hi), _p(self.hits), s, list_ws=self.ws,
+                                       err=self.err)
+        else:
+            check(LIB.nsvf_svo_intersect_sorted(1, 1, sc.octree_centers.shape[0], C,
+                                                sc.voxel_size, H, _p(self.ro), _p(self.rd),
+                                                _p(sc.octree_centers), _p(sc.octree_children),
+                                                _p(self.idx), _p(self.lo), _p(self.hi),
+                                                _p(self.hits), _p(self.err), _p(self.ws), s),
+                  "svo_intersect_sorted")
         torch.cumsum(self.hits, 0, dtype=torch.int32, out=self.scan)
         check(LIB.nsvf_compact_hits(C, _p(self.hits), _p(self.scan), _p(self.pix), _p(self.n_hit),
                                     s), "compact_hits")

@@ -10,7 +10,9 @@ opaque field, so that compositing gradients matter), a batch of 4 views
 pixels drawn (seed 21) among the pixels whose ray hits a voxel and enters no
 two voxels at the same depth (where the reference's unstable depth sort is
 free to order them either way), and targets
-rendered from a second embedding set (seed 7). Both sides sample with the
+rendered from a second embedding set (seed 7). The rays themselves are stored
+(their host computation is not bit-identical across CPU architectures:
+numpy's matrix product rounds differently on Arm). Both sides sample with the
 slot-order sampling distribution (oracle.cpu.probs_steps), so they evaluate
 the same samples.
 
@@ -139,7 +141,8 @@ def main():
     colors = render()
     loss = ((colors - target) ** 2).sum()
     loss.backward()
-    g = {"views": np.array(VIEWS), "pixels": pix, "target": target.numpy(),
+    g = {"views": np.array(VIEWS), "pixels": pix, "ray_start": rays_o.numpy(),
+         "ray_dir": rays_d.numpy(), "target": target.numpy(),
          "loss": np.float64(loss.item()), "sigma_scale": np.float32(SIGMA_SCALE),
          "sigma_bias": np.float32(SIGMA_BIAS),
          "n_samples": np.int64(int(samples["sampled_point_voxel_idx"].ne(-1).sum()))}

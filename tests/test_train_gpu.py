@@ -30,13 +30,10 @@ def _c3(cuda, go):
         enc.values.weight.copy_(scenes.voxel_embeddings(enc.values.weight.shape[0], 32, 0.01, seed=1))
     field = StandInField(weights=scenes.stand_in_mlp_weights(
         seed=2, sigma_scale=float(go["sigma_scale"]), sigma_bias=float(go["sigma_bias"])))
-    rs_all, rd_all = [], []
-    for v, pix in zip(go["views"], go["pixels"]):
-        rs, rd = scenes.frame_view(int(v))
-        rs_all.append(np.broadcast_to(rs, (pix.size, 3)))
-        rd_all.append(rd[pix])
-    ro = torch.from_numpy(np.concatenate(rs_all).astype(np.float32)).to(cuda)
-    rd = torch.from_numpy(np.concatenate(rd_all).astype(np.float32)).to(cuda)
+    # the fixture's own rays (recomputing them from the pixel indices is not
+    # bit-identical across CPU architectures)
+    ro = torch.from_numpy(go["ray_start"]).to(cuda)
+    rd = torch.from_numpy(go["ray_dir"]).to(cuda)
     return enc.to(cuda), field.to(cuda), ro, rd
 
 
