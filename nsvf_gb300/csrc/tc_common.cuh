@@ -266,13 +266,14 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t pari
 }
 
 // Bounded wait: gives up after `limit_ns` (default 2 s) or as soon as
-// *abort is set by another thread; returns false then (the caller records an
-// error and unwinds). Between checks of *abort and the clock a thread sleeps
+// *abort is set by another thread (also when it is already set on entry);
+// returns false then (the caller records an error and unwinds). Between checks of *abort and the clock a thread sleeps
 // in try_wait for at most 0.5 ms.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           uint64_t limit_ns = 2000000000ull) {
   uint64_t t0 = 0;
   for (uint32_t i = 0;; ++i) {
+    if (*abort) return false;     // the CTA is unwinding: no more waiting
     if (mbar_try_wait_sleep(bar, parity, 500000u)) return true;
     if (*abort) return false;
     uint64_t t = globaltimer_ns();
