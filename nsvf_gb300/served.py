@@ -50,6 +50,14 @@ def _p(t):
     return t.data_ptr() if t is not None else None
 
 
+def _is_tensor_core_field(field):
+    layers = getattr(field, "layers", None)
+    if layers is None or not hasattr(field, "mlp"):
+        return False
+    dims = [(getattr(l, "out_features", None), getattr(l, "in_features", None)) for l in layers]
+    return dims == [(128, 32), (128, 128), (128, 128), (128, 128), (4, 128)]
+
+
 class SceneState:
     """Device-resident scene: octree, shifted voxel centres, corner table,
     embeddings, field weights (FP32 and BF16), background."""
@@ -69,9 +77,14 @@ class SceneState:
         self.values = states['voxel_vertex_emb'].detach().float().contiguous()
         self.field = field
         self.device = self.centers.device
-        self.mlp = TensorCoreMLP(field)
-        # BF16 bias correction, calibrated once per scene
-        self.mlp.calibrate_bias(self.calibration_emb())
+        # The tensor-core MLP takes the workloads' 4 x 128 ReLU field; any
+        # other field of the reference's field interface (a checkpointed
+        # radiance field, field.RaidanceField) renders through the served
+        # chain with its own FP32 torch modules (render_frame(mlp="field")).
+        self.mlp = TensorCoreMLP(field) if _is_tensor_core_field(field) else None
+        if self.mlp is not None:
+            # BF16 bias correction, calibrated once per scene
+            self.mlp.calibrate_bias(self.calibration_emb())
         bg = field.bg_color.bg_color.detach().float().cpu()
         self.bg = (ctypes.c_float * 3)(*bg.tolist())
         self.bg_depth = float(field.bg_color.depth)
@@ -98,7 +111,10 @@ class SceneState:
 
     def bytes(self):
         ts = [self.octree_centers, self.octree_children, self.centers, self.feats, self.values]
-        ts += self.mlp.w + self.mlp.b
+        if self.mlp is not None:
+            ts += self.mlp.w + self.mlp.b
+        else:
+            ts += [t for t in self.field.parameters()]
         return sum(t.numel() * t.element_size() for t in ts) + self.svo_grid.bytes()
 
 
@@ -293,7 +309,11 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
     mlp: "tc" (interpolation fused into the tcgen05 BF16 MLP), "tc_fp8" (the
     same with E4M3 hidden layers), "tc_unfused" (interpolation kernel, then
     the MLP kernel), "bf16_emulated" / "fp8_emulated" (torch emulations of
-    the kernels' rounding) or "fp32" (the field's FP32 torch forward). The
+    the kernels' rounding), "fp32" (the 4 x 128 field's FP32 torch forward)
+    or "field" (any field with the reference's field interface, e.g. a
+    checkpointed field.RaidanceField: its FP32 torch forward on the samples'
+    embeddings, positions and ray directions; the default for scenes whose
+    field the tensor-core MLP does not take). The
     two tensor-core modes run on device-side counts with one host read at
     the end of the frame; the others read the sample count mid-frame to size
     their torch tensors.
@@ -302,6 +322,11 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
     nsvf_svo_intersect_sorted); both give the same hit lists bit for bit."""
     dev = scene.device
     R = ray_dir.shape[0]
+    if scene.mlp is None and mlp != "field":
+        if mlp != "tc":
+            raise ValueError("mlp=%r needs the 4 x 128 field; this scene's field renders with "
+                             "mlp='field'" % (mlp,))
+        mlp = "field"
     if out is None:
         out = {"colors": torch.empty(R, 3, device=dev), "depths": torch.empty(R, device=dev),
                "missed": torch.empty(R, device=dev)}
@@ -371,6 +396,11 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
         field = scene.mlp_fp8().reference_fp8(emb).contiguous()
     elif mlp == "fp32":
         field = scene.field.mlp(emb).float().contiguous()
+    elif mlp == "field":
+        field = _field_forward(scene, b, n, ns, ro, rd, offset, vox, xyzd, emb)
+        # the field runs in FP32 like the reference's; the double-float pass
+        # is specific to the 4 x 128 field
+        exact = False
     else:
         raise ValueError("unknown mlp mode %r" % (mlp,))
     if exact:
@@ -395,6 +425,31 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
             n, _p(offset), _p(field), _p(xyzd), _p(depth), _p(b["pix"]), 7.0, scene.bg,
             scene.bg_depth, _p(out["colors"]), _p(out["depths"]), _p(out["missed"]),
             int(bool(kahan)), stream), "composite_segments")
+    return out
+
+
+# samples per call of a field module on the served path's generic mode
+FIELD_CHUNK = 1 << 20
+
+
+def _field_forward(scene, b, n, ns, ro, rd, offset, vox, xyzd, emb):
+    """The scene's field module on the compacted samples, through the
+    reference's field interface (inputs 'emb', 'pos', 'ray', 'dists';
+    fairnr/modules/renderer.py:105-111), FIELD_CHUNK samples at a time (the
+    reference's field forward builds an autograd graph for its normals):
+    -> [ns, 4] (sigma, r, g, b)."""
+    dev = scene.device
+    counts = offset[1:n + 1] - offset[:n]
+    rows = torch.repeat_interleave(torch.arange(n, device=dev), counts, output_size=ns)
+    ray = rd[b["pix"][:n][rows]]
+    out = torch.empty(ns, 4, dtype=torch.float32, device=dev)
+    for s0 in range(0, ns, FIELD_CHUNK):
+        s1 = min(ns, s0 + FIELD_CHUNK)
+        inputs = {"emb": emb[s0:s1], "pos": xyzd[s0:s1, :3], "ray": ray[s0:s1],
+                  "dists": xyzd[s0:s1, 3]}
+        res = scene.field(inputs, outputs=("sigma", "texture"))
+        out[s0:s1, 0] = res["sigma"].reshape(-1).detach().float()
+        out[s0:s1, 1:4] = res["texture"].reshape(-1, 3).detach().float()
     return out
 
 

@@ -188,3 +188,75 @@ def test_reference_radiance_field_renders_like_reference(golden, golden_next, cu
     for k in ["colors", "depths", "missed"]:
         np.testing.assert_allclose(out[k].cpu().numpy(), n["rf_%s" % k], atol=2e-4)
     assert float(n["rf_missed"].min()) < 0.1          # an opaque enough field to test compositing
+
+
+@pytest.mark.gpu
+def test_reference_radiance_field_in_served_chain(golden, golden_next, cuda):
+    """The same checkpointed RaidanceField in the served chain
+    (served.SceneState + render_frame, mlp="field": the field's FP32 torch
+    modules on the compacted samples) renders the frame of the drop-in
+    module path."""
+    from nsvf_gb300.field import RaidanceField
+    from nsvf_gb300.renderer import VolumeRenderer, render_rays
+    from nsvf_gb300.served import SceneState, render_frame
+    g, n = golden, golden_next
+    enc = _encoder(g, cuda)
+    args = argparse.Namespace(inputs_to_density="emb:6:32", inputs_to_texture="feat:0:64, ray:4",
+                              feature_embed_dim=64, density_embed_dim=32, texture_embed_dim=64,
+                              feature_layers=1, texture_layers=2, background_stop_gradient=False)
+    field = RaidanceField(args)
+    state = {k[len("rf_state_"):]: torch.from_numpy(n[k]) for k in n if k.startswith("rf_state_")}
+    field.load_state_dict(state, strict=True)
+    field = field.to(cuda).eval()
+    rs = torch.from_numpy(g["ray_start"]).to(cuda).reshape(3)
+    rd = torch.from_numpy(g["ray_dir"]).to(cuda)
+    ren = VolumeRenderer(argparse.Namespace(chunk_size=64)).eval()
+    with torch.no_grad():
+        ref = render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3))
+    scene = SceneState(enc, field)
+    assert scene.mlp is None                   # not the 4 x 128 tensor-core field
+    out = render_frame(scene, rs, rd, kahan=False)
+    assert out["n_samples"] > 1000
+    for k in ["colors", "depths", "missed"]:
+        np.testing.assert_allclose(out[k].cpu().numpy(), ref[k].reshape(out[k].shape).cpu().numpy(),
+                                   atol=2e-4, err_msg=k)
+    assert float(out["missed"].min()) < 0.1
+
+
+@pytest.mark.gpu
+def test_splitting_on_gpu_then_render(golden, golden_next, cuda):
+    """Splitting on the device gives the reference's split voxels, corner
+    table and keep mask (the embeddings re-interpolated to 1e-6); the split
+    scene (voxel size halved, max_hits x 1.5, as the reference's model does
+    after splitting: fairnr/models/nsvf.py) then rebuilds its octree and
+    renders through the served chain the frame of the drop-in path.
+    (fairnr/models/nsvf.py:148-155: splitting, voxel size x 0.5, max_hits x
+    1.5, runtime caches cleared.)"""
+    from nsvf_gb300 import scenes
+    from nsvf_gb300.field import StandInField
+    from nsvf_gb300.renderer import VolumeRenderer, render_rays
+    from nsvf_gb300.served import SceneState, render_frame
+    g, n = golden, golden_next
+    enc = _encoder(g, cuda)
+    enc.splitting()
+    assert np.array_equal(enc.points.cpu().numpy(), n["split_points"])
+    assert np.array_equal(enc.feats.cpu().numpy(), n["split_feats"])
+    assert int(enc.num_keys) == int(n["split_num_keys"])
+    assert np.array_equal(enc.keep.cpu().numpy(), n["split_keep"])
+    np.testing.assert_allclose(enc.values.weight.detach().cpu().numpy(), n["split_values"],
+                               atol=1e-6)
+    enc.voxel_size *= .5
+    enc.max_hits *= 1.5
+    enc.clean_runtime_caches()
+    field = StandInField(weights=scenes.stand_in_mlp_weights(seed=2, sigma_scale=30.0,
+                                                             sigma_bias=0.5)).to(cuda).eval()
+    rs = torch.from_numpy(g["ray_start"]).to(cuda).reshape(3)
+    rd = torch.from_numpy(g["ray_dir"]).to(cuda)
+    ren = VolumeRenderer(argparse.Namespace(chunk_size=64)).eval()
+    with torch.no_grad():
+        ref = render_rays(enc, field, ren, rs.reshape(1, 1, 1, 3), rd.reshape(1, 1, -1, 3))
+    out = render_frame(SceneState(enc, field), rs, rd, mlp="fp32", kahan=False, exact=False)
+    assert out["n_samples"] > 1000
+    for k in ["colors", "missed"]:
+        np.testing.assert_allclose(out[k].cpu().numpy(), ref[k].reshape(out[k].shape).cpu().numpy(),
+                                   atol=2e-5, err_msg=k)
