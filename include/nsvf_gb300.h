@@ -115,11 +115,13 @@ int64_t nsvf_svo_grid_list_bytes(int64_t rays);
  * nsvf_svo_grid_build blob, `info` (HOST int32[6]) its nsvf_svo_grid_info,
  * `packed` the nsvf_svo_pack workspace of the
  * same octree, `list_ws` nsvf_svo_grid_list_bytes(rays) bytes of device
- * scratch (16-byte aligned). Rays the sweep leaves to the depth-first search
- * are listed there and traversed by it in a second launch: rays with a zero
- * direction component or with a hit beyond depth 10000. Rays with more than
- * n_max hits keep, like the search, the first n_max leaves in visiting
- * order. n_max <= 128. Calls that share `list_ws` must not overlap on the
+ * scratch (16-byte aligned). The hits of a ray past its first n_max go to
+ * an overflow block there (32,768 blocks at most), and an overflow pass (a
+ * warp per ray) keeps, like the search, the first n_max leaves in visiting
+ * order. Rays the sweep leaves to the depth-first search are listed there
+ * and traversed by it in a last launch: rays with a zero direction
+ * component, with a hit beyond depth 10000, with more than n_max + 64 hits,
+ * or past the last overflow block. n_max <= 128. Calls that share `list_ws` must not overlap on the
  * GPU. */
 int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
                             const float *ray_start, const float *ray_dir, const float *points,

@@ -35,10 +35,9 @@
 // cells the ray crosses (44 on average on the c2 frame), against the
 // hundreds of node expansions of the tree walk.
 //
-// Rays with more than n_max hits: the search stops after the first n_max
-// leaves in visiting order. The sweep keeps, of the hits met so far, the
-// n_max with the smallest visiting ranks (a smaller rank replaces the row's
-// largest), so the row ends as that set in (min_depth, rank) order.
+// Rays with more than n_max hits (the search stops after the first n_max
+// leaves in visiting order) are listed for an overflow pass: a warp per ray
+// sweeps it again keeping every hit, and keeps the n_max smallest ranks.
 //
 // Rays the sweep does not take go to the depth-first kernel, through a list:
 // rays with a zero direction component (the slab test's non-finite branch)
@@ -308,36 +307,265 @@ __device__ __forceinline__ bool ancestors_hit(const GridView G, float ox, float 
   return true;
 }
 
-// Largest visiting rank in a full row, and its slot.
-// (returned as rank << 8 | slot; n_max <= 128)
-__device__ __forceinline__ int64_t row_largest_rank(const int32_t *I, int n_max,
-                                                 const int32_t *__restrict__ rank_of) {
-  int32_t best = -1;
-  int pos = 0;
-  for (int q = 0; q < n_max; ++q) {
-    const int32_t rq = __ldg(rank_of + I[q]);
-    if (rq > best) { best = rq; pos = q; }
+// What a sweep ended with.
+constexpr int kSweepDone = 0;     // every hit emitted
+constexpr int kSweepList = 1;     // left to the depth-first kernel (a zero direction component,
+                                  // or a hit beyond depth 10000)
+constexpr int kSweepStopped = 2;  // the emitter stopped it
+
+// The sweep of ray r across the leaf grid: emit(leaf entry, min_depth,
+// max_depth) for every hit, in non-decreasing min_depth (hits with equal
+// min_depth in any order); emit returns false to stop the sweep.
+template <class Emit>
+__device__ __forceinline__ int sweep_ray(int64_t r, const GridView &G,
+                                         const float *__restrict__ ray_start,
+                                         const float *__restrict__ ray_dir, Emit &emit) {
+  Sweep S;
+  bool fast = true;
+  float dir[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S.o[a] = ray_start[r * 3 + a];
+    dir[a] = ray_dir[r * 3 + a];
+    S.inv[a] = nsvf_rcp(dir[a]);
+    fast = fast && isfinite(S.inv[a]);
+    S.sh[a] = S.inv[a] >= 0.0f ? G.hv : -G.hv;
   }
-  return ((int64_t)best << 8) | pos;
+  if (!fast) return kSweepList;
+  // the first time inside the grid's slab on every axis, and the cells active
+  // then: the first cell (in travel order) not yet left, and the first not yet
+  // entered
+  float t = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) t = fmaxf(t, entry_t(G, S, a, 0));
+  bool dead = !(t <= 100000.0f);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) dead = dead || exit_t(G, S, a, G.n[a] - 1) < t;
+  if (dead) return kSweepDone;
+  int old[3], nxt[3], ns[3];
+  float f_old[3], e_nxt[3], f_new[3];   // exits of the first and last active cells
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    // estimate, then correct with the exact exits
+    const float c0 = __ldg(G.tab[a]);
+    const float x = dir[a] * t + S.o[a];
+    float fi = floorf((x - (c0 - G.hv)) / (2.0f * G.hv));
+    fi = fminf(fmaxf(fi, 0.0f), (float)(G.n[a] - 1));
+    int u = S.sh[a] > 0.0f ? (int)fi : G.n[a] - 1 - (int)fi;
+    while (u > 0 && exit_t(G, S, a, u - 1) >= t) --u;
+    while (exit_t(G, S, a, u) < t) ++u;            // ends: the last cell's exit >= t
+    old[a] = u;
+    f_old[a] = exit_t(G, S, a, u);
+    int v = u;
+    float e = entry_t(G, S, a, v);
+    while (e <= t) {
+      ++v;
+      if (v >= G.n[a]) { e = INFINITY; break; }
+      e = entry_t(G, S, a, v);
+    }
+    nxt[a] = v;
+    e_nxt[a] = e;
+    f_new[a] = v > u ? exit_t(G, S, a, v - 1) : f_old[a];
+    ns[a] = u;                                     // the first event: every active cell is new
+  }
+  int64_t cached = -1;
+  ulonglong2 brick = make_ulonglong2(0, 0);
+  int status = kSweepDone;
+  // Visits the cell at travel positions (ux, uy, uz), born at t, with the
+  // exits fx, fy, fz: emits its leaf if there is one.
+  auto visit = [&](int ux, int uy, int uz, float fx, float fy, float fz) {
+    const int gi = S.sh[0] > 0.0f ? ux : G.n[0] - 1 - ux;
+    const int gj = S.sh[1] > 0.0f ? uy : G.n[1] - 1 - uy;
+    const int gk = S.sh[2] > 0.0f ? uz : G.n[2] - 1 - uz;
+    const int64_t w = ((int64_t)(gk >> 2) * G.nb[1] + (gj >> 2)) * G.nb[0] + (gi >> 2);
+    const int bit = ((gk & 3) * 4 + (gj & 3)) * 4 + (gi & 3);
+    if (w != cached) {
+      brick = __ldg(G.bricks + w);
+      cached = w;
+    }
+    if (!((brick.x >> bit) & 1ull)) return;
+    const int64_t rk = (int64_t)brick.y + __popcll(brick.x & ((1ull << bit) - 1ull));
+    const int2 lf = __ldg(G.leaf + rk);
+    // a flagged leaf: its ancestors' faces do not all enclose its own
+    if (lf.y < 0 && !ancestors_hit(G, S.o[0], S.o[1], S.o[2], S.inv[0], S.inv[1], S.inv[2], lf.x))
+      return;
+    if (t > NSVF_MAX_DEPTH_F) {
+      status = kSweepList;
+      return;
+    }
+    float hi = 100000.0f;
+    hi = (fx < hi) ? fx : hi;
+    hi = (fy < hi) ? fy : hi;
+    hi = (fz < hi) ? fz : hi;
+    if (!emit(lf, t, hi)) status = kSweepStopped;
+  };
+  // each event enters at least one cell (a skip enters the cells at t_j)
+  const int64_t max_events = (int64_t)G.n[0] + G.n[1] + G.n[2] + 2;
+  for (int64_t ev = 0; !dead && status == kSweepDone && ev < max_events; ++ev) {
+    if (old[0] < nxt[0] && old[1] < nxt[1] && old[2] < nxt[2]) {
+      // The common event: one axis enters one cell and the other two have
+      // one active cell each: one new triple. (On a dyadic grid a cell's
+      // exit equals the next cell's entry, so the entering axis's previous
+      // cell is still active at t; its triples were born earlier.)
+      const int e0 = nxt[0] - ns[0], e1 = nxt[1] - ns[1], e2 = nxt[2] - ns[2];
+      const int w0 = nxt[0] - old[0], w1 = nxt[1] - old[1], w2 = nxt[2] - old[2];
+      const bool one = (e0 + e1 + e2 == 1) && ((e0 == 1) ? (w1 == 1 && w2 == 1)
+                                               : (e1 == 1) ? (w0 == 1 && w2 == 1)
+                                                           : (w0 == 1 && w1 == 1));
+      if (one) {
+        visit(e0 ? nxt[0] - 1 : old[0], e1 ? nxt[1] - 1 : old[1], e2 ? nxt[2] - 1 : old[2],
+              e0 ? f_new[0] : f_old[0], e1 ? f_new[1] : f_old[1], e2 ? f_new[2] : f_old[2]);
+      } else {
+        for (int ux = old[0]; ux < nxt[0] && status == kSweepDone; ++ux) {
+          const float fx = exit_t(G, S, 0, ux);
+          for (int uy = old[1]; uy < nxt[1] && status == kSweepDone; ++uy) {
+            const float fy = exit_t(G, S, 1, uy);
+            for (int uz = old[2]; uz < nxt[2] && status == kSweepDone; ++uz) {
+              if (ux < ns[0] && uy < ns[1] && uz < ns[2]) continue;   // born earlier
+              visit(ux, uy, uz, fx, fy, exit_t(G, S, 2, uz));
+            }
+          }
+        }
+      }
+    }
+    if (status != kSweepDone) break;
+    // Brick skip. After t, an axis's cells that can still form triples are
+    // the active ones with exit > t and the ones not yet entered. When
+    // that is one cell per axis (c) and c's 4x4x4 brick is empty, every
+    // triple born before t_j -- the first entry, on any axis, of a cell
+    // past the brick -- lies in the brick: those events are taken
+    // silently and the sweep resumes at the event t_j.
+    float tn = INFINITY;
+    bool skip = true;
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const int wdt = nxt[a] - old[a];
+      c[a] = (wdt == 1) ? old[a] : old[a] + 1;
+      skip = skip && (wdt == 1 || (wdt == 2 && f_old[a] <= t));
+    }
+    if (skip) {
+      const int gi = S.sh[0] > 0.0f ? c[0] : G.n[0] - 1 - c[0];
+      const int gj = S.sh[1] > 0.0f ? c[1] : G.n[1] - 1 - c[1];
+      const int gk = S.sh[2] > 0.0f ? c[2] : G.n[2] - 1 - c[2];
+      const int64_t w = ((int64_t)(gk >> 2) * G.nb[1] + (gj >> 2)) * G.nb[0] + (gi >> 2);
+      if (w != cached) {
+        brick = __ldg(G.bricks + w);
+        cached = w;
+      }
+      skip = brick.x == 0ull;
+      if (skip) {
+        const int g3[3] = {gi, gj, gk};
+        int lim[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const int rem = S.sh[a] > 0.0f ? 4 - (g3[a] & 3) : (g3[a] & 3) + 1;
+          lim[a] = min(G.n[a], c[a] + rem);
+          if (lim[a] < G.n[a]) tn = fminf(tn, entry_t(G, S, a, lim[a]));
+        }
+        if (!(tn <= 100000.0f)) break;          // nothing past this empty brick
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          while (nxt[a] < lim[a] && e_nxt[a] < tn) {
+            f_new[a] = exit_t(G, S, a, nxt[a]);
+            if (old[a] == nxt[a]) f_old[a] = f_new[a];
+            ++nxt[a];
+            e_nxt[a] = nxt[a] < G.n[a] ? entry_t(G, S, a, nxt[a]) : INFINITY;
+          }
+        }
+      }
+    }
+    // the next entry event
+    if (!skip) {
+      tn = fminf(e_nxt[0], fminf(e_nxt[1], e_nxt[2]));
+      if (!(tn <= 100000.0f)) break;
+    }
+    t = tn;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      while (old[a] < nxt[a] && f_old[a] < t) {
+        ++old[a];
+        f_old[a] = old[a] == nxt[a] - 1 ? f_new[a]
+                   : (old[a] < G.n[a] ? exit_t(G, S, a, old[a]) : 0.0f);
+      }
+      dead = dead || old[a] >= G.n[a];
+      ns[a] = nxt[a];
+      while (e_nxt[a] == t) {
+        f_new[a] = exit_t(G, S, a, nxt[a]);
+        if (old[a] == nxt[a]) f_old[a] = f_new[a];
+        ++nxt[a];
+        e_nxt[a] = nxt[a] < G.n[a] ? entry_t(G, S, a, nxt[a]) : INFINITY;
+      }
+    }
+  }
+  return status;
 }
 
-// Removes slot `pos` of a full row; the rest keeps its order.
-__device__ __forceinline__ void row_remove(int32_t *I, float *LO, float *HI, int n_max, int pos) {
-  for (int q = pos; q + 1 < n_max; ++q) {
-    I[q] = I[q + 1];
-    LO[q] = LO[q + 1];
-    HI[q] = HI[q + 1];
-  }
-}
+// A hit past a full row, kept for the overflow pass.
+struct OverHit {
+  uint32_t lo_bits;  // min_depth's bits (>= +0, so they order like the value)
+  float hi;
+  int32_t id, rank;
+};
 
-// (No minimum of resident blocks: capping the registers at 80 or 64 spills
-// and was 12 % / 26 % slower on the c2 frame.)
+// Hits past n_max that a ray's overflow block holds; a ray with more goes to
+// the depth-first kernel.
+constexpr int kOverExtra = 64;
+
+// Emits hits into a ray's row, in (min_depth, visiting rank) order: hits come
+// in non-decreasing min_depth, and one with the same min_depth as the row's
+// last slots is placed among them by rank. Hits past n_max go, in order, to
+// an overflow block reserved for the ray (over slot q); when there is no
+// block left or the ray fills it, the sweep stops and the ray goes to the
+// depth-first kernel.
+struct RowEmit {
+  int32_t *I;
+  float *LO, *HI;
+  const int32_t *rank_of;
+  int n_max, cnt;
+  float last_lo;                 // min_depth of the row's last slot
+  int32_t *n_over;
+  OverHit *scratch;
+  int over_cap, q, e;
+  __device__ __forceinline__ bool operator()(int2 lf, float lo, float hi) {
+    if (cnt >= n_max) {
+      if (q < 0) {
+        q = atomicAdd(n_over, 1);
+        if (q >= over_cap) return false;
+      }
+      if (e >= kOverExtra) return false;
+      scratch[(int64_t)q * kOverExtra + e] = OverHit{__float_as_uint(lo), hi, lf.x, lf.y & 0x7fffffff};
+      ++e;
+      return true;
+    }
+    int pos = cnt;
+    if (cnt > 0 && last_lo == lo) {
+      const int32_t my = lf.y & 0x7fffffff;
+      while (pos > 0 && LO[pos - 1] == lo && __ldg(rank_of + I[pos - 1]) > my) {
+        I[pos] = I[pos - 1];
+        LO[pos] = LO[pos - 1];
+        HI[pos] = HI[pos - 1];
+        --pos;
+      }
+    }
+    I[pos] = lf.x;
+    LO[pos] = lo;
+    HI[pos] = hi;
+    ++cnt;
+    last_lo = lo;
+    return true;
+  }
+};
+
+// (No minimum of resident blocks: capping the registers spills and was
+// slower on the c2 frame.)
 __global__ void __launch_bounds__(kGridBlock) svo_grid_kernel(
     int64_t rays, int n_max, const float *__restrict__ ray_start,
     const float *__restrict__ ray_dir, const GridView G, int32_t *__restrict__ idx,
     float *__restrict__ min_depth, float *__restrict__ max_depth, uint8_t *__restrict__ hits,
-    int32_t *__restrict__ list, int32_t *__restrict__ n_list,
-    unsigned long long *__restrict__ next_ray) {
+    int32_t *__restrict__ list, int32_t *__restrict__ n_list, int32_t *__restrict__ over,
+    int32_t *__restrict__ over_cnt, int32_t *__restrict__ n_over, OverHit *__restrict__ scratch,
+    int over_cap, unsigned long long *__restrict__ next_ray) {
   // Persistent warps: each warp takes the next 32 rays from a global
   // counter until there are none left, so the SMs stay full to the end of
   // the frame (rays differ a lot in length: fixed blocks left the SMs active
@@ -347,253 +575,120 @@ __global__ void __launch_bounds__(kGridBlock) svo_grid_kernel(
   const int lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
   for (;;) {
-  unsigned long long base0 = 0;
-  if (lane == 0) base0 = atomicAdd(next_ray, 32ull);
-  const int64_t base = (int64_t)__shfl_sync(full, base0, 0);
-  if (base >= rays) break;
-  const int64_t r = base + lane;
-  const bool live = r < rays;
-  const int64_t rr = live ? r : 0;
-  Sweep S;
-  bool fast = true;
-  float dir[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    S.o[a] = ray_start[rr * 3 + a];
-    dir[a] = ray_dir[rr * 3 + a];
-    S.inv[a] = nsvf_rcp(dir[a]);
-    fast = fast && isfinite(S.inv[a]);
-    S.sh[a] = S.inv[a] >= 0.0f ? G.hv : -G.hv;
-  }
-  int32_t *I = idx + rr * n_max;
-  float *LO = min_depth + rr * n_max, *HI = max_depth + rr * n_max;
-  int cnt = 0;
-  bool to_list = live && !fast;
-
-  if (live && fast) {
-    // the first time inside the grid's slab on every axis, and the cells
-    // active then: the first cell (in travel order) not yet left, and the
-    // first not yet entered
-    float t = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) t = fmaxf(t, entry_t(G, S, a, 0));
-    bool dead = !(t <= 100000.0f);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) dead = dead || exit_t(G, S, a, G.n[a] - 1) < t;
-    int old[3], nxt[3], ns[3];
-    float f_old[3], e_nxt[3], f_new[3];   // exits of the first and last active cells
-    if (!dead) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        // estimate, then correct with the exact exits
-        const float c0 = __ldg(G.tab[a]);
-        const float x = dir[a] * t + S.o[a];
-        float fi = floorf((x - (c0 - G.hv)) / (2.0f * G.hv));
-        fi = fminf(fmaxf(fi, 0.0f), (float)(G.n[a] - 1));
-        int u = S.sh[a] > 0.0f ? (int)fi : G.n[a] - 1 - (int)fi;
-        while (u > 0 && exit_t(G, S, a, u - 1) >= t) --u;
-        while (exit_t(G, S, a, u) < t) ++u;            // ends: the last cell's exit >= t
-        old[a] = u;
-        f_old[a] = exit_t(G, S, a, u);
-        int v = u;
-        float e = entry_t(G, S, a, v);
-        while (e <= t) {
-          ++v;
-          if (v >= G.n[a]) { e = INFINITY; break; }
-          e = entry_t(G, S, a, v);
-        }
-        nxt[a] = v;
-        e_nxt[a] = e;
-        f_new[a] = v > u ? exit_t(G, S, a, v - 1) : f_old[a];
-        ns[a] = u;                                   // the first event: every active cell is new
+    unsigned long long base0 = 0;
+    if (lane == 0) base0 = atomicAdd(next_ray, 32ull);
+    const int64_t base = (int64_t)__shfl_sync(full, base0, 0);
+    if (base >= rays) break;
+    const int64_t r = base + lane;
+    const bool live = r < rays;
+    const int64_t rr = live ? r : 0;
+    RowEmit em{idx + rr * n_max, min_depth + rr * n_max, max_depth + rr * n_max, G.rank_of,
+               n_max, 0, -1.0f, n_over, scratch, over_cap, -1, 0};
+    const int st = live ? sweep_ray(rr, G, ray_start, ray_dir, em) : kSweepDone;
+    if (em.q >= 0 && em.q < over_cap) {
+      // an overflow ray: the overflow pass writes its row (or skips slot q
+      // when the ray went to the depth-first kernel)
+      over[em.q] = st == kSweepDone ? (int32_t)r : -1;
+      over_cnt[em.q] = em.e;
+    }
+    if (st != kSweepDone) {
+      list[atomicAdd(n_list, 1)] = (int32_t)r;
+    } else if (live && em.q < 0) {
+      hits[r] = em.cnt > 0;
+    }
+    // pad the rows (misses: id -1, depths 10000), a warp per row
+    const bool pad = live && st == kSweepDone && em.q < 0;
+    for (int q = 0; q < 32; ++q) {
+      const int cq = __shfl_sync(full, em.cnt, q);
+      if (!__shfl_sync(full, (int)pad, q)) continue;
+      const int64_t rq = base + q;
+      for (int l = cq + lane; l < n_max; l += 32) {
+        idx[rq * n_max + l] = -1;
+        min_depth[rq * n_max + l] = NSVF_MAX_DEPTH_F;
+        max_depth[rq * n_max + l] = NSVF_MAX_DEPTH_F;
       }
     }
-    int64_t cached = -1;
-    ulonglong2 brick = make_ulonglong2(0, 0);
-    int64_t row_max = -1;   // a full row's largest rank << 8 | its slot (-1: not known)
-    // Emits a hit (its leaf entry, min_depth lo, max_depth hi) into the row.
-    float last_lo = -1.0f;                 // min_depth of the row's last slot
-    auto emit = [&](int2 lf, float lo, float hi) {
-      // a flagged leaf: its ancestors' faces do not all enclose its own
-      if (lf.y < 0 && !ancestors_hit(G, S.o[0], S.o[1], S.o[2], S.inv[0], S.inv[1], S.inv[2],
-                                    lf.x))
-        return;
-      if (lo > NSVF_MAX_DEPTH_F) {
-        to_list = true;
-        return;
-      }
-      const int32_t my = lf.y & 0x7fffffff;
-      if (cnt >= n_max) {
-        // The search keeps the first n_max leaves in visiting order: the row
-        // holds the n_max smallest ranks met so far; a smaller rank replaces
-        // the largest (the rest of the row keeps its order).
-        if (row_max < 0) row_max = row_largest_rank(I, n_max, G.rank_of);
-        if (my > (int32_t)(row_max >> 8)) return;
-        row_remove(I, LO, HI, n_max, (int)(row_max & 0xff));
-        cnt = n_max - 1;
-        row_max = -1;                      // rescanned at the next full row
-        last_lo = LO[cnt - 1];
-      }
-      // equal min_depth: visiting order (hits come in non-decreasing lo)
-      int pos = cnt;
-      if (cnt > 0 && last_lo == lo) {
-        while (pos > 0 && LO[pos - 1] == lo && __ldg(G.rank_of + I[pos - 1]) > my) {
-          I[pos] = I[pos - 1];
-          LO[pos] = LO[pos - 1];
-          HI[pos] = HI[pos - 1];
-          --pos;
-        }
-      }
-      I[pos] = lf.x;
-      LO[pos] = lo;
-      HI[pos] = hi;
-      ++cnt;
-      last_lo = lo;
-    };
-    // Visits the cell at travel positions (ux, uy, uz), born at t, with the
-    // exits fx, fy, fz.
-    auto visit = [&](int ux, int uy, int uz, float fx, float fy, float fz) {
-      const int gi = S.sh[0] > 0.0f ? ux : G.n[0] - 1 - ux;
-      const int gj = S.sh[1] > 0.0f ? uy : G.n[1] - 1 - uy;
-      const int gk = S.sh[2] > 0.0f ? uz : G.n[2] - 1 - uz;
-      const int64_t w = ((int64_t)(gk >> 2) * G.nb[1] + (gj >> 2)) * G.nb[0] + (gi >> 2);
-      const int bit = ((gk & 3) * 4 + (gj & 3)) * 4 + (gi & 3);
-      if (w != cached) {
-        brick = __ldg(G.bricks + w);
-        cached = w;
-      }
-      if (!((brick.x >> bit) & 1ull)) return;
-      const int64_t rk = (int64_t)brick.y + __popcll(brick.x & ((1ull << bit) - 1ull));
-      float hi = 100000.0f;
-      hi = (fx < hi) ? fx : hi;
-      hi = (fy < hi) ? fy : hi;
-      hi = (fz < hi) ? fz : hi;
-      emit(__ldg(G.leaf + rk), t, hi);
-    };
-    // each event enters at least one cell (a skip enters the cells at t_j)
-    const int64_t max_events = (int64_t)G.n[0] + G.n[1] + G.n[2] + 2;
-    for (int64_t ev = 0; !dead && !to_list && ev < max_events; ++ev) {
-      if (old[0] < nxt[0] && old[1] < nxt[1] && old[2] < nxt[2]) {
-        // The common event: one axis enters one cell and the other two have
-        // one active cell each: one new triple. (On a dyadic grid a cell's
-        // exit equals the next cell's entry, so the entering axis's previous
-        // cell is still active at t; its triples were born earlier.)
-        const int e0 = nxt[0] - ns[0], e1 = nxt[1] - ns[1], e2 = nxt[2] - ns[2];
-        const int w0 = nxt[0] - old[0], w1 = nxt[1] - old[1], w2 = nxt[2] - old[2];
-        const bool one = (e0 + e1 + e2 == 1) && ((e0 == 1) ? (w1 == 1 && w2 == 1)
-                                                 : (e1 == 1) ? (w0 == 1 && w2 == 1)
-                                                             : (w0 == 1 && w1 == 1));
-        if (one) {
-          visit(e0 ? nxt[0] - 1 : old[0], e1 ? nxt[1] - 1 : old[1], e2 ? nxt[2] - 1 : old[2],
-                e0 ? f_new[0] : f_old[0], e1 ? f_new[1] : f_old[1], e2 ? f_new[2] : f_old[2]);
-        } else {
-          for (int ux = old[0]; ux < nxt[0] && !to_list; ++ux) {
-            const float fx = exit_t(G, S, 0, ux);
-            for (int uy = old[1]; uy < nxt[1] && !to_list; ++uy) {
-              const float fy = exit_t(G, S, 1, uy);
-              for (int uz = old[2]; uz < nxt[2] && !to_list; ++uz) {
-                if (ux < ns[0] && uy < ns[1] && uz < ns[2]) continue;   // born earlier
-                visit(ux, uy, uz, fx, fy, exit_t(G, S, 2, uz));
-              }
-            }
-          }
-        }
-      }
-      if (to_list) break;
-      // Brick skip. After t, an axis's cells that can still form triples are
-      // the active ones with exit > t and the ones not yet entered. When
-      // that is one cell per axis (c) and c's 4x4x4 brick is empty, every
-      // triple born before t_j -- the first entry, on any axis, of a cell
-      // past the brick -- lies in the brick: those events are taken
-      // silently and the sweep resumes at the event t_j.
-      float tn = INFINITY;
-      bool skip = true;
-      int c[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const int wdt = nxt[a] - old[a];
-        c[a] = (wdt == 1) ? old[a] : old[a] + 1;
-        skip = skip && (wdt == 1 || (wdt == 2 && f_old[a] <= t));
-      }
-      if (skip) {
-        const int gi = S.sh[0] > 0.0f ? c[0] : G.n[0] - 1 - c[0];
-        const int gj = S.sh[1] > 0.0f ? c[1] : G.n[1] - 1 - c[1];
-        const int gk = S.sh[2] > 0.0f ? c[2] : G.n[2] - 1 - c[2];
-        const int64_t w = ((int64_t)(gk >> 2) * G.nb[1] + (gj >> 2)) * G.nb[0] + (gi >> 2);
-        if (w != cached) {
-          brick = __ldg(G.bricks + w);
-          cached = w;
-        }
-        skip = brick.x == 0ull;
-        if (skip) {
-          const int g3[3] = {gi, gj, gk};
-          int lim[3];
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const int rem = S.sh[a] > 0.0f ? 4 - (g3[a] & 3) : (g3[a] & 3) + 1;
-            lim[a] = min(G.n[a], c[a] + rem);
-            if (lim[a] < G.n[a]) tn = fminf(tn, entry_t(G, S, a, lim[a]));
-          }
-          if (!(tn <= 100000.0f)) break;          // nothing past this empty brick
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            while (nxt[a] < lim[a] && e_nxt[a] < tn) {
-              f_new[a] = exit_t(G, S, a, nxt[a]);
-              if (old[a] == nxt[a]) f_old[a] = f_new[a];
-              ++nxt[a];
-              e_nxt[a] = nxt[a] < G.n[a] ? entry_t(G, S, a, nxt[a]) : INFINITY;
-            }
-          }
-        }
-      }
-      // the next entry event
-      if (!skip) {
-        tn = fminf(e_nxt[0], fminf(e_nxt[1], e_nxt[2]));
-        if (!(tn <= 100000.0f)) break;
-      }
-      t = tn;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        while (old[a] < nxt[a] && f_old[a] < t) {
-          ++old[a];
-          f_old[a] = old[a] == nxt[a] - 1 ? f_new[a]
-                     : (old[a] < G.n[a] ? exit_t(G, S, a, old[a]) : 0.0f);
-        }
-        dead = dead || old[a] >= G.n[a];
-        ns[a] = nxt[a];
-        while (e_nxt[a] == t) {
-          f_new[a] = exit_t(G, S, a, nxt[a]);
-          if (old[a] == nxt[a]) f_old[a] = f_new[a];
-          ++nxt[a];
-          e_nxt[a] = nxt[a] < G.n[a] ? entry_t(G, S, a, nxt[a]) : INFINITY;
-        }
-      }
-    }
-  }
-  if (to_list) {
-    const int32_t q = atomicAdd(n_list, 1);
-    list[q] = (int32_t)r;
-  } else if (live) {
-    hits[r] = cnt > 0;
-  }
-  // pad the rows (misses: id -1, depths 10000), a warp per row
-  const bool pad = live && !to_list;
-  for (int q = 0; q < 32; ++q) {
-    const int cq = __shfl_sync(full, cnt, q);
-    if (!__shfl_sync(full, (int)pad, q)) continue;
-    const int64_t rq = base + q;
-    for (int l = cq + lane; l < n_max; l += 32) {
-      idx[rq * n_max + l] = -1;
-      min_depth[rq * n_max + l] = NSVF_MAX_DEPTH_F;
-      max_depth[rq * n_max + l] = NSVF_MAX_DEPTH_F;
-    }
-  }
   }
 }
 
-// The ray list's length and the persistent warps' ray counter start at 0.
-__global__ void zero_kernel(int32_t *n_list, unsigned long long *next_ray) {
+// Rays with more than n_max hits. The search keeps the first n_max leaves in
+// visiting order, then the encoder sorts them by (min_depth, visiting order).
+// The sweep wrote such a ray's first n_max hits to its row and the rest to
+// its overflow block; a warp per ray gathers both into shared memory, sorts
+// them by visiting rank, keeps the first n_max and sorts those by
+// (min_depth, rank). (Keeping the n_max smallest ranks in the row during the
+// sweep cost a rescan of the row through L2 per replacement, up to 2x the
+// sweep's time on views with many such rays; sweeping such rays again in a
+// second pass, one lane per ray, took 0.15 ms on the c2 frame.)
+constexpr int kOverWarps = 4;
+constexpr int kOverMax = 256;     // n_max (<= 128) + kOverExtra, rounded up
+
+// Bitonic sort of buf[0, P) (P a power of two) by key(), ascending, by the
+// 32 lanes of a warp.
+template <class Key>
+__device__ __forceinline__ void warp_bitonic(OverHit *buf, int P, int lane, Key key) {
+  for (int size = 2; size <= P; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = lane; i < P / 2; i += 32) {
+        const int a = 2 * i - (i & (stride - 1)), b = a + stride;
+        const bool asc = (a & size) == 0;
+        if ((key(buf[a]) > key(buf[b])) == asc) {
+          const OverHit x = buf[a];
+          buf[a] = buf[b];
+          buf[b] = x;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * kOverWarps) svo_grid_overflow_kernel(
+    int n_max, const int32_t *__restrict__ rank_of, int32_t *__restrict__ idx,
+    float *__restrict__ min_depth, float *__restrict__ max_depth, uint8_t *__restrict__ hits,
+    const int32_t *__restrict__ over, const int32_t *__restrict__ over_cnt,
+    const int32_t *__restrict__ n_over, const OverHit *__restrict__ scratch, int over_cap) {
+  __shared__ OverHit bufs[kOverWarps][kOverMax];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  OverHit *buf = bufs[w];
+  const int64_t n0 = *n_over, n = n0 < over_cap ? n0 : over_cap;
+  for (int64_t q = (int64_t)blockIdx.x * kOverWarps + w; q < n;
+       q += (int64_t)gridDim.x * kOverWarps) {
+    const int64_t r = over[q];
+    if (r < 0) continue;                     // the ray went to the depth-first kernel
+    const int e = over_cnt[q], k = n_max + e;
+    int32_t *I = idx + r * n_max;
+    float *LO = min_depth + r * n_max, *HI = max_depth + r * n_max;
+    for (int j = lane; j < n_max; j += 32)
+      buf[j] = OverHit{__float_as_uint(LO[j]), HI[j], I[j], __ldg(rank_of + I[j])};
+    for (int j = lane; j < e; j += 32) buf[n_max + j] = scratch[q * kOverExtra + j];
+    int P = 1;
+    while (P < k) P <<= 1;
+    for (int i = k + lane; i < P; i += 32) buf[i] = OverHit{0xffffffffu, 0.0f, -1, 0x7fffffff};
+    __syncwarp();
+    warp_bitonic(buf, P, lane, [](const OverHit &h) { return h.rank; });
+    // the first n_max ranks, by (min_depth, rank)
+    int P2 = 1;
+    while (P2 < n_max) P2 <<= 1;
+    for (int i = n_max + lane; i < P2; i += 32) buf[i] = OverHit{0xffffffffu, 0.0f, -1, 0x7fffffff};
+    __syncwarp();
+    warp_bitonic(buf, P2, lane, [](const OverHit &h) {
+      return ((unsigned long long)h.lo_bits << 32) | (unsigned)h.rank;
+    });
+    for (int j = lane; j < n_max; j += 32) {
+      I[j] = buf[j].id;
+      LO[j] = __uint_as_float(buf[j].lo_bits);
+      HI[j] = buf[j].hi;
+    }
+    if (lane == 0) hits[r] = 1;
+    __syncwarp();
+  }
+}
+
+// The lists' lengths and the persistent warps' ray counter start at 0.
+__global__ void zero_kernel(int32_t *n_list, int32_t *n_over, unsigned long long *next_ray) {
   *n_list = 0;
+  *n_over = 0;
   *next_ray = 0ull;
 }
 
@@ -648,7 +743,16 @@ int nsvf_svo_grid_info(const void *grid_host, int32_t *out) {
   return NSVF_OK;
 }
 
-int64_t nsvf_svo_grid_list_bytes(int64_t rays) { return 16 + 4 * (rays > 0 ? rays : 0); }
+// Overflow blocks of a call of `rays` rays: one per ray up to 32,768.
+static int64_t grid_over_cap(int64_t rays) { return rays < 32768 ? (rays > 0 ? rays : 0) : 32768; }
+
+int64_t nsvf_svo_grid_list_bytes(int64_t rays) {
+  const int64_t R = rays > 0 ? rays : 0, oc = grid_over_cap(R);
+  // counters, ray list, overflow slots (ray, hit count), then 16-byte
+  // aligned the overflow blocks
+  const int64_t blk_off = (16 + 4 * R + 8 * oc + 15) / 16 * 16;
+  return blk_off + oc * kOverExtra * (int64_t)sizeof(OverHit);
+}
 
 int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
                             const float *ray_start, const float *ray_dir, const float *points,
@@ -665,11 +769,20 @@ int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
       rays > 0x7fffffff)
     return NSVF_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  // list workspace: [0, 4) list length, [8, 16) ray counter, [16, ...) list
+  // list workspace: [0, 4) list length, [4, 8) overflow slots taken, [8, 16)
+  // ray counter, then the ray list (rays entries), the overflow slots' rays
+  // and hit counts (over_cap entries each) and, 16-byte aligned, the
+  // overflow blocks (over_cap x kOverExtra hits)
+  const int64_t over_cap = grid_over_cap(rays);
   int32_t *n_list = static_cast<int32_t *>(list_ws);
+  int32_t *n_over = n_list + 1;
   unsigned long long *next_ray =
       reinterpret_cast<unsigned long long *>(static_cast<unsigned char *>(list_ws) + 8);
   int32_t *list = n_list + 4;
+  int32_t *over = list + rays;
+  int32_t *over_cnt = over + over_cap;
+  const int64_t blk_off = (16 + 4 * rays + 8 * over_cap + 15) / 16 * 16;
+  OverHit *scratch = reinterpret_cast<OverHit *>(static_cast<unsigned char *>(list_ws) + blk_off);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return NSVF_ERR_CUDA;
   if (g_grid_blocks[dev] == 0) {
@@ -680,7 +793,7 @@ int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
       return NSVF_ERR_CUDA;
     g_grid_blocks[dev] = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   }
-  zero_kernel<<<1, 1, 0, s>>>(n_list, next_ray);
+  zero_kernel<<<1, 1, 0, s>>>(n_list, n_over, next_ray);
   int st = nsvf_launch_status();
   if (st != NSVF_OK) return st;
   const unsigned char *B = static_cast<const unsigned char *>(grid);
@@ -704,8 +817,18 @@ int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
   const int64_t need = (rays + kGridBlock - 1) / kGridBlock;
   const int blocks = (int)(need < g_grid_blocks[dev] ? need : g_grid_blocks[dev]);
   svo_grid_kernel<<<blocks, kGridBlock, 0, s>>>(rays, n_max, ray_start, ray_dir, G, idx,
-                                                min_depth, max_depth, hits, list, n_list,
+                                                min_depth, max_depth, hits, list, n_list, over,
+                                                over_cnt, n_over, scratch, (int)over_cap,
                                                 next_ray);
+  st = nsvf_launch_status();
+  if (st != NSVF_OK) return st;
+  // the overflow rays: their count is on the device; 8 blocks of 4 warps per
+  // SM stride over them
+  const int64_t over_blocks = (over_cap + kOverWarps - 1) / kOverWarps;
+  svo_grid_overflow_kernel<<<(int)(over_blocks < 152 * 8 ? over_blocks : 152 * 8),
+                             32 * kOverWarps, 0, s>>>(n_max, G.rank_of, idx, min_depth,
+                                                      max_depth, hits, over, over_cnt, n_over,
+                                                      scratch, (int)over_cap);
   st = nsvf_launch_status();
   if (st != NSVF_OK) return st;
   return nsvf_svo_sorted_list_launch(rays, rays, n, n_max, ray_start, ray_dir, packed, list,
