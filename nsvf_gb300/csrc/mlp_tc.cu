@@ -8,23 +8,29 @@
 // memory (108 KB) and streams 128-sample tiles through them: the hidden
 // activations never leave the SM.
 //
-// BF16 CTA = 18 warps. Two tile slots (TMEM columns [256 g, 256 g + 256):
-// accumulator D at +0, head output at +128, a constant ones block at +144,
-// the activations at +192). Warps 0-7 are the epilogue: all eight work on one
-// slot's layer at a time and alternate the slots, so one slot's MMAs run
-// while the other slot is converted. Warp 8 allocates TMEM; lane 0 of warp
-// 8 issues slot 0's tcgen05.mma instructions and lane 0 of warp 17 slot 1's,
-// so the two slots' chains never wait on each other's issue. Warps 9-16 are two loader
-// warpgroups that build the input tiles (embedding gathers and trilinear
-// interpolation) into a ring of shared-memory buffers. Per layer:
-//   MMA thread: a bias step (the ones block x a (hi, mid, lo) bf16 split of
+// BF16 CTA = 19 warps, three tile slots. A slot's chain of layers is latency
+// bound (each layer waits for the previous layer's epilogue), so the tensor
+// pipe is kept busy by running several slots' chains at once. Tensor memory
+// (512 columns) holds the three accumulators (128 columns each) and the
+// activations of two slots (64 columns each); the third slot's activations
+// live in shared memory, and each slot's head output reuses the first 16
+// columns of its accumulator. Warps 0-7 are the epilogue: all eight work on
+// one slot's layer at a time and take the slots in turn, so the other slots'
+// MMAs run while one slot is converted. Warp 8 allocates TMEM; lane 0 of
+// warps 8, 17 and 18 issues the tcgen05.mma instructions of slots 0, 1 and
+// 2, so the slots' chains never wait on each other's issue. Warps 9-16 are
+// two loader warpgroups that build the input tiles (embedding gathers and
+// trilinear interpolation) into a ring of shared-memory buffers. Per layer:
+//   MMA thread: a bias step (a ones block x a (hi, mid, lo) bf16 split of
 //   the bias, K = 16) that starts D at the bias, then the layer's K / 16
-//   MMAs with A = the previous activations in TMEM -> tcgen05.commit arrives
-//   on mma_done[g] -> each epilogue warp reads 64 columns of D
-//   (tcgen05.ld), applies ReLU, rounds to bf16 pairs and stores them back as
-//   the next layer's A (tcgen05.st) -> one arrival per warp on act_ready[g].
+//   MMAs with A = the previous activations -> tcgen05.commit arrives on
+//   mma_done[g] -> each epilogue warp reads 64 columns of D (tcgen05.ld),
+//   applies ReLU, rounds to bf16 pairs and stores them as the next layer's A
+//   (tcgen05.st, or st.shared for slot 2) -> one arrival per warp on
+//   act_ready[g].
 // The first layer reads its A (the input tile) from shared memory. The FP8
-// variant has the same structure; its three hidden layers are E4M3
+// variant has the same structure with two slots (18 warps, the head output
+// in columns of its own); its three hidden layers are E4M3
 // (kind::f8f6f4, K = 32 per MMA) with A = E4M3 activations in tensor memory
 // (four per column), its bias step holds bias / dq (the layer's
 // dequantisation), and its epilogue scales the accumulator by dq * qs
@@ -45,33 +51,45 @@ constexpr int TILE = 128;   // samples per MMA tile (M)
 constexpr int NB = 4;       // input tile ring depth
 constexpr uint32_t kTmemCols = 512;
 
-// Warp roles and tile slots (both variants): 18 warps; two tile slots of
-// 256 TMEM columns (accumulator at +0, head output at +128, ones block at
-// +144, E4M3 activations at +160 (FP8), BF16 activations at +192); epilogue
-// warps 0-7, MMA warps 8 (slot 0) and 17 (slot 1), loader warps 9-16.
+// Warp roles and tile slots. Epilogue warps 0-7, loader warps 9-16, one MMA
+// warp per slot (8, 17 and, for BF16, 18); each MMA warp's lane 0 issues one
+// slot's MMAs.
+//   BF16: three slots. Accumulator D of slot g at TMEM column 128 g; the
+//   bf16 activations (HID per row, two per column: 64 columns) of slots 0
+//   and 1 at 384 + 64 g, those of slot 2 in shared memory (act2). The
+//   head's 16 output columns are the first 16 of D, so the slot's next tile
+//   starts its first layer only after the epilogue has read the head
+//   (head_free).
+//   FP8: two slots of 256 columns: D at +0, head output at +128, E4M3
+//   activations (four per column: 32 columns) at +160, the head's bf16
+//   input at +192.
+// The bias step of every layer reads its A operand (rows of (1, 1, 1, 0,
+// ...)) from shared memory (ones_a).
 template <bool F8>
 struct Cfg {
-  static constexpr int kSlots = 2;
+  static constexpr int kSlots = F8 ? 2 : 3;
   static constexpr int kEpiWarps = 8;
   static constexpr int kLoaderWarp0 = kEpiWarps + 1;
   static constexpr int kMmaWarp = kEpiWarps;
-  static constexpr int kThreads = 18 * 32;
-  // a second MMA warp; each MMA warp's lane 0 issues one slot's MMAs
   static constexpr int kMmaWarp2 = kLoaderWarp0 + 8;
-  static constexpr uint32_t kSlotCols = 256u;
-  // TMEM column of slot g's (sigma, rgb) head output. The MMA lane issues
-  // the slot's next tile's first layer without waiting for the epilogue to
-  // read the head, so the head must not share columns with it.
-  __device__ static constexpr uint32_t head_col(int g) { return 256u * (uint32_t)g + 128u; }
-  // BF16 activations of slot g (HID bf16 per row, two per column: 64
-  // columns): the A operand of the BF16 hidden layers and of the head.
-  __device__ static constexpr uint32_t act_col(int g) { return 256u * (uint32_t)g + 192u; }
-  // FP8: E4M3 activations of slot g (HID per row, four per column: 32
-  // columns), the A operand of the E4M3 hidden layers.
+  static constexpr int kMmaWarp3 = kMmaWarp2 + 1;
+  static constexpr int kThreads = (16 + kSlots) * 32;
+  // the head's output shares columns with D (the next tile's first layer
+  // waits for the head to be read)
+  static constexpr bool kHeadInD = !F8;
+  __device__ static constexpr uint32_t d_col(int g) { return (F8 ? 256u : 128u) * (uint32_t)g; }
+  __device__ static constexpr uint32_t head_col(int g) {
+    return F8 ? 256u * (uint32_t)g + 128u : 128u * (uint32_t)g;
+  }
+  // bf16 activations in tensor memory: the A operand of the BF16 hidden
+  // layers and of the head (BF16 slots 0 and 1; both FP8 slots)
+  __device__ static constexpr uint32_t act_col(int g) {
+    return F8 ? 256u * (uint32_t)g + 192u : 384u + 64u * (uint32_t)g;
+  }
+  // BF16 slot 2 keeps its activations in shared memory
+  __device__ static constexpr bool act_in_smem(int g) { return !F8 && g == 2; }
+  // FP8: E4M3 activations of slot g, the A operand of the E4M3 hidden layers
   __device__ static constexpr uint32_t act8_col(int g) { return 256u * (uint32_t)g + 160u; }
-  // 8 columns holding bf16 (1, 1, 1, 0, ...) in every lane: the A operand of
-  // the hidden layers' bias step.
-  __device__ static constexpr uint32_t ones_col(int g) { return 256u * (uint32_t)g + 144u; }
   static constexpr int kHidBytes = F8 ? HID * HID : HID * HID * 2;  // one hidden weight matrix
 };
 
@@ -87,6 +105,9 @@ struct __align__(128) MlpSmem {
   // an A tile whose rows are (1, 1, 1, 0, ...).
   __nv_bfloat16 bias_b[4][HID * 16];
   __nv_bfloat16 ones_a[TILE * 16];
+  // BF16 slot 2's activations (K-major, TILE x HID): written by the epilogue,
+  // read by the slot's next layer
+  __nv_bfloat16 act2[F8 ? 8 : TILE * HID];
   // per loader warp: its 32 rows' corner keys (kSkipKey = skip) and
   // trilinear weights, written by the row's lane and read by the 8 lanes
   // that gather the row
@@ -98,6 +119,7 @@ struct __align__(128) MlpSmem {
   float bias4[NOUT];
   uint64_t mma_done[Cfg<F8>::kSlots][5];  // per slot and layer: one phase per tile
   uint64_t act_ready[Cfg<F8>::kSlots];    // epilogue -> MMA: hidden activations written
+  uint64_t head_free[Cfg<F8>::kSlots];    // epilogue -> MMA: head output read (kHeadInD)
   uint64_t in_full[NB];                   // loaders -> MMA: input tile written
   uint64_t in_empty[NB];                  // MMA -> loaders: first layer done reading
   uint32_t tmem_base;
@@ -459,6 +481,20 @@ __device__ __forceinline__ void epi_chunk(const float (&v)[32], uint32_t ta, int
   }
 }
 
+// The same for activations kept in shared memory (K-major, K = HID): row
+// `row`'s bf16 [c, c + 32) as four 16-byte chunks. The eight lanes of a
+// quarter warp hold rows 8 j .. 8 j + 7, one core matrix: no bank conflicts.
+__device__ __forceinline__ void epi_chunk_smem(const float (&v)[32], uint8_t *act, int row, int c) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint4 w = make_uint4(pack_relu_bf16x2(v[8 * q], v[8 * q + 1]),
+                               pack_relu_bf16x2(v[8 * q + 2], v[8 * q + 3]),
+                               pack_relu_bf16x2(v[8 * q + 4], v[8 * q + 5]),
+                               pack_relu_bf16x2(v[8 * q + 6], v[8 * q + 7]));
+    *reinterpret_cast<uint4 *>(act + kmajor_off(row, c + 8 * q, HID)) = w;
+  }
+}
+
 // Output stage of one row (the whole warp calls it): the head's 16 TMEM
 // columns at taddr, plus bias, to p.out as (sigma, r, g, b); or, for pruning,
 // the row's score reduced into its voxel's.
@@ -524,12 +560,11 @@ __device__ __forceinline__ void head_store(const MlpParams &p, const float *bias
 }
 
 // Persistent CTA (one per SM), roles as in Cfg:
-//   epilogue warps  ReLU + rounding of each hidden layer back to tensor
-//                   memory as the next layer's A operand, and the output
-//                   stage; all 8 warps on one slot's layer at a time,
-//                   alternating the slots;
-//   MMA warps       warp 8 allocates TMEM; lane 0 of warp 8 issues slot 0's
-//                   tcgen05.mma, lane 0 of warp 17 slot 1's;
+//   epilogue warps  ReLU + rounding of each hidden layer into the next
+//                   layer's A operand, and the output stage; all 8 warps on
+//                   one slot's layer at a time, taking the slots in turn;
+//   MMA warps       warp 8 allocates TMEM; lane 0 of warps 8, 17 (and 18)
+//                   issues the tcgen05.mma of slots 0, 1 (and 2);
 //   loader warps    two warpgroups that build the input tiles (the embedding
 //                   gathers and interpolation) into a ring of NB buffers
 //                   ahead of the MMAs.
@@ -572,6 +607,8 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       // one arrival per epilogue warp (lane 0, after the warp's fences and
       // a __syncwarp): all 8 warps work on each slot's layer
       mbar_init(&S.act_ready[g], C::kEpiWarps);
+      // one arrival per warp of the half that reads slot g's head
+      mbar_init(&S.head_free[g], 4);
     }
     for (int q = 0; q < NB; ++q) {
       mbar_init(&S.in_full[q], 4);    // one arrival per loader warp
@@ -586,20 +623,6 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = S.tmem_base;
-  {
-    // each slot's ones block in tensor memory (the A operand of the hidden
-    // layers' bias step), written once by warps 0-3 (lane quarter = warp)
-    // and never changed
-    if (warp < 4) {
-      const uint32_t ones[8] = {kOnes2, kOne, 0u, 0u, 0u, 0u, 0u, 0u};
-      for (int g = 0; g < C::kSlots; ++g)
-        tmem_st8(tmem + ((uint32_t)(warp * 32) << 16) + C::ones_col(g), ones);
-      tmem_wait_st();
-    }
-    fence_before_sync();
-    __syncthreads();
-    fence_after_sync();
-  }
   volatile int *abort = &S.abort;
   // With ns_dev the row count comes from device memory (a count produced by
   // an earlier kernel on the stream), clamped to the buffers' capacity p.ns.
@@ -613,16 +636,16 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
   const int64_t G = gridDim.x, b = blockIdx.x;
   auto tile_of = [&](int64_t i) { return b + i * G; };
 
-  const bool mma_role = warp == C::kMmaWarp || warp == C::kMmaWarp2;
+  const bool mma_role = warp == C::kMmaWarp || warp == C::kMmaWarp2 ||
+                        (C::kSlots > 2 && warp == C::kMmaWarp3);
   const bool loader_role = warp >= C::kLoaderWarp0 && warp < C::kLoaderWarp0 + 8;
   if (mma_role) {
     // One issuing thread per slot, so a slot whose activations are ready
-    // never waits behind the other slot's issue: lane 0 of kMmaWarp (slot 0)
-    // and of kMmaWarp2 (slot 1).
-    const int issue_slot = warp == C::kMmaWarp ? 0 : 1;
-    if (issue_slot >= 0 && lane == 0) {
-      const int g_lo = issue_slot, g_hi = issue_slot + 1;
-      uint32_t ph_act[C::kSlots] = {};
+    // never waits behind another slot's issue: lane 0 of kMmaWarp (slot 0),
+    // kMmaWarp2 (slot 1) and kMmaWarp3 (slot 2).
+    const int g = warp == C::kMmaWarp ? 0 : warp == C::kMmaWarp2 ? 1 : 2;
+    if (lane == 0) {
+      uint32_t ph_act = 0, ph_head = 0;
       bool ok = true;
       // Descriptors, computed once: the first layer's weights and input
       // ring buffer 0 (buffer q is 8 KB further: + 512 in the address
@@ -638,51 +661,59 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       const uint64_t d_ones = sdesc(smem_u32(S.ones_a), 128u, 256u);
       const uint64_t d_bias = sdesc(smem_u32(S.bias_b[0]), 128u, 256u);
       const uint64_t d_w4 = sdesc(smem_u32(S.w4), 128u, (HID / 8) * 128u);
+      // slot 2's shared-memory activations (BF16 only)
+      const uint64_t d_act2 = sdesc(smem_u32(S.act2), 128u, (HID / 8) * 128u);
+      const bool smem_act = C::act_in_smem(g);
+      const uint32_t d = tmem + C::d_col(g);
       static_assert(sizeof(S.ain[0]) == 8192 && C::kHidBytes % 16 == 0, "descriptor steps");
 #pragma unroll 1
-      for (int64_t i = 0; ok; i += C::kSlots) {
-        if (tile_of(i) >= n_tiles) break;
+      for (int64_t ii = g; ok; ii += C::kSlots) {
+        if (tile_of(ii) >= n_tiles) break;
 #pragma unroll 1
-        for (int layer = 0; layer < 5 && ok; ++layer) {
-#pragma unroll 1
-          for (int g = g_lo; g < g_hi && ok; ++g) {
-            const int64_t ii = i + g;
-            if (tile_of(ii) >= n_tiles) break;
-            const uint32_t d = tmem + C::kSlotCols * g;
-            if (layer == 0) {
-              int q = (int)(ii % NB);
-              if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
-              fence_after_sync();
-              // bias step (overwrites D), then the layer accumulating onto it
-              mma_bf16(d, d_ones, d_bias, idesc_bf16_f32(TILE, HID), 0u);
-              issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
-              mma_commit(&S.mma_done[g][0]);
-              mma_commit(&S.in_empty[q]);
-            } else {
-              if (!mbar_wait(&S.act_ready[g], ph_act[g], abort)) { ok = false; break; }
-              ph_act[g] ^= 1u;
-              fence_after_sync();
-              if (layer < 4) {
-                // bias step (bias / dq, bf16), then the layer accumulating
-                // onto it: BF16 K steps of 16 with A = the bf16 activations,
-                // or E4M3 K steps of 32 with A = the E4M3 activations
-                mma_bf16_ts(d, tmem + C::ones_col(g), d_bias + 256u * (uint32_t)layer,
-                            idesc_bf16_f32(TILE, HID), 0u);
-                const uint64_t bd = d_wh + kHidStep * (uint32_t)(layer - 1);
-                if constexpr (F8) {
-#pragma unroll
-                  for (int k = 0; k < HID / 32; ++k)
-                    mma_e4m3_ts(d, tmem + C::act8_col(g) + 8u * k, bd + 16u * k,
-                                idesc_e4m3_f32(TILE, HID), 1u);
-                } else {
-                  issue_ts<HID / 16, true>(d, tmem + C::act_col(g), bd, idesc_bf16_f32(TILE, HID));
-                }
-              } else {
-                issue_ts<HID / 16, false>(tmem + C::head_col(g), tmem + C::act_col(g), d_w4,
-                                          idesc_bf16_f32(TILE, NOUT));
-              }
-              mma_commit(&S.mma_done[g][layer]);
+        for (int layer = 0; layer < 5; ++layer) {
+          if (layer == 0) {
+            int q = (int)(ii % NB);
+            if (!mbar_wait(&S.in_full[q], (uint32_t)((ii / NB) & 1), abort)) { ok = false; break; }
+            // the slot's previous head must have been read before the
+            // first layer overwrites D
+            if (C::kHeadInD && ii >= C::kSlots) {
+              if (!mbar_wait(&S.head_free[g], ph_head, abort)) { ok = false; break; }
+              ph_head ^= 1u;
             }
+            fence_after_sync();
+            // bias step (overwrites D), then the layer accumulating onto it
+            mma_bf16(d, d_ones, d_bias, idesc_bf16_f32(TILE, HID), 0u);
+            issue_ss<E / 16, true>(d, d_in0 + 512u * (uint32_t)q, d_w0, idesc_bf16_f32(TILE, HID));
+            mma_commit(&S.mma_done[g][0]);
+            mma_commit(&S.in_empty[q]);
+          } else {
+            if (!mbar_wait(&S.act_ready[g], ph_act, abort)) { ok = false; break; }
+            ph_act ^= 1u;
+            fence_after_sync();
+            if (layer < 4) {
+              // bias step (bias / dq, bf16), then the layer accumulating
+              // onto it: BF16 K steps of 16 with A = the bf16 activations,
+              // or E4M3 K steps of 32 with A = the E4M3 activations
+              mma_bf16(d, d_ones, d_bias + 256u * (uint32_t)layer, idesc_bf16_f32(TILE, HID), 0u);
+              const uint64_t bd = d_wh + kHidStep * (uint32_t)(layer - 1);
+              if constexpr (F8) {
+#pragma unroll
+                for (int k = 0; k < HID / 32; ++k)
+                  mma_e4m3_ts(d, tmem + C::act8_col(g) + 8u * k, bd + 16u * k,
+                              idesc_e4m3_f32(TILE, HID), 1u);
+              } else if (smem_act) {
+                issue_ss<HID / 16, true>(d, d_act2, bd, idesc_bf16_f32(TILE, HID));
+              } else {
+                issue_ts<HID / 16, true>(d, tmem + C::act_col(g), bd, idesc_bf16_f32(TILE, HID));
+              }
+            } else if (smem_act) {
+              issue_ss<HID / 16, false>(tmem + C::head_col(g), d_act2, d_w4,
+                                        idesc_bf16_f32(TILE, NOUT));
+            } else {
+              issue_ts<HID / 16, false>(tmem + C::head_col(g), tmem + C::act_col(g), d_w4,
+                                        idesc_bf16_f32(TILE, NOUT));
+            }
+            mma_commit(&S.mma_done[g][layer]);
           }
         }
       }
@@ -763,18 +794,20 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     // unwind.
     {
       // The 8 warps work on one slot's layer at a time (warp w: TMEM lane
-      // quarter w & 3, columns [64 (w >> 2), + 64)) and alternate the two
-      // slots layer by layer, so that one slot's MMAs run while the warps
-      // convert the other slot's activations. The MMA lanes issue in the
-      // same order (per tile pair: layer by layer, slot 0 then slot 1).
+      // quarter w & 3, columns [64 (w >> 2), + 64)) and take the slots in
+      // turn layer by layer, so that the other slots' MMAs run while the
+      // warps convert one slot's activations. The MMA lanes issue in the
+      // same order (per group of kSlots tiles: layer by layer, slot by slot).
       const int q4 = warp & 3, h = warp >> 2;
       const int row = q4 * 32 + lane;
       const uint32_t tq = tmem + ((uint32_t)(q4 * 32) << 16);
+      uint8_t *act2 = reinterpret_cast<uint8_t *>(S.act2);
       bool ok = true;
-      for (int64_t i = 0; ok; i += 2) {
+      for (int64_t i = 0; ok; i += C::kSlots) {
         if (tile_of(i) >= n_tiles) break;
-        const int ng = tile_of(i + 1) < n_tiles ? 2 : 1;
-        const uint32_t par = (uint32_t)((i / 2) & 1);
+        int ng = 1;
+        while (ng < C::kSlots && tile_of(i + ng) < n_tiles) ++ng;
+        const uint32_t par = (uint32_t)((i / C::kSlots) & 1);
         for (int layer = 0; layer < 4 && ok; ++layer) {
           for (int g = 0; g < ng; ++g) {
             if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][layer], par, abort))) {
@@ -782,17 +815,23 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
               break;
             }
             fence_after_sync();
-            const uint32_t tl = tq + C::kSlotCols * g + 64 * h;
+            const uint32_t tl = tq + C::d_col(g) + 64 * h;
             // the next layer's A operand: bf16 pairs (BF16, and the FP8
             // variant's head input) or E4M3 quadruples (FP8 hidden layers)
             const uint32_t ta = tq + C::act_col(g), ta8 = tq + C::act8_col(g);
             // two 32-column chunks, the second one's TMEM load in flight
-            // while the first is converted and stored back to tensor memory
+            // while the first is converted and stored
             float va[32], vb[32];
             tmem_ld32(tl, va);
             tmem_wait_ld_bind(va);
             tmem_ld32(tl + 32, vb);
-            if (!F8) {
+            if (!F8 && C::act_in_smem(g)) {
+              epi_chunk_smem(va, act2, row, 64 * h);
+              tmem_wait_ld_bind(vb);
+              epi_chunk_smem(vb, act2, row, 64 * h + 32);
+              // the generic-proxy stores, before the MMA's async-proxy reads
+              fence_async_smem();
+            } else if (!F8) {
               epi_chunk(va, ta, 64 * h);
               tmem_wait_ld_bind(vb);
               epi_chunk(vb, ta, 64 * h + 32);
@@ -814,11 +853,18 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
           }
         }
         if (!ok) break;
-        // the head of slot g is written by the warps of half h == g
-        if (h < ng) {
-          if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[h][4], par, abort))) break;
+        // the head of slot g is read by the warps of half g & 1
+        for (int g = h; g < ng; g += 2) {
+          if (!__all_sync(0xffffffffu, mbar_wait(&S.mma_done[g][4], par, abort))) {
+            ok = false;
+            break;
+          }
           fence_after_sync();
-          head_store<MODE>(p, S.bias4, tq + C::head_col(h), tile_of(i + h) * TILE + row, ns, lane);
+          head_store<MODE>(p, S.bias4, tq + C::head_col(g), tile_of(i + g) * TILE + row, ns, lane);
+          if (C::kHeadInD) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.head_free[g]);
+          }
         }
       }
     }
@@ -831,6 +877,11 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
     tmem_dealloc(tmem, kTmemCols);
   }
 }
+
+// Shared memory per CTA (plus 1 KB for the 1024-byte alignment of the
+// dynamic buffer) within the 227 KB an SM gives one block.
+static_assert(sizeof(MlpSmem<false>) + 1024 <= 232448 && sizeof(MlpSmem<true>) + 1024 <= 232448,
+              "shared memory");
 
 int g_num_sms = 0;
 
