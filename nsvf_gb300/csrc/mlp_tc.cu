@@ -819,28 +819,32 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
             // the next layer's A operand: bf16 pairs (BF16, and the FP8
             // variant's head input) or E4M3 quadruples (FP8 hidden layers)
             const uint32_t ta = tq + C::act_col(g), ta8 = tq + C::act8_col(g);
-            // two 32-column chunks, the second one's TMEM load in flight
-            // while the first is converted and stored
+            // two 32-column chunks: BF16 loads both before one wait; FP8
+            // (more registers in its conversion) converts the first while
+            // the second one's load is in flight
             float va[32], vb[32];
             tmem_ld32(tl, va);
+            if (!F8) tmem_ld32(tl + 32, vb);
             tmem_wait_ld_bind(va);
-            tmem_ld32(tl + 32, vb);
-            if (!F8 && C::act_in_smem(g)) {
-              epi_chunk_smem(va, act2, row, 64 * h);
+            if (!F8) {
               tmem_wait_ld_bind(vb);
-              epi_chunk_smem(vb, act2, row, 64 * h + 32);
-              // the generic-proxy stores, before the MMA's async-proxy reads
-              fence_async_smem();
-            } else if (!F8) {
-              epi_chunk(va, ta, 64 * h);
-              tmem_wait_ld_bind(vb);
-              epi_chunk(vb, ta, 64 * h + 32);
+              if (C::act_in_smem(g)) {
+                epi_chunk_smem(va, act2, row, 64 * h);
+                epi_chunk_smem(vb, act2, row, 64 * h + 32);
+                // the generic-proxy stores, before the MMA's async-proxy reads
+                fence_async_smem();
+              } else {
+                epi_chunk(va, ta, 64 * h);
+                epi_chunk(vb, ta, 64 * h + 32);
+              }
             } else if (layer < 3) {
+              tmem_ld32(tl + 32, vb);
               const float dqs = p.dqs[layer];
               epi_chunk8(va, dqs, ta8, 64 * h);
               tmem_wait_ld_bind(vb);
               epi_chunk8(vb, dqs, ta8, 64 * h + 32);
             } else {
+              tmem_ld32(tl + 32, vb);
               const float dq = p.dq[layer];
               epi_chunk_dq(va, dq, ta, 64 * h);
               tmem_wait_ld_bind(vb);
