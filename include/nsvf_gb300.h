@@ -459,6 +459,39 @@ int nsvf_sample_compact_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int 
                                const int64_t *offset, int64_t sample_cap, int32_t *voxel,
                                float *xyz_dist, float *depth, int32_t *err, void *stream);
 
+/* sample_scan_compact_dev / _pieces: nsvf_sample_count_dev (or _pieces),
+ * the exclusive prefix sum of the counts into offset, and
+ * nsvf_sample_compact_dev (or _pieces) in one pass. Blocks of 8 rows take
+ * their rows in ticket order and find their first sample by a look-back over
+ * the earlier blocks' published counts. The outputs are those of the three
+ * steps: the same samples at the same positions, offset[r] for r < *n_rows_dev
+ * and the total at offset[*n_rows_dev] and offset[rows_cap] (entries in
+ * between are not written). scan_ws: device workspace of
+ * nsvf_sample_scan_bytes(rows_cap) bytes, 8-byte aligned, zeroed by the call
+ * on the stream (NSVF_ERR_CAPACITY if smaller). Rows with max_hits > 128 are
+ * refused (NSVF_ERR_INVALID): use the two-pass entry points. A look-back
+ * that waits too long sets err bit 8. Replaces the count and compaction
+ * launches of the served chain's sampling (fairnr/clib/src/sample_gpu.cu:
+ * 108-202 for one ray's samples). */
+int64_t nsvf_sample_scan_bytes(int64_t rows_cap);
+int nsvf_sample_scan_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                                 const int32_t *pts_idx, const float *min_depth,
+                                 const float *max_depth, const float *probs, const float *steps,
+                                 const float *ray_start, int64_t ray_start_stride,
+                                 const float *ray_dir, const int64_t *ray_index, int64_t *offset,
+                                 int64_t sample_cap, int32_t *voxel, float *xyz_dist, float *depth,
+                                 void *scan_ws, int64_t scan_ws_bytes, int32_t *err,
+                                 void *stream);
+int nsvf_sample_scan_compact_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                                    const int32_t *pts_idx, const float *min_depth,
+                                    const float *max_depth, const float *probs,
+                                    const float *steps, const int64_t *piece_rows, int max_pieces,
+                                    const float *ray_start, int64_t ray_start_stride,
+                                    const float *ray_dir, const int64_t *ray_index,
+                                    int64_t *offset, int64_t sample_cap, int32_t *voxel,
+                                    float *xyz_dist, float *depth, void *scan_ws,
+                                    int64_t scan_ws_bytes, int32_t *err, void *stream);
+
 /* composite_segments_dev: nsvf_composite_segments over *n_rays_dev rays,
  * each ray's segment [offset[r], offset[r + 1]) clamped to the sample
  * buffers' capacity sample_cap (a frame whose samples overflowed them -- the

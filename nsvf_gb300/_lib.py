@@ -75,6 +75,11 @@ def _load():
         "nsvf_sample_count_dev": ([i64, P, i32, P, P, P, P, P, P, P], i32),
         "nsvf_sample_compact_dev": ([i64, P, i32, P, P, P, P, P, P, i64, P, P, P, i64, P, P, P,
                                      P, P], i32),
+        "nsvf_sample_scan_bytes": ([i64], i64),
+        "nsvf_sample_scan_compact_dev": ([i64, P, i32, P, P, P, P, P, P, i64, P, P, P, i64, P, P,
+                                          P, P, i64, P, P], i32),
+        "nsvf_sample_scan_compact_pieces": ([i64, P, i32, P, P, P, P, P, P, i32, P, i64, P, P, P,
+                                             i64, P, P, P, P, i64, P, P], i32),
         "nsvf_composite_segments_dev": ([i64, P, P, i64, P, P, P, P, f32, P, f32, P, P, P, i32, P],
                                         i32),
         "nsvf_field_samples_bf16_dev": ([i64, P, P, P, i64, i64, f32, P, P, P, P, P, P, P, P, i64,
@@ -126,4 +131,5 @@ def exported_symbols():
         "nsvf_field_refine_fp32_dev", "nsvf_parallel_ray_sampling",
         "nsvf_parallel_sampling_smem_bytes", "nsvf_pinhole_rays_multi", "nsvf_piece_rows",
         "nsvf_sample_count_pieces", "nsvf_sample_compact_pieces",
+        "nsvf_sample_scan_bytes", "nsvf_sample_scan_compact_dev", "nsvf_sample_scan_compact_pieces",
     ]

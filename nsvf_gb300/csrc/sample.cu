@@ -453,6 +453,93 @@ struct TailWrite {
   }
 };
 
+// The samples of row r (table T, walk state w, built by build_tab) written
+// to [start, end) of the compacted buffers, clipped to sample_cap; a count
+// that differs from end - start, or an end past sample_cap, sets bit 2 of
+// *err. All 32 lanes call it.
+__device__ __forceinline__ void warp_write_samples(
+    const RayTab &T, const WarpRay &w, int H, int64_t r, int64_t tail, int64_t nxt, int lane,
+    const int32_t *__restrict__ pts_idx, const float *__restrict__ min_depth,
+    const float *__restrict__ max_depth, const float *__restrict__ probs,
+    const float *__restrict__ steps, const float *__restrict__ ray_start,
+    int64_t ray_start_stride, const float *__restrict__ ray_dir,
+    const int64_t *__restrict__ ray_index, int64_t start, int64_t end, int64_t sample_cap,
+    int32_t *__restrict__ vox, float4 *__restrict__ xyzd, float *__restrict__ depth,
+    int32_t *__restrict__ err) {
+  const int32_t *I = pts_idx + r * H;
+  const int64_t rr = ray_index ? ray_index[r] : r;
+  const float *o = ray_start + rr * ray_start_stride;
+  if (w.B == 0) {
+    // an empty first slot: the per-thread walk on lane 0
+    if (lane == 0) {
+      int64_t e = end < sample_cap ? end : sample_cap;
+      CompactEmit em{vox, xyzd, depth, o[0], o[1], o[2], ray_dir[rr * 3], ray_dir[rr * 3 + 1],
+                     ray_dir[rr * 3 + 2], start < e ? start : e, e};
+      bool over = icdf_walk(H, I, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H,
+                            max_depth + r * H, probs + r * H, steps[r], nullptr, 0, -1.0f, em);
+      if ((over || em.pos != end) && err) atomicOr(err, 2);
+    }
+    return;
+  }
+  const float ox = o[0], oy = o[1], oz = o[2];
+  const float dx = ray_dir[rr * 3], dy = ray_dir[rr * 3 + 1], dz = ray_dir[rr * 3 + 2];
+  const int64_t base = start, lim = end < sample_cap ? end : sample_cap;
+  // Sample j's lower edge is sample j - 1's depth z when both are steps of
+  // one bin: lane - 1 computed it (lane 31 of the previous round for lane
+  // 0), so each step's division runs once.
+  float z_last = 0.0f;
+  for (int j0 = 0; j0 < w.M; j0 += 32) {
+    const int j = j0 + lane;
+    TabStep sp;
+    if (j < w.M) sp = tab_step(T, w, j);
+    float z_prev = __shfl_up_sync(0xffffffffu, sp.z, 1);
+    if (lane == 0) z_prev = z_last;
+    z_last = __shfl_sync(0xffffffffu, sp.z, 31);
+    if (j < w.M) {
+      int32_t id;
+      float t, dist;
+      tab_finish(T, w, sp, z_prev, id, t, dist);
+      const int64_t pos = base + j;
+      if (pos < lim) {
+        vox[pos] = id;
+        xyzd[pos] = make_float4(__fadd_rn(ox, __fmul_rn(dx, t)), __fadd_rn(oy, __fmul_rn(dy, t)),
+                                __fadd_rn(oz, __fmul_rn(dz, t)), fmaxf(dist, 0.0f));
+        depth[pos] = t;
+      }
+    }
+  }
+  if (lane == 0) {
+    TailWrite tw{vox, xyzd, depth, ox, oy, oz, dx, dy, dz, base + w.M, lim, false};
+    if (base + w.M > lim) tw.over = true;
+    tab_tail(T, w, H, pts_idx + tail * H, pts_idx, nxt, tw);
+    if ((tw.over || tw.pos != end || end > sample_cap) && err) atomicOr(err, 2);
+  }
+}
+
+// The number of samples of row r (lane 0's value; the table is built).
+__device__ __forceinline__ int warp_count_samples(const RayTab &T, const WarpRay &w, int H,
+                                                  int64_t r, int64_t tail, int64_t nxt, int lane,
+                                                  const int32_t *__restrict__ pts_idx,
+                                                  const float *__restrict__ min_depth,
+                                                  const float *__restrict__ max_depth,
+                                                  const float *__restrict__ probs,
+                                                  const float *__restrict__ steps) {
+  int n = 0;
+  if (lane == 0) {
+    if (w.B == 0) {
+      CountEmit em{0};
+      icdf_walk(H, pts_idx + r * H, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H,
+                max_depth + r * H, probs + r * H, steps[r], nullptr, 0, -1.0f, em);
+      n = em.n;
+    } else {
+      TailCount tc{0};
+      tab_tail(T, w, H, pts_idx + tail * H, pts_idx, nxt, tc);
+      n = w.M + tc.n;
+    }
+  }
+  return n;
+}
+
 // WRITE = false: count[r] = number of valid samples of row r (rows past the
 // device-side row count get 0). WRITE = true: the samples, compacted at
 // offset[r].
@@ -483,75 +570,28 @@ __global__ void __launch_bounds__(32 * kWarpRays) icdf_warp_kernel(
     const int32_t *I = pts_idx + r * H;
     WarpRay w = build_tab(T, H, I, min_depth + r * H, max_depth + r * H, probs + r * H,
                           steps[r], lane);
-    if (w.B == 0) {
-      // an empty first slot: the per-thread walk on lane 0
-      if (lane == 0) {
-        if (!WRITE) {
-          CountEmit em{0};
-          icdf_walk(H, I, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H, max_depth + r * H,
-                    probs + r * H, steps[r], nullptr, 0, -1.0f, em);
-          count[r] = em.n;
-        } else {
-          int64_t rr = ray_index ? ray_index[r] : r;
-          const float *o = ray_start + rr * ray_start_stride;
-          int64_t e = offset[r + 1] < sample_cap ? offset[r + 1] : sample_cap;
-          CompactEmit em{vox, xyzd, depth, o[0], o[1], o[2], ray_dir[rr * 3], ray_dir[rr * 3 + 1],
-                         ray_dir[rr * 3 + 2], offset[r] < e ? offset[r] : e, e};
-          bool over = icdf_walk(H, I, pts_idx + tail * H, pts_idx, nxt, min_depth + r * H,
-                                max_depth + r * H, probs + r * H, steps[r], nullptr, 0, -1.0f,
-                                em);
-          if ((over || em.pos != offset[r + 1]) && err) atomicOr(err, 2);
-        }
-      }
-      __syncwarp();
-      continue;
-    }
     if (!WRITE) {
-      if (lane == 0) {
-        TailCount tc{0};
-        tab_tail(T, w, H, pts_idx + tail * H, pts_idx, nxt, tc);
-        count[r] = w.M + tc.n;
-      }
+      const int n = warp_count_samples(T, w, H, r, tail, nxt, lane, pts_idx, min_depth,
+                                       max_depth, probs, steps);
+      if (lane == 0) count[r] = n;
     } else {
-      const int64_t rr = ray_index ? ray_index[r] : r;
-      const float *o = ray_start + rr * ray_start_stride;
-      const float ox = o[0], oy = o[1], oz = o[2];
-      const float dx = ray_dir[rr * 3], dy = ray_dir[rr * 3 + 1], dz = ray_dir[rr * 3 + 2];
-      const int64_t base = offset[r], lim = offset[r + 1] < sample_cap ? offset[r + 1] : sample_cap;
-      // Sample j's lower edge is sample j - 1's depth z when both are steps
-      // of one bin: lane - 1 computed it (lane 31 of the previous round for
-      // lane 0), so each step's division runs once.
-      float z_last = 0.0f;
-      for (int j0 = 0; j0 < w.M; j0 += 32) {
-        const int j = j0 + lane;
-        TabStep sp;
-        if (j < w.M) sp = tab_step(T, w, j);
-        float z_prev = __shfl_up_sync(0xffffffffu, sp.z, 1);
-        if (lane == 0) z_prev = z_last;
-        z_last = __shfl_sync(0xffffffffu, sp.z, 31);
-        if (j < w.M) {
-          int32_t id;
-          float t, dist;
-          tab_finish(T, w, sp, z_prev, id, t, dist);
-          const int64_t pos = base + j;
-          if (pos < lim) {
-            vox[pos] = id;
-            xyzd[pos] = make_float4(__fadd_rn(ox, __fmul_rn(dx, t)), __fadd_rn(oy, __fmul_rn(dy, t)),
-                                    __fadd_rn(oz, __fmul_rn(dz, t)), fmaxf(dist, 0.0f));
-            depth[pos] = t;
-          }
-        }
-      }
-      if (lane == 0) {
-        TailWrite tw{vox, xyzd, depth, ox, oy, oz, dx, dy, dz, base + w.M, lim, false};
-        if (base + w.M > lim) tw.over = true;
-        tab_tail(T, w, H, pts_idx + tail * H, pts_idx, nxt, tw);
-        if ((tw.over || tw.pos != offset[r + 1] || offset[r + 1] > sample_cap) && err)
-          atomicOr(err, 2);
-      }
+      warp_write_samples(T, w, H, r, tail, nxt, lane, pts_idx, min_depth, max_depth, probs, steps,
+                         ray_start, ray_start_stride, ray_dir, ray_index, offset[r],
+                         offset[r + 1], sample_cap, vox, xyzd, depth, err);
     }
     __syncwarp();                          // the table is rebuilt for the next ray
   }
+}
+
+int scan_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  return sms;
 }
 
 // Blocks for the warp-per-ray kernels: enough warps to cover the rows (or
@@ -567,6 +607,116 @@ int warp_grid(int64_t rows) {
   int64_t want = (rows + kWarpRays - 1) / kWarpRays;
   int64_t lim = (int64_t)sms * 16;
   return (int)(want < 1 ? 1 : (want < lim ? want : lim));
+}
+
+// Count and compaction in one pass (served path, warp per ray). Blocks take
+// chunks of kWarpRays consecutive rows in ticket order (scan[0]); a block
+// counts its rows' samples, publishes the chunk's count in scan[1 + c]
+// (kScanAgg), finds the samples of all earlier chunks by a look-back over
+// their published words (one warp, 32 chunks per step, stopping at the
+// nearest chunk whose inclusive total is known: kScanInc), publishes its own
+// inclusive total, and writes its rows' samples from there. offset[r] is the
+// exclusive prefix sum of the counts, as the count pass and a prefix sum
+// give it; the total is written to offset[rows] and offset[rows_cap]. A
+// chunk's predecessors took their tickets first and publish their counts
+// before they look back, so every wait ends; each is still bounded (bit 8
+// of *err when one gives up).
+constexpr unsigned long long kScanAgg = 1ull << 62, kScanInc = 2ull << 62;
+constexpr unsigned long long kScanVal = (1ull << 62) - 1;
+
+__device__ __forceinline__ unsigned long long scan_load(const unsigned long long *p) {
+  return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+
+__global__ void __launch_bounds__(32 * kWarpRays) icdf_scan_kernel(
+    int64_t rows_cap, int H, const int32_t *__restrict__ pts_idx,
+    const float *__restrict__ min_depth, const float *__restrict__ max_depth,
+    const float *__restrict__ probs, const float *__restrict__ steps,
+    const int64_t *__restrict__ n_dev, const float *__restrict__ ray_start,
+    int64_t ray_start_stride, const float *__restrict__ ray_dir,
+    const int64_t *__restrict__ ray_index, int64_t *__restrict__ offset, int64_t sample_cap,
+    int32_t *__restrict__ vox, float4 *__restrict__ xyzd, float *__restrict__ depth,
+    unsigned long long *__restrict__ scan, int32_t *__restrict__ err,
+    const int64_t *__restrict__ piece_rows, int max_pieces) {
+  __shared__ RayTab tabs[kWarpRays];
+  __shared__ int s_cnt[kWarpRays];
+  __shared__ long long s_chunk, s_base;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  RayTab &T = tabs[wib];
+  int64_t rows = rows_cap, K = 1, C = 1, N = 1, G = 1;
+  dyn_rows(n_dev, rows_cap, rows, K, C, N, G);
+  const int64_t n_chunks = (rows + kWarpRays - 1) / kWarpRays;
+  if (n_chunks == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) offset[0] = offset[rows_cap] = 0;
+    return;
+  }
+  unsigned long long *status = scan + 1;
+  for (;;) {
+    if (threadIdx.x == 0) s_chunk = (long long)atomicAdd(scan, 1ull);
+    __syncthreads();
+    const int64_t c = s_chunk;
+    if (c >= n_chunks) break;
+    const int64_t r = c * kWarpRays + wib;
+    WarpRay w{};
+    int64_t tail = 0, nxt = -1;
+    int n = 0;
+    if (r < rows) {
+      row_layout(r, K, C, N, G, piece_rows, max_pieces, tail, nxt);
+      w = build_tab(T, H, pts_idx + r * H, min_depth + r * H, max_depth + r * H, probs + r * H,
+                    steps[r], lane);
+      n = warp_count_samples(T, w, H, r, tail, nxt, lane, pts_idx, min_depth, max_depth, probs,
+                             steps);
+    }
+    if (lane == 0) s_cnt[wib] = n;
+    __syncthreads();
+    if (wib == 0) {
+      unsigned long long agg = 0;
+      for (int k = 0; k < kWarpRays; ++k) agg += (unsigned long long)s_cnt[k];
+      unsigned long long prefix = 0;
+      if (c == 0) {
+        if (lane == 0) atomicExch(status, kScanInc | agg);
+      } else {
+        if (lane == 0) atomicExch(status + c, kScanAgg | agg);
+        // look back 32 chunks at a time: lane k reads chunk j - k
+        int64_t j = c - 1;
+        bool ok = true;
+        for (;;) {
+          const int64_t jj = j - lane;
+          unsigned long long v = jj >= 0 ? scan_load(status + jj) : kScanInc;
+          for (int it = 0; !__all_sync(0xffffffffu, v != 0ull); ++it) {
+            if (it > (1 << 22)) { ok = false; break; }
+            __nanosleep(32);
+            if (v == 0ull) v = scan_load(status + jj);
+          }
+          if (!ok) break;
+          // the nearest chunk with an inclusive total ends this step's sum
+          const unsigned inc = __ballot_sync(0xffffffffu, (v & kScanInc) != 0ull);
+          const int stop = inc ? __ffs(inc) - 1 : 31;
+          unsigned long long part = lane <= stop ? (v & kScanVal) : 0ull;
+          for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+          prefix += part;
+          if (inc) break;
+          j -= 32;
+        }
+        if (!ok && lane == 0 && err) atomicOr(err, 8);
+        if (lane == 0) atomicExch(status + c, kScanInc | (prefix + agg));
+      }
+      if (lane == 0) {
+        s_base = (long long)prefix;
+        if (c == n_chunks - 1) offset[rows] = offset[rows_cap] = (int64_t)(prefix + agg);
+      }
+    }
+    __syncthreads();
+    if (r < rows) {
+      int64_t start = s_base;
+      for (int k = 0; k < wib; ++k) start += s_cnt[k];
+      if (lane == 0) offset[r] = start;
+      warp_write_samples(T, w, H, r, tail, nxt, lane, pts_idx, min_depth, max_depth, probs, steps,
+                         ray_start, ray_start_stride, ray_dir, ray_index, start, start + s_cnt[wib],
+                         sample_cap, vox, xyzd, depth, err);
+    }
+    __syncthreads();                      // tables and s_cnt are reused by the next chunk
+  }
 }
 
 // Uniform sampler (fairnr/clib/src/sample_gpu.cu:15-106): merge interval
@@ -943,6 +1093,61 @@ int nsvf_sample_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max
                                     max_depth, probs, steps, nullptr, 0, ray_start,
                                     ray_start_stride, ray_dir, ray_index, offset, sample_cap,
                                     voxel, xyz_dist, depth, err, stream);
+}
+
+int64_t nsvf_sample_scan_bytes(int64_t rows_cap) {
+  if (rows_cap < 0) return 0;
+  return (int64_t)sizeof(unsigned long long) * (2 + (rows_cap + kWarpRays - 1) / kWarpRays);
+}
+
+int nsvf_sample_scan_compact_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                                    const int32_t *pts_idx, const float *min_depth,
+                                    const float *max_depth, const float *probs,
+                                    const float *steps, const int64_t *piece_rows, int max_pieces,
+                                    const float *ray_start, int64_t ray_start_stride,
+                                    const float *ray_dir, const int64_t *ray_index,
+                                    int64_t *offset, int64_t sample_cap, int32_t *voxel,
+                                    float *xyz_dist, float *depth, void *scan_ws,
+                                    int64_t scan_ws_bytes, int32_t *err, void *stream) {
+  if (rows_cap < 0 || max_hits < 1 || max_hits > kMaxH || !n_rows_dev || sample_cap < 0 ||
+      (ray_start_stride != 0 && ray_start_stride != 3) || max_pieces < 0 ||
+      (max_pieces > 0 && !piece_rows))
+    return NSVF_ERR_INVALID;
+  if (!offset) return NSVF_ERR_INVALID;
+  if (rows_cap == 0) {
+    return cudaMemsetAsync(offset, 0, sizeof(int64_t), (cudaStream_t)stream) == cudaSuccess
+               ? NSVF_OK : NSVF_ERR_CUDA;
+  }
+  if (!pts_idx || !min_depth || !max_depth || !probs || !steps || !ray_start || !ray_dir ||
+      !voxel || !xyz_dist || !depth || !scan_ws || (((uintptr_t)xyz_dist) & 15) ||
+      (((uintptr_t)scan_ws) & 7))
+    return NSVF_ERR_INVALID;
+  const int64_t need = nsvf_sample_scan_bytes(rows_cap);
+  if (scan_ws_bytes < need) return NSVF_ERR_CAPACITY;
+  if (cudaMemsetAsync(scan_ws, 0, (size_t)need, (cudaStream_t)stream) != cudaSuccess)
+    return NSVF_ERR_CUDA;
+  const int64_t *pr = max_pieces > 0 ? piece_rows : nullptr;
+  icdf_scan_kernel<<<warp_grid(rows_cap) < 8 * scan_sms() ? warp_grid(rows_cap) : 8 * scan_sms(),
+                     32 * kWarpRays, 0, (cudaStream_t)stream>>>(
+      rows_cap, max_hits, pts_idx, min_depth, max_depth, probs, steps, n_rows_dev, ray_start,
+      ray_start_stride, ray_dir, ray_index, offset, sample_cap, voxel, (float4 *)xyz_dist, depth,
+      (unsigned long long *)scan_ws, err, pr, max_pieces);
+  return nsvf_launch_status();
+}
+
+int nsvf_sample_scan_compact_dev(int64_t rows_cap, const int64_t *n_rows_dev, int max_hits,
+                                 const int32_t *pts_idx, const float *min_depth,
+                                 const float *max_depth, const float *probs, const float *steps,
+                                 const float *ray_start, int64_t ray_start_stride,
+                                 const float *ray_dir, const int64_t *ray_index, int64_t *offset,
+                                 int64_t sample_cap, int32_t *voxel, float *xyz_dist, float *depth,
+                                 void *scan_ws, int64_t scan_ws_bytes, int32_t *err,
+                                 void *stream) {
+  return nsvf_sample_scan_compact_pieces(rows_cap, n_rows_dev, max_hits, pts_idx, min_depth,
+                                         max_depth, probs, steps, nullptr, 0, ray_start,
+                                         ray_start_stride, ray_dir, ray_index, offset, sample_cap,
+                                         voxel, xyz_dist, depth, scan_ws, scan_ws_bytes, err,
+                                         stream);
 }
 
 int nsvf_uniform_ray_sampling(int b, int m, int max_hits, int max_steps, float step_size,

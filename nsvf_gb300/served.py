@@ -9,9 +9,11 @@ For one frame of rays of a resident scene:
    (on a torch prefix sum of the hit flags)
 3. nsvf_gather_probs          -- the hit rays' lists and their sampling
    distribution (fairnr/models/nsvf.py:65-74), warp per ray
-4. nsvf_sample_count_dev / nsvf_sample_compact_dev -- the inverse-CDF walk
-   (deterministic jitter, the reference's launch layout) writing only the
-   valid samples, compacted per ray
+4. nsvf_sample_scan_compact_dev -- the inverse-CDF walk (deterministic
+   jitter, the reference's launch layout) writing only the valid samples,
+   compacted per ray: counts, their prefix sum and the samples in one pass
+   (nsvf_sample_count_dev, a prefix sum and nsvf_sample_compact_dev where
+   the host needs the sample count before the field runs)
 5. nsvf_field_samples_bf16    -- corner-embedding interpolation fused into the
                                  tcgen05 BF16 field MLP (FP32 accumulation);
                                  embeddings and activations stay on chip
@@ -144,6 +146,7 @@ def _frame_buffers(scene, R, stream):
          "n_hit": e(1, dtype=i64), "I": e(R, H, dtype=i32), "L": e(R, H), "U": e(R, H),
          "probs": e(R, H), "steps": e(R), "count": e(R, dtype=i32),
          "offset": torch.zeros(R + 1, dtype=i64, device=dev),
+         "scan_ws": torch.empty(int(LIB.nsvf_sample_scan_bytes(R)), dtype=torch.uint8, device=dev),
          "ws": ext._svo_workspace(1, scene.octree_centers.shape[0], dev),
          "bg": torch.tensor(list(scene.bg), dtype=torch.float32, device=dev),
          "err": torch.zeros(1, dtype=i32, device=dev),
@@ -221,6 +224,17 @@ def _exact_pass(scene, b, R, ro, rd, vox, xyzd, depth, field, err, stream, cap, 
               "field_refine_fp32_dev")
 
 
+def _scan_compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, err, stream):
+    """Counts, offsets and samples of the hit rays in one pass."""
+    dev = scene.device
+    with ext._timed("sample_scan_compact", dev):
+        check(LIB.nsvf_sample_scan_compact_dev(
+            R, _p(b["n_hit"]), scene.max_hits, _p(b["I"]), _p(b["L"]), _p(b["U"]), _p(b["probs"]),
+            _p(b["steps"]), _p(ro), 3, _p(rd), _p(b["pix"]), _p(b["offset"]), cap, _p(vox),
+            _p(xyzd), _p(depth), _p(b["scan_ws"]), b["scan_ws"].numel(), err, stream),
+            "sample_scan_compact_dev")
+
+
 def _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, err, stream):
     dev = scene.device
     with ext._timed("sample_compact", dev):
@@ -228,6 +242,20 @@ def _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, err, stream):
                                           _p(b["U"]), _p(b["probs"]), _p(b["steps"]), _p(ro), 3,
                                           _p(rd), _p(b["pix"]), _p(b["offset"]), cap, _p(vox),
                                           _p(xyzd), _p(depth), err, stream), "sample_compact_dev")
+
+
+# Rows up to this many hit slots take the one-pass count + compaction.
+SCAN_MAX_HITS = 128
+
+
+def _count(scene, b, R, stream):
+    """Per-hit-ray sample counts and their prefix sum into b["offset"]."""
+    dev = scene.device
+    with ext._timed("sample_count", dev):
+        check(LIB.nsvf_sample_count_dev(R, _p(b["n_hit"]), scene.max_hits, _p(b["I"]), _p(b["L"]),
+                                        _p(b["U"]), _p(b["probs"]), _p(b["steps"]), _p(b["count"]),
+                                        stream), "sample_count_dev")
+    torch.cumsum(b["count"], 0, out=b["offset"][1:])
 
 
 def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, exact, stream):
@@ -250,7 +278,11 @@ def _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, exact, stream):
         err.zero_()
         if exact:
             n_outl.zero_()
-        _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, _p(err), stream)
+        if scene.max_hits <= SCAN_MAX_HITS:
+            _scan_compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, _p(err), stream)
+        else:
+            _count(scene, b, R, stream)
+            _compact(scene, b, R, ro, rd, cap, vox, xyzd, depth, _p(err), stream)
         ns_dev = _p(b["offset"][R:])
         common = (_p(vox), _p(xyzd), scene.centers.size(0), scene.values.size(0), scene.voxel_size,
                   _p(scene.centers), _p(scene.feats), _p(scene.values))
@@ -363,17 +395,13 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
                                     _p(b["idx"]), _p(b["lo"]), _p(b["hi"]), _p(b["I"]), _p(b["L"]),
                                     _p(b["U"]), _p(b["probs"]), _p(b["steps"]), stream),
               "gather_probs")
-    with ext._timed("sample_count", dev):
-        check(LIB.nsvf_sample_count_dev(R, _p(b["n_hit"]), H, _p(b["I"]), _p(b["L"]), _p(b["U"]),
-                                        _p(b["probs"]), _p(b["steps"]), _p(b["count"]), stream),
-              "sample_count_dev")
-    offset = b["offset"]
-    torch.cumsum(b["count"], 0, out=offset[1:])
     out["colors"].copy_(b["bg"].expand(R, 3))
     out["depths"].fill_(scene.bg_depth)
     out["missed"].fill_(1.0)
     if mlp in ("tc", "tc_fp8"):
         return _samples_on_device(scene, b, R, ro, rd, out, mlp, kahan, exact, stream)
+    _count(scene, b, R, stream)
+    offset = b["offset"]
     counts = b["counts_host"]
     counts[0:1].copy_(b["n_hit"], non_blocking=True)
     counts[1:2].copy_(offset[R:], non_blocking=True)

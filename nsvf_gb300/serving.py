@@ -15,9 +15,10 @@ launches with each other and with the tails of large ones.
   3. order-preserving hit compaction (torch cumsum + `nsvf_compact_hits`) and
      each piece's hit-row range (`nsvf_piece_rows`);
   4. the hit rays' lists and sampling distribution (`nsvf_gather_probs`);
-  5. inverse-CDF sample count, offsets and compaction with a launch layout of
-     its own per piece (`nsvf_sample_count_pieces`,
-     `nsvf_sample_compact_pieces`), so a piece renders the same whatever else
+  5. inverse-CDF sample count, offsets and compaction in one pass with a
+     launch layout of its own per piece (`nsvf_sample_scan_compact_pieces`;
+     `nsvf_sample_count_pieces` + `nsvf_sample_compact_pieces` for more than
+     128 hit slots), so a piece renders the same whatever else
      shares its chunk;
   6. interpolation + tcgen05 BF16 MLP on the device-side sample count (`nsvf_field_samples_bf16_dev`),
      then the double-float re-evaluation of the samples far outside their voxel (`nsvf_field_exact_dev`)
@@ -132,6 +133,7 @@ class ChunkPipeline:
         self.refine_rows = z(self.outl_cap, dtype=i64)
         self.n_refine = z(1, dtype=i64)
         self.ws = torch.empty(self._ws_bytes(scene, C), dtype=u8, device=dev)
+        self.scan_ws = torch.empty(int(LIB.nsvf_sample_scan_bytes(C)), dtype=u8, device=dev)
         self.bg = torch.tensor(list(scene.bg), device=dev)
         self.graph = None
         self.use_graph = use_graph
@@ -144,7 +146,7 @@ class ChunkPipeline:
         outl = max(4096, cap // 1024)
         per_ray = 24 + 12 * H + 1 + 4 + 8 + 16 * H + 4 + 4 + 8 + 20
         return C * per_ray + cap * 40 + outl * 16 + ChunkPipeline._ws_bytes(scene, C) + \
-            MAX_PIECES * 80 + 64
+            int(LIB.nsvf_sample_scan_bytes(C)) + MAX_PIECES * 80 + 64
 
     @staticmethod
     def _ws_bytes(scene, C):
@@ -182,16 +184,26 @@ class ChunkPipeline:
         check(LIB.nsvf_gather_probs(C, _p(self.n_hit), H, sc.step_size, _p(self.pix), _p(self.idx),
                                     _p(self.lo), _p(self.hi), _p(self.I), _p(self.L), _p(self.U),
                                     _p(self.probs), _p(self.steps), s), "gather_probs")
-        check(LIB.nsvf_sample_count_pieces(C, _p(self.n_hit), H, _p(self.I), _p(self.L), _p(self.U),
-                                           _p(self.probs), _p(self.steps), _p(self.piece_rows),
-                                           MAX_PIECES, _p(self.count), s), "sample_count_pieces")
-        torch.cumsum(self.count, 0, out=self.offset[1:])
-        check(LIB.nsvf_sample_compact_pieces(C, _p(self.n_hit), H, _p(self.I), _p(self.L),
-                                             _p(self.U), _p(self.probs), _p(self.steps),
-                                             _p(self.piece_rows), MAX_PIECES, _p(self.ro), 3,
-                                             _p(self.rd), _p(self.pix), _p(self.offset), self.cap,
-                                             _p(self.vox), _p(self.xyzd), _p(self.sdepth),
-                                             _p(self.err), s), "sample_compact_pieces")
+        if H <= 128:
+            check(LIB.nsvf_sample_scan_compact_pieces(
+                C, _p(self.n_hit), H, _p(self.I), _p(self.L), _p(self.U), _p(self.probs),
+                _p(self.steps), _p(self.piece_rows), MAX_PIECES, _p(self.ro), 3, _p(self.rd),
+                _p(self.pix), _p(self.offset), self.cap, _p(self.vox), _p(self.xyzd),
+                _p(self.sdepth), _p(self.scan_ws), self.scan_ws.numel(), _p(self.err), s),
+                "sample_scan_compact_pieces")
+        else:
+            check(LIB.nsvf_sample_count_pieces(C, _p(self.n_hit), H, _p(self.I), _p(self.L),
+                                               _p(self.U), _p(self.probs), _p(self.steps),
+                                               _p(self.piece_rows), MAX_PIECES, _p(self.count), s),
+                  "sample_count_pieces")
+            torch.cumsum(self.count, 0, out=self.offset[1:])
+            check(LIB.nsvf_sample_compact_pieces(C, _p(self.n_hit), H, _p(self.I), _p(self.L),
+                                                 _p(self.U), _p(self.probs), _p(self.steps),
+                                                 _p(self.piece_rows), MAX_PIECES, _p(self.ro), 3,
+                                                 _p(self.rd), _p(self.pix), _p(self.offset),
+                                                 self.cap, _p(self.vox), _p(self.xyzd),
+                                                 _p(self.sdepth), _p(self.err), s),
+                  "sample_compact_pieces")
         m = sc.mlp
         self.n_outl.zero_()
         self.n_refine.zero_()

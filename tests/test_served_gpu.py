@@ -267,3 +267,76 @@ def test_host_frames_match_render_frame(cuda):
     pipe.render([(h[0], h[1]) + ring[i % 2] for i, h in enumerate(host)])
     assert torch.equal(ring[0][0], refs[4][0]) and torch.equal(ring[1][0], refs[3][0])
     assert pipe.n_samples > 0
+
+
+@pytest.mark.parametrize("rows", [0, 1, 13, None])
+def test_scan_compact_equals_two_pass(cuda, rows):
+    """nsvf_sample_scan_compact_dev (counts, prefix sum and samples in one
+    pass with a look-back between blocks) against the count pass, a prefix
+    sum and the compaction pass on the hit rows of a served frame: offsets
+    and samples equal bit for bit, for 0, 1 and 13 rows (a partial block) and
+    all ~20k hit rows; with too small a sample buffer both set error bit 2,
+    report the same total and write the same samples up to the capacity."""
+    from nsvf_gb300 import ext, scenes, served
+    from nsvf_gb300._lib import LIB
+    enc, field, ren, vs = _scene(cuda, 1.0 / 32, 1.0, 30.0, 0.5, 64)
+    rs, rd = scenes.pinhole_rays(scenes.sphere_cameras(3, 4.0, seed=9)[1], 160, 160, 200.0)
+    rs_t, rd_t = torch.from_numpy(rs).to(cuda), torch.from_numpy(rd).to(cuda)
+    scene = served.SceneState(enc, field)
+    served.render_frame(scene, rs_t, rd_t)
+    ext.check_errors(cuda)
+    b = next(iter(scene._frames.values()))
+    R, H = rd.shape[0], scene.max_hits
+    n_all = int(b["n_hit"].item())
+    assert n_all > 5000
+    n = n_all if rows is None else rows
+    n_dev = torch.tensor([n], dtype=torch.int64, device=cuda)
+    p = served._p
+    stream = ext.ctypes_stream(cuda)
+    ro = b["ro"]
+    common = (R, p(n_dev), H, p(b["I"]), p(b["L"]), p(b["U"]), p(b["probs"]), p(b["steps"]))
+    rays = (p(ro), 3, p(rd_t), p(b["pix"]))
+
+    def two_pass(cap):
+        count = torch.zeros(R, dtype=torch.int32, device=cuda)
+        off = torch.zeros(R + 1, dtype=torch.int64, device=cuda)
+        assert LIB.nsvf_sample_count_dev(*common, p(count), stream) == 0
+        torch.cumsum(count, 0, out=off[1:])
+        vox = torch.full((cap,), -7, dtype=torch.int32, device=cuda)
+        xyzd = torch.zeros(cap, 4, device=cuda)
+        depth = torch.zeros(cap, device=cuda)
+        err = torch.zeros(1, dtype=torch.int32, device=cuda)
+        assert LIB.nsvf_sample_compact_dev(*common, *rays, p(off), cap, p(vox), p(xyzd),
+                                           p(depth), p(err), stream) == 0
+        return off, vox, xyzd, depth, int(err.item())
+
+    def one_pass(cap):
+        off = torch.full((R + 1,), -5, dtype=torch.int64, device=cuda)
+        vox = torch.full((cap,), -7, dtype=torch.int32, device=cuda)
+        xyzd = torch.zeros(cap, 4, device=cuda)
+        depth = torch.zeros(cap, device=cuda)
+        err = torch.zeros(1, dtype=torch.int32, device=cuda)
+        nb = int(LIB.nsvf_sample_scan_bytes(R))
+        ws = torch.empty(nb, dtype=torch.uint8, device=cuda)
+        assert LIB.nsvf_sample_scan_compact_dev(*common, *rays, p(off), cap, p(vox), p(xyzd),
+                                                p(depth), p(ws), nb, p(err), stream) == 0
+        # too small a workspace is refused
+        assert LIB.nsvf_sample_scan_compact_dev(*common, *rays, p(off), cap, p(vox), p(xyzd),
+                                                p(depth), p(ws), nb - 8, p(err),
+                                                stream) == ext.NSVF_ERR_CAPACITY
+        return off, vox, xyzd, depth, int(err.item())
+
+    total = int(b["offset"][R].item()) if rows is None else None
+    for cap in ([max(total, 1), max(total // 2, 1)] if rows is None else [R * 64]):
+        o2, v2, x2, d2, e2 = two_pass(cap)
+        o1, v1, x1, d1, e1 = one_pass(cap)
+        tot = int(o2[R].item())
+        assert int(o1[R].item()) == tot
+        assert torch.equal(o1[:n + 1], o2[:n + 1])
+        if rows is None:
+            assert tot == total
+        assert e1 == e2 == (2 if tot > cap else 0)
+        k = min(tot, cap)
+        assert torch.equal(v1[:k], v2[:k]) and torch.equal(d1[:k], d2[:k])
+        assert torch.equal(x1[:k], x2[:k])
+        assert bool((v1[k:] == -7).all())
