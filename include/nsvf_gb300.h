@@ -128,6 +128,20 @@ int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
                             const int32_t *children, const void *grid, const int32_t *info,
                             const void *packed, void *list_ws, int32_t *idx, float *min_depth,
                             float *max_depth, uint8_t *hits, int32_t *err, void *stream);
+/* svo_intersect_grid_rows: nsvf_svo_intersect_grid with pad_rows = 1; with
+ * pad_rows = 0 the rows of rays the sweep finishes are not padded: a hit
+ * ray's row ends with one -1 after its last hit (when it has fewer than
+ * n_max), a missed ray's row is not written (hits[r] = 0), and slots past
+ * the -1 keep what they held. Rows of overflow rays and of rays listed for
+ * the depth-first search are complete. For readers that stop at a row's
+ * first -1, such as nsvf_gather_probs: the rows' padding is most of the
+ * call's writes (12 * n_max bytes per missed ray). */
+int nsvf_svo_intersect_grid_rows(int64_t rays, int n, float voxelsize, int n_max,
+                                 const float *ray_start, const float *ray_dir,
+                                 const float *points, const int32_t *children, const void *grid,
+                                 const int32_t *info, const void *packed, void *list_ws,
+                                 int32_t *idx, float *min_depth, float *max_depth, uint8_t *hits,
+                                 int32_t *err, int pad_rows, void *stream);
 
 /* svo_intersect_noalloc: has no counterpart in the reference. The same
  * computation and outputs as nsvf_svo_intersect, for callers that cannot
@@ -416,7 +430,9 @@ int nsvf_ray_probs(int64_t rows, int max_hits, float step_size, const int32_t *i
 /* gather_probs: for rows i < *n_hit, copies the sorted hit list of ray pix[i]
  * ([., max_hits] idx/min/max) and builds its sampling distribution exactly as
  * nsvf_ray_probs does (same sum order, same roundings), so the served chain
- * samples exactly the drop-in path's samples. */
+ * samples exactly the drop-in path's samples. A row is read up to its first
+ * -1 (rows of nsvf_svo_intersect_grid_rows without padding); the copies are
+ * padded with id -1 and depths 10000 either way. */
 int nsvf_gather_probs(int64_t cap, const int64_t *n_hit, int max_hits, float step_size,
                       const int64_t *pix, const int32_t *idx, const float *min_depth,
                       const float *max_depth, int32_t *out_idx, float *out_min, float *out_max,

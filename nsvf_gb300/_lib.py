@@ -39,6 +39,8 @@ def _load():
         "nsvf_svo_grid_list_bytes": ([i64], i64),
         "nsvf_svo_intersect_grid": ([i64, i32, f32, i32, P, P, P, P, P, P, P, P, P, P, P, P, P,
                                      P], i32),
+        "nsvf_svo_intersect_grid_rows": ([i64, i32, f32, i32, P, P, P, P, P, P, P, P, P, P, P, P,
+                                          P, i32, P], i32),
         "nsvf_ball_intersect": ([i32, i32, i32, i32, f32, i32, P, P, P, P, P, P, P], i32),
         "nsvf_triangle_intersect": ([i32, i32, i32, i32, f32, f32, i32, P, P, P, P, P, P, P], i32),
         "nsvf_uniform_ray_sampling": ([i32, i32, i32, i32, f32, P, P, P, P, P, P, P, P, P], i32),
@@ -117,7 +119,7 @@ def exported_symbols():
         "nsvf_status_string", "nsvf_launch_count", "nsvf_aabb_intersect", "nsvf_svo_workspace_bytes",
         "nsvf_svo_intersect", "nsvf_svo_intersect_sorted", "nsvf_svo_pack",
         "nsvf_svo_grid_build", "nsvf_svo_grid_info", "nsvf_svo_grid_list_bytes",
-        "nsvf_svo_intersect_grid", "nsvf_ball_intersect",
+        "nsvf_svo_intersect_grid", "nsvf_svo_intersect_grid_rows", "nsvf_ball_intersect",
         "nsvf_triangle_intersect",
         "nsvf_uniform_ray_sampling", "nsvf_inverse_cdf_sampling", "nsvf_build_octree",
         "nsvf_trilinear_embed", "nsvf_trilinear_embed_backward", "nsvf_composite",

@@ -180,7 +180,11 @@ __global__ void __launch_bounds__(kBlock) ray_probs_kernel(
 }
 
 // Warp per row i < *n_hit: copy the hit list of ray pix[i] and build its
-// sampling distribution with row_total (the drop-in path's sum order).
+// sampling distribution with row_total's sum order (the drop-in path's).
+// The row is read up to its first -1 only, so it may end there (rows of the
+// unpadded leaf-grid sweep): the copy is padded like the sweep pads its rows
+// (id -1, depths 10000) and the padded slots' terms (+0) leave the sum
+// unchanged, so padded and unpadded rows give the same bits.
 __global__ void __launch_bounds__(kBlock) gather_probs_kernel(
     int64_t cap, const int64_t *__restrict__ n_hit, int H, float step,
     const int64_t *__restrict__ pix, const int32_t *__restrict__ idx,
@@ -194,12 +198,26 @@ __global__ void __launch_bounds__(kBlock) gather_probs_kernel(
     const int64_t r = pix[i];
     const int32_t *ir = idx + r * H;
     const float *lr = lo + r * H, *hr = hi + r * H;
-    const float tot = row_total(ir, lr, hr, H, lane);
+    // the valid slots: before the row's first -1
+    int cnt = H;
+    for (int base = 0; base < H; base += 32) {
+      const bool end = base + lane < H && ir[base + lane] == -1;
+      const unsigned m = __ballot_sync(0xffffffffu, end);
+      if (m) { cnt = base + __ffs(m) - 1; break; }
+    }
+    float tot = 0.0f;
+    for (int base = 0; base < cnt; base += 32) {
+      const float dv = base + lane < cnt ? __fsub_rn(hr[base + lane], lr[base + lane]) : 0.0f;
+      const int m = cnt - base < 32 ? cnt - base : 32;
+      for (int j = 0; j < m; ++j) tot = __fadd_rn(tot, __shfl_sync(0xffffffffu, dv, j));
+    }
     for (int k = lane; k < H; k += 32) {
-      I[i * H + k] = ir[k];
-      L[i * H + k] = lr[k];
-      U[i * H + k] = hr[k];
-      probs[i * H + k] = __fdiv_rn(slot_d(ir, lr, hr, k), tot);
+      const bool v = k < cnt;
+      const float a = v ? lr[k] : NSVF_MAX_DEPTH_F, b = v ? hr[k] : NSVF_MAX_DEPTH_F;
+      I[i * H + k] = v ? ir[k] : -1;
+      L[i * H + k] = a;
+      U[i * H + k] = b;
+      probs[i * H + k] = __fdiv_rn(v ? __fsub_rn(b, a) : 0.0f, tot);
     }
     if (lane == 0) steps[i] = __fdiv_rn(tot, step);
   }

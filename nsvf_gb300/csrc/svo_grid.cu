@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(kGridBlock) svo_grid_kernel(
     float *__restrict__ min_depth, float *__restrict__ max_depth, uint8_t *__restrict__ hits,
     int32_t *__restrict__ list, int32_t *__restrict__ n_list, int32_t *__restrict__ over,
     int32_t *__restrict__ over_cnt, int32_t *__restrict__ n_over, OverHit *__restrict__ scratch,
-    int over_cap, unsigned long long *__restrict__ next_ray) {
+    int over_cap, unsigned long long *__restrict__ next_ray, bool pad_rows) {
   // Persistent warps: each warp takes the next 32 rays from a global
   // counter until there are none left, so the SMs stay full to the end of
   // the frame (rays differ a lot in length: fixed blocks left the SMs active
@@ -595,6 +595,13 @@ __global__ void __launch_bounds__(kGridBlock) svo_grid_kernel(
       list[atomicAdd(n_list, 1)] = (int32_t)r;
     } else if (live && em.q < 0) {
       hits[r] = em.cnt > 0;
+    }
+    if (!pad_rows) {
+      // rows end at their first -1: a hit ray's row gets one after its last
+      // hit (when it has room), a missed ray's row is not written
+      if (live && st == kSweepDone && em.q < 0 && em.cnt > 0 && em.cnt < n_max)
+        idx[r * n_max + em.cnt] = -1;
+      continue;
     }
     // pad the rows (misses: id -1, depths 10000), a warp per row
     const bool pad = live && st == kSweepDone && em.q < 0;
@@ -754,11 +761,12 @@ int64_t nsvf_svo_grid_list_bytes(int64_t rays) {
   return blk_off + oc * kOverExtra * (int64_t)sizeof(OverHit);
 }
 
-int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
-                            const float *ray_start, const float *ray_dir, const float *points,
-                            const int32_t *children, const void *grid, const int32_t *info,
-                            const void *packed, void *list_ws, int32_t *idx, float *min_depth,
-                            float *max_depth, uint8_t *hits, int32_t *err, void *stream) {
+int nsvf_svo_intersect_grid_rows(int64_t rays, int n, float voxelsize, int n_max,
+                                 const float *ray_start, const float *ray_dir,
+                                 const float *points, const int32_t *children, const void *grid,
+                                 const int32_t *info, const void *packed, void *list_ws,
+                                 int32_t *idx, float *min_depth, float *max_depth, uint8_t *hits,
+                                 int32_t *err, int pad_rows, void *stream) {
   if (!info || info[5] != n || info[0] < 1 || info[1] < 1 || info[2] < 1 || info[3] < 1)
     return NSVF_ERR_INVALID;
   if (rays < 0 || n < 1 || n_max < 1 || !points || !children || !grid || !packed || !list_ws ||
@@ -819,7 +827,7 @@ int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
   svo_grid_kernel<<<blocks, kGridBlock, 0, s>>>(rays, n_max, ray_start, ray_dir, G, idx,
                                                 min_depth, max_depth, hits, list, n_list, over,
                                                 over_cnt, n_over, scratch, (int)over_cap,
-                                                next_ray);
+                                                next_ray, pad_rows != 0);
   st = nsvf_launch_status();
   if (st != NSVF_OK) return st;
   // the overflow rays: their count is on the device; 8 blocks of 4 warps per
@@ -833,6 +841,16 @@ int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
   if (st != NSVF_OK) return st;
   return nsvf_svo_sorted_list_launch(rays, rays, n, n_max, ray_start, ray_dir, packed, list,
                                      n_list, idx, min_depth, max_depth, hits, err, s);
+}
+
+int nsvf_svo_intersect_grid(int64_t rays, int n, float voxelsize, int n_max,
+                            const float *ray_start, const float *ray_dir, const float *points,
+                            const int32_t *children, const void *grid, const int32_t *info,
+                            const void *packed, void *list_ws, int32_t *idx, float *min_depth,
+                            float *max_depth, uint8_t *hits, int32_t *err, void *stream) {
+  return nsvf_svo_intersect_grid_rows(rays, n, voxelsize, n_max, ray_start, ray_dir, points,
+                                      children, grid, info, packed, list_ws, idx, min_depth,
+                                      max_depth, hits, err, 1, stream);
 }
 
 }  // extern "C"

@@ -256,17 +256,20 @@ class SvoGrid:
         return ws
 
     def intersect_into(self, R, n_max, ro, rd, idx, lo, hi, hits, stream, list_ws=None,
-                       err=None):
+                       err=None, padded=True):
         """nsvf_svo_intersect_grid on raw device pointers (R rays); `err` (a
-        device int32 tensor) defaults to the device's error word."""
+        device int32 tensor) defaults to the device's error word. padded=False
+        (nsvf_svo_intersect_grid_rows): a row ends at its first -1 and missed
+        rays' rows are not written (for readers that stop there, such as
+        nsvf_gather_probs)."""
         ws = list_ws if list_ws is not None else self.list_workspace(R, self.grid.device)
         if err is None:
             err = error_word(self.grid.device)
-        check(LIB.nsvf_svo_intersect_grid(
+        check(LIB.nsvf_svo_intersect_grid_rows(
             R, self.n, self.voxel_size, int(n_max), ro, rd, _ptr(self.centers),
             _ptr(self.children), _ptr(self.grid), self.info.ctypes.data, _ptr(self.packed),
             _ptr(ws), idx, lo, hi, hits,
-            _ptr(err), stream), "svo_intersect_grid")
+            _ptr(err), int(bool(padded)), stream), "svo_intersect_grid_rows")
 
 
 def svo_intersect_grid(grid, ray_start, ray_dir, n_max):

@@ -378,8 +378,9 @@ def render_frame(scene, ray_start, ray_dir, kahan=True, out=None, mlp="tc", exac
     n_nodes = scene.octree_centers.shape[0]
     if traversal == "grid" and scene.svo_grid.ok:
         with ext._timed("svo_intersect_grid", dev):
+            # rows end at their first -1: nsvf_gather_probs reads no further
             scene.svo_grid.intersect_into(R, H, _p(ro), _p(rd), _p(b["idx"]), _p(b["lo"]),
-                                          _p(b["hi"]), _p(b["hits"]), stream)
+                                          _p(b["hi"]), _p(b["hits"]), stream, padded=False)
     else:
         with ext._timed("svo_intersect_sorted", dev):
             check(LIB.nsvf_svo_intersect_sorted(1, 1, n_nodes, R, scene.voxel_size, H, _p(ro),

@@ -168,7 +168,7 @@ class ChunkPipeline:
         if sc.svo_grid.ok:
             sc.svo_grid.intersect_into(C, H, _p(self.ro), _p(self.rd), _p(self.idx), _p(self.lo),
                                        _p(self.hi), _p(self.hits), s, list_ws=self.ws,
-                                       err=self.err)
+                                       err=self.err, padded=False)
         else:
             check(LIB.nsvf_svo_intersect_sorted(1, 1, sc.octree_centers.shape[0], C,
                                                 sc.voxel_size, H, _p(self.ro), _p(self.rd),

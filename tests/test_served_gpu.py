@@ -129,7 +129,8 @@ def test_probs_slot_order(cuda, H):
     """nsvf_gather_probs and nsvf_ray_probs, bit for bit: d = max - min on hit
     slots, tot = d_0 + d_1 + ... one slot at a time in slot order (FP32),
     probs = d / tot, steps = tot / step; the oracle's probs_steps is the same
-    sequential sum."""
+    sequential sum. gather_probs reads a row up to its first -1 and pads its
+    copy like the traversals pad their rows (depths 10000)."""
     from nsvf_gb300 import ext
     from nsvf_gb300._lib import LIB
     from oracle import cpu
@@ -163,8 +164,10 @@ def test_probs_slot_order(cuda, H):
                                  U.data_ptr(), probs.data_ptr(), steps.data_ptr(),
                                  ext.ctypes_stream(cuda)) == 0
     assert np.array_equal(I[:n].cpu().numpy(), idx[pix])
-    assert np.array_equal(L[:n].cpu().numpy(), lo[pix])
-    assert np.array_equal(U[:n].cpu().numpy(), hi[pix])
+    # slots past a row's first -1 are copied as the traversals pad them
+    pad = idx[pix] == -1
+    assert np.array_equal(L[:n].cpu().numpy(), np.where(pad, np.float32(10000), lo[pix]))
+    assert np.array_equal(U[:n].cpu().numpy(), np.where(pad, np.float32(10000), hi[pix]))
     assert np.array_equal(probs[:n].cpu().numpy(), d / tot)
     assert np.array_equal(steps[:n].cpu().numpy(), tot[:, 0] / step)
 

@@ -93,6 +93,59 @@ def _plane_rays(n, seed, vs):
     return o.astype(np.float32), d.astype(np.float32)
 
 
+@pytest.mark.parametrize("n_max", [64, 8])
+def test_unpadded_rows_gather_the_same(c2, cuda, n_max):
+    """nsvf_svo_intersect_grid_rows without padding (the served chain's form)
+    on the c2 frame: hit flags equal; a hit ray's row holds the padded call's
+    hits and then a -1; a missed ray's row is not written; and
+    nsvf_gather_probs turns both forms into the same bits (n_max 8: rows of
+    overflow and listed rays, which are complete either way)."""
+    from nsvf_gb300 import ext
+    from nsvf_gb300._lib import LIB
+    g = _grid(c2, cuda)
+    o, d = workload.frame(0)
+    R = d.shape[0]
+    ro = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(o, d.shape), np.float32)).to(cuda)
+    rd = torch.from_numpy(d).to(cuda)
+    ref = ext.svo_intersect_grid(g, ro, rd, n_max)
+    idx = torch.full((R, n_max), 7777, dtype=torch.int32, device=cuda)
+    lo = torch.full((R, n_max), float("nan"), device=cuda)
+    hi = torch.full((R, n_max), float("nan"), device=cuda)
+    hits = torch.full((R,), 9, dtype=torch.uint8, device=cuda)
+    stream = ext.ctypes_stream(cuda)
+    g.intersect_into(R, n_max, ro.data_ptr(), rd.data_ptr(), idx.data_ptr(), lo.data_ptr(),
+                     hi.data_ptr(), hits.data_ptr(), stream, padded=False)
+    ext.check_errors(cuda)
+    r_idx = ref[0].reshape(R, n_max)
+    assert torch.equal(hits, ref[3].reshape(R).to(torch.uint8))
+    cnt = (r_idx != -1).sum(1)
+    hit = hits.bool()
+    assert int(hit.sum()) > 100000
+    valid = torch.arange(n_max, device=cuda)[None, :] < cnt[:, None]
+    assert torch.equal(idx[valid], r_idx[valid])
+    assert torch.equal(lo[valid], ref[1].reshape(R, n_max)[valid])
+    assert torch.equal(hi[valid], ref[2].reshape(R, n_max)[valid])
+    term = hit & (cnt < n_max)
+    assert bool((idx[term, :].gather(1, cnt[term, None]) == -1).all())
+    assert bool((idx[~hit] == 7777).all())
+    pix = torch.nonzero(hit).reshape(-1)
+    n_hit = torch.tensor([pix.numel()], dtype=torch.int64, device=cuda)
+
+    def gathered(i_, l_, h_):
+        n = pix.numel()
+        out = [torch.empty(n, n_max, dtype=torch.int32, device=cuda)] + \
+            [torch.empty(n, n_max, device=cuda) for _ in range(3)] + [torch.empty(n, device=cuda)]
+        assert LIB.nsvf_gather_probs(n, n_hit.data_ptr(), n_max, 1.0 / 512, pix.data_ptr(),
+                                     i_.data_ptr(), l_.data_ptr(), h_.data_ptr(),
+                                     *[t.data_ptr() for t in out], stream) == 0
+        return out
+
+    a = gathered(*(t.reshape(R, n_max).contiguous() for t in ref[:3]))
+    b = gathered(idx, lo, hi)
+    for x, y in zip(a, b):
+        assert np.array_equal(_bits(_np(x)), _bits(_np(y)))
+
+
 @pytest.mark.parametrize("case", ["camera", "inside", "planes", "small_n_max"])
 def test_c2_matches_dfs_kernel(c2, cuda, case):
     g = _grid(c2, cuda)
