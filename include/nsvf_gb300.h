@@ -477,7 +477,7 @@ int nsvf_sample_compact_pieces(int64_t rows_cap, const int64_t *n_rows_dev, int 
 
 /* sample_scan_compact_dev / _pieces: nsvf_sample_count_dev (or _pieces),
  * the exclusive prefix sum of the counts into offset, and
- * nsvf_sample_compact_dev (or _pieces) in one pass. Blocks of 8 rows take
+ * nsvf_sample_compact_dev (or _pieces) in one pass. Blocks of 4 rows take
  * their rows in ticket order and find their first sample by a look-back over
  * the earlier blocks' published counts. The outputs are those of the three
  * steps: the same samples at the same positions, offset[r] for r < *n_rows_dev
