@@ -272,6 +272,63 @@ def test_host_frames_match_render_frame(cuda):
     assert pipe.n_samples > 0
 
 
+@pytest.mark.parametrize("pieces", [[0], [0, 5, 1000], [0, 2047, 2048, 4000, 6000]])
+def test_scan_compact_pieces_equals_two_pass(cuda, pieces):
+    """nsvf_sample_scan_compact_pieces against nsvf_sample_count_pieces, a
+    prefix sum and nsvf_sample_compact_pieces on a served frame's hit rows
+    cut into pieces (each with the reference's launch layout for its own row
+    count, as the serving chunks use them): offsets and samples equal bit for
+    bit, including a one-row piece and pieces that end past the rows."""
+    from nsvf_gb300 import ext, scenes, served
+    from nsvf_gb300._lib import LIB
+    enc, field, ren, vs = _scene(cuda, 1.0 / 32, 1.0, 30.0, 0.5, 64)
+    rs, rd = scenes.pinhole_rays(scenes.sphere_cameras(3, 4.0, seed=9)[1], 160, 160, 200.0)
+    rs_t, rd_t = torch.from_numpy(rs).to(cuda), torch.from_numpy(rd).to(cuda)
+    scene = served.SceneState(enc, field)
+    served.render_frame(scene, rs_t, rd_t)
+    ext.check_errors(cuda)
+    b = next(iter(scene._frames.values()))
+    R, H = rd.shape[0], scene.max_hits
+    n = int(b["n_hit"].item())
+    assert n > 5000
+    P = len(pieces)
+    pr = torch.tensor(pieces + [n], dtype=torch.int64, device=cuda)
+    p = served._p
+    stream = ext.ctypes_stream(cuda)
+    common = (R, p(b["n_hit"]), H, p(b["I"]), p(b["L"]), p(b["U"]), p(b["probs"]), p(b["steps"]),
+              p(pr), P)
+    rays = (p(b["ro"]), 3, p(rd_t), p(b["pix"]))
+    cap = R * 64
+    count = torch.zeros(R, dtype=torch.int32, device=cuda)
+    o2 = torch.zeros(R + 1, dtype=torch.int64, device=cuda)
+    assert LIB.nsvf_sample_count_pieces(*common, p(count), stream) == 0
+    torch.cumsum(count, 0, out=o2[1:])
+    outs = []
+    for one_pass in (False, True):
+        vox = torch.full((cap,), -7, dtype=torch.int32, device=cuda)
+        xyzd = torch.zeros(cap, 4, device=cuda)
+        depth = torch.zeros(cap, device=cuda)
+        err = torch.zeros(1, dtype=torch.int32, device=cuda)
+        if one_pass:
+            off = torch.full((R + 1,), -5, dtype=torch.int64, device=cuda)
+            nb = int(LIB.nsvf_sample_scan_bytes(R))
+            ws = torch.empty(nb, dtype=torch.uint8, device=cuda)
+            assert LIB.nsvf_sample_scan_compact_pieces(*common, *rays, p(off), cap, p(vox), p(xyzd),
+                                                       p(depth), p(ws), nb, p(err), stream) == 0
+        else:
+            off = o2
+            assert LIB.nsvf_sample_compact_pieces(*common, *rays, p(off), cap, p(vox), p(xyzd),
+                                                  p(depth), p(err), stream) == 0
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        outs.append((off, vox, xyzd, depth))
+    (o_a, v_a, x_a, d_a), (o_b, v_b, x_b, d_b) = outs
+    tot = int(o_a[R].item())
+    assert int(o_b[R].item()) == tot > 10 ** 5
+    assert torch.equal(o_a[:n + 1], o_b[:n + 1])
+    assert torch.equal(v_a, v_b) and torch.equal(d_a, d_b) and torch.equal(x_a, x_b)
+
+
 @pytest.mark.parametrize("rows", [0, 1, 13, None])
 def test_scan_compact_equals_two_pass(cuda, rows):
     """nsvf_sample_scan_compact_dev (counts, prefix sum and samples in one
