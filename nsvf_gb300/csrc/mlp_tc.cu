@@ -101,8 +101,8 @@ struct __align__(128) MlpSmem {
   __nv_bfloat16 ain[NB][TILE * E];
   // the bias step of each layer (an extra bf16 K = 16 MMA): B rows n =
   // (hi, mid, lo, 0, ...) with hi + mid + lo = bias[l][n] / dq[l] (three
-  // bf16 terms; dq = 1 except after an FP8 layer), and, for the first layer,
-  // an A tile whose rows are (1, 1, 1, 0, ...).
+  // bf16 terms; dq = 1 except after an FP8 layer), and the A tile that every
+  // layer's bias step reads, rows (1, 1, 1, 0, ...).
   __nv_bfloat16 bias_b[4][HID * 16];
   __nv_bfloat16 ones_a[TILE * 16];
   // BF16 slot 2's activations (K-major, TILE x HID): written by the epilogue,
@@ -242,7 +242,7 @@ constexpr uint32_t kOne = 0x00003F80u, kOnes2 = 0x3F803F80u;
 // The bias step's operands (BF16), written once per CTA: row n of layer l's
 // B block is (hi, mid, lo, 0, ...) with hi = bf16(b), mid = bf16(b - hi),
 // lo = bf16(b - hi - mid) -- their sum is b to within the FP32 rounding of the
-// accumulation -- and every row of the first layer's A block is
+// accumulation -- and every row of the A block that all layers share is
 // (1, 1, 1, 0, ...). Both are no-swizzle K-major tiles with K = 16.
 __device__ __forceinline__ void stage_bias_step(__nv_bfloat16 (*bias_b)[HID * 16],
                                                 __nv_bfloat16 *ones_a,
@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(Cfg<F8>::kThreads, 1) mlp_tc_kernel(const MlpP
       const uint64_t d_w0 = sdesc(smem_u32(S.w0), 128u, (E / 8) * 128u);
       const uint64_t d_wh = sdesc(smem_u32(S.wh[0]), 128u, (F8 ? HID / 16 : HID / 8) * 128u);
       constexpr uint32_t kHidStep = C::kHidBytes / 16;
-      // the bias step: the first layer's ones block (A, shared memory) and
+      // the bias step of every layer: the ones block (A, shared memory) and
       // layer l's bias block (B; + 256 per layer)
       const uint64_t d_ones = sdesc(smem_u32(S.ones_a), 128u, 256u);
       const uint64_t d_bias = sdesc(smem_u32(S.bias_b[0]), 128u, 256u);
