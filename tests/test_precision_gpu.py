@@ -77,17 +77,18 @@ def test_error_budget_against_fp64(cuda):
     assert rep["plain_fp32"]["max_rgb_err"] <= 1e-4, rep
 
 
-@pytest.mark.parametrize("voxel", [1.0 / 64, 1.0 / 128])
-def test_full_frame_error_bar_every_pixel(cuda, voxel):
+@pytest.mark.parametrize("voxel,cam", [(1.0 / 64, 0), (1.0 / 128, 0), (1.0 / 64, 91)])
+def test_full_frame_error_bar_every_pixel(cuda, voxel, cam):
     """c2 (125,476 voxels, voxel 1/64) and c4 (500,832 voxels, voxel 1/128):
-    camera 0 at 800x800. The served BF16 frame and the served chain with the
-    FP32 field meet the 2e-3 max RGB error bar against the float64 render on
-    every pixel, including the ~0.1-0.2 % of hit pixels with a sample far
-    outside its voxel (evaluated again in double-float)."""
+    camera 0 at 800x800, and c2's camera 91 (the largest error of seven c2
+    cameras measured: 1.0e-3). The served BF16 frame and the served chain
+    with the FP32 field meet the 2e-3 max RGB error bar against the float64
+    render on every pixel, including the ~0.1-0.2 % of hit pixels with a
+    sample far outside its voxel (evaluated again in double-float)."""
     from nsvf_gb300 import scenes
     from nsvf_gb300.precision import report
     enc, field, ren, vs = _scene(cuda, voxel, 0.01, 1.0, 0.0, 64)
-    rs, rd = scenes.frame_view(0, size=800)
+    rs, rd = scenes.frame_view(cam, size=800)
     rep = report(enc, field, ren, torch.from_numpy(rs).to(cuda), torch.from_numpy(rd).to(cuda))
     print("precision report:", rep)
     assert rep["hit_pixels"] > 100000
